@@ -1,0 +1,576 @@
+// ORACLE — test infrastructure, not product code.
+//
+// A from-scratch CPU restatement of the sDbscan / sOPTICS hot path of the
+// reference (NinhPham/sDbscan), stage by stage, each function citing the
+// reference lines it follows.  Only the tests, the smoke check and the CPU
+// baseline leg of bench.py load it, and only as the checker / the timed CPU
+// arm; the product never calls it.
+//
+// Parity pin: it is checked against the reference itself (its unmodified
+// sources compiled against oracle/shim, see oracle/Makefile) through the
+// golden fixtures in tests/golden, and directly against oracle/_ref where that
+// library exists.  Numerical contract, identical to the shim's: dot products
+// and squared norms are sequential fmaf over ascending index; sums are
+// sequential adds; the Walsh-Hadamard transform is the radix-2 form with
+// ascending strides (bit-identical to the reference's fht_float).
+//
+// Portable C++17 + OpenMP: builds and gives the same bits on x86-64 and
+// aarch64 (-ffp-contract=off, explicit std::fma).
+#include <omp.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <queue>
+#include <random>
+#include <unordered_map>
+#include <unordered_set>
+#include <utility>
+#include <vector>
+
+namespace {
+
+enum Dist { D_COSINE = 0, D_L1 = 1, D_L2 = 2, D_CHI2 = 3, D_JS = 4 };
+
+const double kPI = 3.141592653589793238460;  // src/Header.h:19
+const float kNegInf = -2147483648.0f;         // src/Header.h:20
+const float kJsEps = 0.000001f;               // src/Header.h:22, converted to float by the array update
+
+// computeDist (src/Utilities.h:212-287).
+float distance(const float* x, const float* y, int d, int code) {
+    switch (code) {
+        case D_COSINE: {  // 1 - x.y  (:214-215)
+            float s = 0.0f;
+            for (int i = 0; i < d; ++i) s = std::fma(x[i], y[i], s);
+            return 1 - s;
+        }
+        case D_L1: {  // sum |x - y|  (:216-217)
+            float s = 0.0f;
+            for (int i = 0; i < d; ++i) s = s + std::fabs(x[i] - y[i]);
+            return s;
+        }
+        case D_L2: {  // ||x - y||  (:218-219)
+            float s = 0.0f;
+            for (int i = 0; i < d; ++i) {
+                const float t = x[i] - y[i];
+                s = std::fma(t, t, s);
+            }
+            return std::sqrt(s);
+        }
+        case D_CHI2: {  // 1 - 2 sum_{x,y>0} xy/(x+y)  (:220-243)
+            float t = 0.0f;
+            for (int i = 0; i < d; ++i)
+                if (x[i] > 0 && y[i] > 0) t = t + (x[i] * y[i]) / (x[i] + y[i]);
+            return (float)(1.0 - 2.0 * (double)t);
+        }
+        case D_JS: {  // (:245-266), elementwise with EPSILON added to both
+            const float l2 = (float)std::log(2.0);
+            float s = 0.0f;
+            for (int i = 0; i < d; ++i) {
+                const float a = x[i] + kJsEps, b = y[i] + kJsEps;
+                const float t1 = (std::log((a + b) / a) / l2) * a;
+                const float t2 = (std::log((a + b) / b) / l2) * b;
+                s = s + (t1 + t2);
+            }
+            return (float)(1.0 - (double)s / 2.0);
+        }
+    }
+    return 0.0f;
+}
+
+// In-place radix-2 Walsh-Hadamard transform, strides 1, 2, 4, ... (the order
+// the reference's fht_float reproduces bit for bit; src/fht.h:11).
+void fwht(float* v, int N) {
+    for (int h = 1; h < N; h <<= 1)
+        for (int i = 0; i < N; i += 2 * h)
+            for (int j = i; j < i + h; ++j) {
+                const float a = v[j], b = v[j + h];
+                v[j] = a + b;
+                v[j + h] = a - b;
+            }
+}
+
+// Kernel embedding of one point (src/sDbscan.cpp:53-68; embedChi2
+// src/Utilities.h:132-164; embedJS :174-208).  `out` has ker zeros on entry.
+void embed(const float* x, int d, int code, int ker, float L, const float* R, float* out) {
+    if (code == D_COSINE) {
+        std::memcpy(out, x, sizeof(float) * d);
+    } else if (code == D_L1 || code == D_L2) {
+        const int h = ker / 2;
+        for (int r = 0; r < h; ++r) {  // R is h x d column-major
+            float s = 0.0f;
+            for (int c = 0; c < d; ++c) s = std::fma(R[(size_t)c * h + r], x[c], s);
+            out[r] = std::cos(s);
+            out[h + r] = std::sin(s);
+        }
+    } else if (code == D_CHI2 || code == D_JS) {
+        int comps = (ker / d) - 1;
+        comps /= 2;
+        for (int i = 0; i < d; ++i)
+            if (x[i] > 0) {
+                if (code == D_CHI2) out[i] = std::sqrt(x[i] * L);
+                else out[i] = (float)std::sqrt((double)(x[i] * L) * 2.0 / std::log(4.0));
+            }
+        for (int c = 1; c <= comps; ++c) {
+            const int base = d + (c - 1) * 2 * d;
+            for (int i = 0; i < d; ++i) {
+                if (!(x[i] > 0)) continue;
+                float f;
+                if (code == D_CHI2) {
+                    f = (float)std::sqrt(2.0 * (double)x[i] * (double)L / std::cosh(kPI * c * (double)L));
+                } else {
+                    const float cl = c * L;
+                    const float q = 1 + 4 * cl * cl;
+                    f = (float)(2.0 / (std::log(4.0) * (double)q * std::cosh(kPI * c * (double)L)));
+                    f = (float)std::sqrt(2.0 * (double)x[i] * (double)L * (double)f);
+                }
+                const float ang = (c * L) * std::log(x[i]);
+                out[base + i] = f * std::cos(ang);
+                out[base + d + i] = f * std::sin(ang);
+            }
+        }
+    }
+}
+
+// Fixed-size min-heap top-k with the reference's exact replacement rule:
+// fill to k, then replace the minimum only on strict `>` (src/sDbscan.cpp:111-132).
+// Comparisons look at the value only, as IFPair does (src/Header.h:56-69).
+struct ValIdx {
+    float v;
+    int i;
+};
+struct GreaterVal {
+    bool operator()(const ValIdx& a, const ValIdx& b) const { return a.v > b.v; }
+};
+typedef std::priority_queue<ValIdx, std::vector<ValIdx>, GreaterVal> MinHeap;
+
+inline void heap_offer(MinHeap& h, int k, int idx, float v) {
+    if ((int)h.size() < k) h.push({v, idx});
+    else if (v > h.top().v) {
+        h.pop();
+        h.push({v, idx});
+    }
+}
+
+struct Timer {
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    double lap() {
+        auto t = std::chrono::steady_clock::now();
+        double s = std::chrono::duration<double>(t - t0).count();
+        t0 = t;
+        return s;
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+// ---- host RNG (src/Utilities.h:47-64, :76-93, :105-122) ----------------------
+
+void orc_hd3_bits(int nbits, int seed, uint8_t* out) {
+    std::default_random_engine gen((unsigned)seed);
+    std::uniform_int_distribution<uint32_t> u(0, 1);
+    for (int i = 0; i < nbits; ++i) out[i] = (uint8_t)(u(gen) & 1);
+}
+
+// rows x cols column-major, filled column first like the reference.
+void orc_gauss(int rows, int cols, float mean, float stddev, int seed, float* out) {
+    std::default_random_engine gen((unsigned)seed);
+    std::normal_distribution<float> nd(mean, stddev);
+    for (int c = 0; c < cols; ++c)
+        for (int r = 0; r < rows; ++r) out[(size_t)c * rows + r] = nd(gen);
+}
+
+void orc_cauchy(int rows, int cols, float x0, float gamma, int seed, float* out) {
+    std::default_random_engine gen((unsigned)seed);
+    std::cauchy_distribution<float> cd(x0, gamma);
+    for (int c = 0; c < cols; ++c)
+        for (int r = 0; r < rows; ++r) out[(size_t)c * rows + r] = cd(gen);
+}
+
+// ---- transformData (src/Utilities.h:289-335) ---------------------------------
+// X: d x n column-major, modified in place.  Returns 0, or 1 (negative value)
+// / 2 (zero-sum column) where the reference prints an error and exits.
+int orc_transform(float* X, int n, int d, int code) {
+    if (code == D_COSINE) {
+#pragma omp parallel for
+        for (int p = 0; p < n; ++p) {
+            float* x = X + (size_t)p * d;
+            float s = 0.0f;
+            for (int i = 0; i < d; ++i) s = std::fma(x[i], x[i], s);
+            const float nrm = std::sqrt(s);
+            for (int i = 0; i < d; ++i) x[i] = x[i] / nrm;
+        }
+    } else if (code == D_CHI2 || code == D_JS) {
+        for (size_t i = 0; i < (size_t)n * d; ++i)
+            if (X[i] < 0) return 1;
+        int bad = 0;
+#pragma omp parallel for reduction(| : bad)
+        for (int p = 0; p < n; ++p) {
+            float* x = X + (size_t)p * d;
+            float s = 0.0f;
+            for (int i = 0; i < d; ++i) s = s + x[i];
+            if (s <= 0) {
+                bad = 1;
+                continue;
+            }
+            for (int i = 0; i < d; ++i) x[i] = x[i] / s;
+        }
+        if (bad) return 2;
+    }
+    return 0;
+}
+
+// ---- projection (src/sDbscan.cpp:46-91) --------------------------------------
+// X: transformed data, d x n column-major.  bits: 3*fhtDim signs (0/1).
+// R: (ker/2) x d column-major (L1/L2 only).  out: n x nproj, point-major
+// (point p's projections contiguous) == the reference's MATRIX_FHT (nproj x n
+// column-major).
+void orc_project(const float* X, int n, int d, int code, int ker, float L, const float* R, const uint8_t* bits,
+                 int fhtDim, int nproj, float* out) {
+#pragma omp parallel
+    {
+        std::vector<float> v(fhtDim);
+#pragma omp for
+        for (int p = 0; p < n; ++p) {
+            std::fill(v.begin(), v.end(), 0.0f);
+            embed(X + (size_t)p * d, d, code, ker, L, R, v.data());
+            for (int r = 0; r < 3; ++r) {
+                for (int i = 0; i < fhtDim; ++i) v[i] *= (float)(2 * (int)bits[r * fhtDim + i] - 1);
+                fwht(v.data(), fhtDim);
+            }
+            std::memcpy(out + (size_t)p * nproj, v.data(), sizeof(float) * nproj);
+        }
+    }
+}
+
+// ---- per-point top-k (src/sDbscan.cpp:97-143) --------------------------------
+// P: n x nproj point-major.  topK: n x 2k point-major (== the reference's
+// matrix_topK, 2k x n column-major); row 0 is the most extreme.
+void orc_topk(const float* P, int n, int nproj, int k, int* topK) {
+#pragma omp parallel for
+    for (int p = 0; p < n; ++p) {
+        MinHeap close, far;
+        const float* v = P + (size_t)p * nproj;
+        for (int r = 0; r < nproj; ++r) {
+            heap_offer(close, k, r, v[r]);
+            heap_offer(far, k, r, -v[r]);
+        }
+        int* o = topK + (size_t)p * 2 * k;
+        for (int j = k - 1; j >= 0; --j) {
+            o[j] = close.top().i;
+            close.pop();
+            o[j + k] = far.top().i;
+            far.pop();
+        }
+    }
+}
+
+// ---- per-vector top-m (src/sDbscan.cpp:151-208) ------------------------------
+// topM: nproj x 2m vector-major (== matrix_topM, 2m x nproj column-major).
+void orc_topm(const float* P, int n, int nproj, int m, int* topM) {
+#pragma omp parallel for
+    for (int r = 0; r < nproj; ++r) {
+        MinHeap close, far;
+        for (int p = 0; p < n; ++p) {
+            const float v = P[(size_t)p * nproj + r];
+            heap_offer(close, m, p, v);
+            heap_offer(far, m, p, -v);
+        }
+        int* o = topM + (size_t)r * 2 * m;
+        for (int j = m - 1; j >= 0; --j) {
+            o[j] = close.top().i;
+            close.pop();
+            o[j + m] = far.top().i;
+            far.pop();
+        }
+    }
+}
+
+// ---- core points (src/sDbscan.cpp:217-408) -----------------------------------
+// Computes, for every point, its de-duplicated symmetric eps-neighbourhood
+// (own candidates within eps, plus every point that found it as a candidate
+// within eps), the core flag (|N| >= minPts - 1) and |N|.
+// Outputs: core[n], degree[n]; neighbour lists are kept internally and can be
+// read with orc_neighbors_* (sorted ascending, for every point).
+struct Graph {
+    std::vector<std::vector<int>> nb;
+    std::vector<std::vector<float>> nd;  // distances (only when with_dist)
+};
+static Graph g_graph;
+
+// ref_order=1 keeps each list in the order the reference leaves it: the push
+// sequence de-duplicated through std::unordered_map<int, float> (:1428-1431)
+// and read back in the map's iteration order.  With one thread the push
+// sequence is the reference's own, so the lists match it element for element.
+void orc_find_core(const float* X, int n, int d, int code, const int* topK, int k, const int* topM, int m, float eps,
+                   int minPts, int with_dist, int ref_order, uint8_t* core, int32_t* degree) {
+    std::vector<std::vector<std::pair<int, float>>> nb(n);
+#pragma omp parallel
+    {
+        std::vector<uint64_t> seen(((size_t)n + 63) / 64);
+#pragma omp for schedule(dynamic, 64)
+        for (int p = 0; p < n; ++p) {
+            std::fill(seen.begin(), seen.end(), 0ull);  // per-point n-bit set (:260)
+            const float* xp = X + (size_t)p * d;
+            for (int j = 0; j < k; ++j) {
+                for (int side = 0; side < 2; ++side) {  // close list then far list (:262-356)
+                    const int r = topK[(size_t)p * 2 * k + j + side * k];
+                    for (int i = 0; i < m; ++i) {
+                        const int q = topM[(size_t)r * 2 * m + i + side * m];
+                        if (q == p) continue;  // (:272)
+                        if (seen[q >> 6] >> (q & 63) & 1) continue;
+                        seen[q >> 6] |= 1ull << (q & 63);
+                        const float dist = distance(xp, X + (size_t)q * d, d, code);
+                        if (dist <= eps) {  // (:286-296)
+#pragma omp critical
+                            {
+                                nb[p].push_back({q, dist});
+                                nb[q].push_back({p, dist});
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    g_graph.nb.assign(n, {});
+    g_graph.nd.assign(n, {});
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int p = 0; p < n; ++p) {  // de-duplicate + core flag (:374-400)
+        auto& l = nb[p];
+        std::vector<int> ids;
+        std::vector<float> ds;
+        if (ref_order) {
+            std::unordered_map<int, float> mp(l.begin(), l.end());
+            for (const auto& e : mp) {
+                ids.push_back(e.first);
+                ds.push_back(e.second);
+            }
+        } else {
+            std::sort(l.begin(), l.end(), [](const std::pair<int, float>& a, const std::pair<int, float>& b) {
+                return a.first < b.first;
+            });
+            for (size_t t = 0; t < l.size(); ++t)
+                if (t == 0 || l[t].first != l[t - 1].first) {
+                    ids.push_back(l[t].first);
+                    ds.push_back(l[t].second);
+                }
+        }
+        degree[p] = (int32_t)ids.size();
+        core[p] = (int)ids.size() >= minPts - 1 ? 1 : 0;
+        g_graph.nb[p].swap(ids);
+        if (with_dist) g_graph.nd[p].swap(ds);
+        std::vector<std::pair<int, float>>().swap(l);
+    }
+}
+
+int64_t orc_neighbors_total(int n) {
+    int64_t t = 0;
+    for (int p = 0; p < n; ++p) t += (int64_t)g_graph.nb[p].size();
+    return t;
+}
+// CSR export: offsets[n+1], idx[total], dist[total] (dist may be null).
+void orc_neighbors_export(int n, int64_t* offsets, int32_t* idx, float* dist) {
+    int64_t o = 0;
+    for (int p = 0; p < n; ++p) {
+        offsets[p] = o;
+        for (size_t t = 0; t < g_graph.nb[p].size(); ++t, ++o) {
+            idx[o] = g_graph.nb[p][t];
+            if (dist) dist[o] = g_graph.nd[p][t];
+        }
+    }
+    offsets[n] = o;
+}
+void orc_graph_free() {
+    std::vector<std::vector<int>>().swap(g_graph.nb);
+    std::vector<std::vector<float>>().swap(g_graph.nd);
+}
+
+// ---- formCluster (src/sDbscan.cpp:509-637) -----------------------------------
+// Over a CSR neighbour graph (lists of core points are what matters; lists
+// of non-core points are ignored, as the reference clears them at :379).
+// Returns n_clusters_ (number of clusters + 1, or 2 when there are none: :633).
+int orc_form_cluster(int n, const uint8_t* core, const int64_t* off, const int32_t* idx, int32_t* labels) {
+    std::fill(labels, labels + n, -1);
+    int id = -1, ncl = 0;
+    std::vector<uint8_t> conn(n, 0);
+    std::vector<int> touched;
+    for (int p = 0; p < n; ++p) {
+        if (!core[p] || labels[p] != -1) continue;
+        ++id;
+        std::vector<int> seeds(1, p);
+        touched.assign(1, p);
+        conn[p] = 1;
+        while (!seeds.empty()) {
+            const int x = seeds.back();
+            seeds.pop_back();
+            for (int64_t t = off[x]; t < off[x + 1]; ++t) {
+                const int y = idx[t];
+                if (conn[y]) continue;
+                conn[y] = 1;
+                touched.push_back(y);
+                if (core[y] && labels[y] == -1) seeds.push_back(y);
+            }
+        }
+        for (int y : touched) {
+            if (labels[y] == -1) labels[y] = id;
+            conn[y] = 0;
+        }
+        ncl = id;
+    }
+    return ncl + 2;
+}
+
+// ---- core distance (src/sDbscan.cpp:1424-1460) -------------------------------
+// coreDist[p] = (minPts-1)-th smallest neighbour distance for core points, 0
+// otherwise (FVector(n, 0.0) at :1420).  Uses the graph of orc_find_core.
+void orc_core_dist(int n, int minPts, const uint8_t* core, float* coreDist) {
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int p = 0; p < n; ++p) {
+        coreDist[p] = 0.0f;
+        if (!core[p]) continue;
+        std::vector<float> v = g_graph.nd[p];
+        std::nth_element(v.begin(), v.begin() + (minPts - 2), v.end());
+        coreDist[p] = v[minPts - 2];
+    }
+}
+
+// ---- formOptics_scikit (src/sDbscan.cpp:1588-1703) ---------------------------
+// CSR graph with distances.  tie_mode 0: the reference's heap, which compares
+// reachability values only (Min_PQ_Pair, src/Header.h:100), so equal values
+// pop in an order set by the heap and the neighbour-list order.  tie_mode 1:
+// the canonical order used by the GPU engine — pops by (reachability, point
+// id), which makes the ordering independent of neighbour-list order.
+int64_t orc_form_optics(int n, const uint8_t* core, const float* coreDist, const int64_t* off, const int32_t* idx,
+                        const float* dist, int tie_mode, int32_t* ordering, float* reach) {
+    std::fill(reach, reach + n, kNegInf);
+    std::vector<uint8_t> done(n, 0);
+    int64_t no = 0;
+    struct E {
+        float v;
+        int i;
+    };
+    auto cmp0 = [](const E& a, const E& b) { return a.v > b.v; };
+    auto cmp1 = [](const E& a, const E& b) { return a.v > b.v || (a.v == b.v && a.i > b.i); };
+    std::priority_queue<E, std::vector<E>, decltype(cmp0)> h0(cmp0);
+    std::priority_queue<E, std::vector<E>, decltype(cmp1)> h1(cmp1);
+    auto push = [&](int y, float v) {
+        if (tie_mode) h1.push({v, y});
+        else h0.push({v, y});
+    };
+    auto relax = [&](int x) {
+        const float cd = coreDist[x];
+        for (int64_t t = off[x]; t < off[x + 1]; ++t) {
+            const int y = idx[t];
+            if (done[y]) continue;
+            const float r = std::max(cd, dist[t]);
+            if (reach[y] == kNegInf) {
+                reach[y] = r;
+                push(y, r);
+            } else if (reach[y] > r) {
+                reach[y] = r;
+                push(y, r);
+            }
+        }
+    };
+    for (int p = 0; p < n; ++p) {
+        if (done[p]) continue;
+        done[p] = 1;
+        ordering[no++] = p;
+        if (!core[p]) continue;
+        relax(p);
+        while (tie_mode ? !h1.empty() : !h0.empty()) {
+            int y;
+            if (tie_mode) {
+                y = h1.top().i;
+                h1.pop();
+            } else {
+                y = h0.top().i;
+                h0.pop();
+            }
+            if (done[y]) continue;
+            done[y] = 1;
+            ordering[no++] = y;
+            if (core[y]) relax(y);
+        }
+    }
+    return no;
+}
+
+// ---- whole fits, for the CPU baseline (src/sDbscan.cpp:830-890, 1711-1769) ---
+// X: d x n column-major, not modified.  bits: 3*fhtDim; R may be null unless
+// L1/L2.  times[5]: transform, index, core, cluster/optics, total (seconds).
+// Returns n_clusters_ (fit_sdbscan) or 0, or a negative transform error.
+int orc_fit_sdbscan(const float* X, int n, int d, int code, int nproj, int k, int m, int ker, float L,
+                    const float* R, const uint8_t* bits, int fhtDim, float eps, int minPts, int threads,
+                    int32_t* labels, uint8_t* core, double* times) {
+    if (threads > 0) omp_set_num_threads(threads);
+    Timer tm, all;
+    std::vector<float> Xc(X, X + (size_t)n * d);
+    int err = orc_transform(Xc.data(), n, d, code);
+    if (err) return -err;
+    times[0] = tm.lap();
+    std::vector<float> P((size_t)n * nproj);
+    std::vector<int> topK((size_t)n * 2 * k), topM((size_t)nproj * 2 * m);
+    orc_project(Xc.data(), n, d, code, ker, L, R, bits, fhtDim, nproj, P.data());
+    orc_topk(P.data(), n, nproj, k, topK.data());
+    orc_topm(P.data(), n, nproj, m, topM.data());
+    std::vector<float>().swap(P);
+    times[1] = tm.lap();
+    std::vector<int32_t> deg(n);
+    orc_find_core(Xc.data(), n, d, code, topK.data(), k, topM.data(), m, eps, minPts, 0, 0, core, deg.data());
+    times[2] = tm.lap();
+    std::vector<int64_t> off(n + 1);
+    std::vector<int32_t> idx(orc_neighbors_total(n));
+    orc_neighbors_export(n, off.data(), idx.data(), nullptr);
+    const int ncl = orc_form_cluster(n, core, off.data(), idx.data(), labels);
+    times[3] = tm.lap();
+    times[4] = all.lap();
+    orc_graph_free();
+    return ncl;
+}
+
+int orc_fit_soptics(const float* X, int n, int d, int code, int nproj, int k, int m, int ker, float L,
+                    const float* R, const uint8_t* bits, int fhtDim, float eps, int minPts, int threads,
+                    int tie_mode, int32_t* ordering, float* reach, uint8_t* core, float* coreDist, double* times) {
+    if (threads > 0) omp_set_num_threads(threads);
+    Timer tm, all;
+    std::vector<float> Xc(X, X + (size_t)n * d);
+    int err = orc_transform(Xc.data(), n, d, code);
+    if (err) return -err;
+    times[0] = tm.lap();
+    std::vector<float> P((size_t)n * nproj);
+    std::vector<int> topK((size_t)n * 2 * k), topM((size_t)nproj * 2 * m);
+    orc_project(Xc.data(), n, d, code, ker, L, R, bits, fhtDim, nproj, P.data());
+    orc_topk(P.data(), n, nproj, k, topK.data());
+    orc_topm(P.data(), n, nproj, m, topM.data());
+    std::vector<float>().swap(P);
+    times[1] = tm.lap();
+    std::vector<int32_t> deg(n);
+    orc_find_core(Xc.data(), n, d, code, topK.data(), k, topM.data(), m, eps, minPts, 1, tie_mode == 0, core, deg.data());
+    orc_core_dist(n, minPts, core, coreDist);
+    times[2] = tm.lap();
+    const int64_t tot = orc_neighbors_total(n);
+    std::vector<int64_t> off(n + 1);
+    std::vector<int32_t> idx(tot);
+    std::vector<float> dist(tot);
+    orc_neighbors_export(n, off.data(), idx.data(), dist.data());
+    orc_form_optics(n, core, coreDist, off.data(), idx.data(), dist.data(), tie_mode, ordering, reach);
+    times[3] = tm.lap();
+    times[4] = all.lap();
+    orc_graph_free();
+    return 0;
+}
+
+// Distance of one pair, exposed for tests of the numerical contract.
+float orc_distance(const float* x, const float* y, int d, int code) { return distance(x, y, d, code); }
+
+void orc_set_threads(int t) {
+    if (t > 0) omp_set_num_threads(t);
+}
+
+}  // extern "C"

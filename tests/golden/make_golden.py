@@ -1,0 +1,93 @@
+"""Generates the golden fixtures in this folder from the reference itself.
+
+Runs the reference's unmodified sDbscan class (built by ``make -C oracle ref``
+from the reference sources against the shim headers in ``oracle/shim``) with
+one thread on small seeded inputs, and stores inputs and outputs as
+compressed ``.npz`` files.  Run on the development machine where the
+reference sources exist:
+
+    python tests/golden/make_golden.py
+
+The fixtures are what pins the oracle (and through it the GPU engine) to the
+reference on machines where the reference cannot be built.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.oracle import Ref, build_ref  # noqa: E402
+from sdbscan_gb300 import datasets as ds  # noqa: E402
+
+
+def cases():
+    """(name, X, params, eps, minPts, optics)."""
+    X1, _ = ds.cfg1_cosine(2000, 32, seed=11)
+    yield "cosine_vmf_2000x32", X1, dict(n_proj=256, topK=5, topM=20, distance="Cosine"), 0.15, 10, False
+    X2, _ = ds.cfg1_cosine(1500, 100, seed=12)  # d not a power of two, d < fhtDim
+    yield "cosine_d100_1500", X2, dict(n_proj=128, topK=4, topM=25, distance="Cosine"), 0.15, 8, False
+    X3, _ = ds.cfg2_mnist_like(2000, 196, seed=13)
+    yield "cosine_mnistlike_2000x196", X3, dict(n_proj=256, topK=10, topM=30, distance="Cosine"), 0.25, 20, False
+    yield "cosine_optics_2000x32", X1, dict(n_proj=256, topK=5, topM=20, distance="Cosine"), 0.2, 10, True
+    X4, _ = ds.cfg4_dirichlet(1500, 64, n_comp=5, seed=14)
+    yield "chi2_ker512_1500x64", X4, dict(n_proj=256, topK=5, topM=20, distance="Chi2", ker_n_features=512), 0.3, 10, False
+    yield "chi2_optics_ker1024_1500x64", X4, dict(n_proj=1024, topK=5, topM=20, distance="Chi2",
+                                                   ker_n_features=1024), 0.3, 10, True
+    X5, _ = ds.cfg3_aniso_l2(1500, 16, n_comp=5, scale=0.1, seed=15)
+    yield "l2_rff_1500x16", X5, dict(n_proj=256, topK=5, topM=20, distance="L2", ker_n_features=256,
+                                      ker_sigma=0.5), 0.6, 10, False
+    yield "l1_rff_1500x16", X5, dict(n_proj=256, topK=5, topM=20, distance="L1", ker_n_features=256,
+                                      ker_sigma=0.5), 2.0, 10, False
+    yield "js_ker512_1500x64", X4, dict(n_proj=256, topK=5, topM=20, distance="JS", ker_n_features=512), 0.3, 10, False
+    # edge cases
+    rng = np.random.default_rng(16)
+    base = rng.standard_normal((40, 24)).astype(np.float32)
+    Xd = np.repeat(base, 25, axis=0)  # every point has 24 exact duplicates: massive ties
+    yield "cosine_duplicates_1000x24", Xd, dict(n_proj=64, topK=3, topM=30, distance="Cosine"), 0.05, 5, False
+    X6, _ = ds.cfg1_cosine(800, 16, seed=17)
+    yield "cosine_all_noise_800x16", X6, dict(n_proj=64, topK=2, topM=10, distance="Cosine"), 1e-6, 5, False
+    X7 = (np.ones((500, 8)) + 1e-3 * rng.standard_normal((500, 8))).astype(np.float32)
+    yield "cosine_single_cluster_500x8", X7, dict(n_proj=32, topK=2, topM=40, distance="Cosine"), 0.01, 5, False
+    X8, _ = ds.cfg1_cosine(60, 12, seed=18)  # m close to n
+    yield "cosine_tiny_60x12", X8, dict(n_proj=16, topK=1, topM=50, distance="Cosine"), 0.3, 3, False
+    X9, _ = ds.cfg1_cosine(3000, 64, seed=19)
+    yield "cosine_k1_m1_3000x64", X9, dict(n_proj=1024, topK=1, topM=1, distance="Cosine"), 0.2, 2, False
+
+
+def main():
+    if build_ref() is None:
+        sys.exit("the reference sources are not available here; fixtures cannot be regenerated")
+    for name, X, params, eps, minPts, optics in cases():
+        n, d = X.shape
+        r = Ref(n, d)
+        r.set_params(**params, n_threads=1, random_seed=7)
+        if optics:
+            r.fit_sOptics(X, eps, minPts)
+        else:
+            r.fit_sDbscan(X, eps, minPts)
+        out = dict(X=X, bits=r.bits(), R=r.R(), topK=r.topK(), topM=r.topM(), core=r.core())
+        out["proj_head"] = r.projections()[: min(n, 64)]
+        if optics:
+            off, idx, dd = r.neighbor_dist()
+            out.update(ordering=r.ordering_, reachability=r.reachability_, core_dist=r.core_dist(),
+                       degree=np.diff(off).astype(np.int32))
+        else:
+            off, idx = r.neighbors()
+            out.update(labels=r.labels_, n_clusters=np.int32(r.n_clusters_),
+                       core_degree=np.diff(off).astype(np.int32))
+        meta = dict(params, eps=eps, minPts=minPts, optics=optics, random_seed=7, n_threads=1)
+        out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(name, "n_clusters" if not optics else "ordering", r.n_clusters_ if not optics else len(r.ordering_),
+              "cores", int(out["core"].sum()))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,92 @@
+"""The oracle restatement against the reference's own outputs.
+
+The golden fixtures were produced by the reference itself (its unmodified
+sources, one thread, seed 7; see tests/golden/make_golden.py).  Every stage of
+the oracle must reproduce them bit for bit: sign bits, random Fourier matrix,
+projections, top-k / top-m index matrices, core flags, neighbourhood sizes,
+labels, n_clusters_, core distances, and - with the reference's neighbour-list
+order (one thread) - the sOPTICS ordering and reachability.
+"""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import fht_dim
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+def _load(path):
+    z = np.load(path)
+    meta = json.loads(bytes(z["meta"]).decode())
+    return z, meta
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_oracle_matches_reference_fixture(port, path):
+    z, meta = _load(path)
+    X = z["X"]
+    n, d = X.shape
+    dist = meta["distance"]
+    ker = d if dist == "Cosine" else meta.get("ker_n_features", 1024)
+    nproj, k, m = meta["n_proj"], meta["topK"], meta["topM"]
+    fd = fht_dim(nproj, ker)
+    bits = port.hd3_bits(3 * fd, meta["random_seed"])
+    np.testing.assert_array_equal(bits, z["bits"])
+    R = port._R(dist, ker, d, meta.get("ker_sigma", 1.0), meta["random_seed"])
+    if R is not None:
+        np.testing.assert_array_equal(R, z["R"])
+    Xt, rc = port.transform(X, dist)
+    assert rc == 0
+    P = port.project(Xt, dist, ker, 0.4, R, bits, fd, nproj)
+    np.testing.assert_array_equal(P[: z["proj_head"].shape[0]], z["proj_head"])
+    topK = port.topk(P, k)
+    topM = port.topm(P, m)
+    np.testing.assert_array_equal(topK, z["topK"])
+    np.testing.assert_array_equal(topM, z["topM"])
+    port.L.orc_set_threads(1)
+    core, deg, off, idx, dd = port.find_core(Xt, dist, topK, topM, meta["eps"], meta["minPts"],
+                                             with_dist=True, ref_order=meta["optics"])
+    port.L.orc_set_threads(0)
+    np.testing.assert_array_equal(core, z["core"])
+    if meta["optics"]:
+        np.testing.assert_array_equal(deg, z["degree"])
+        cd = port.core_dist(n, meta["minPts"], core)
+        np.testing.assert_array_equal(cd, z["core_dist"])
+        order, reach = port.form_optics(core, cd, off, idx, dd, tie_mode=0)
+        np.testing.assert_array_equal(order, z["ordering"])
+        np.testing.assert_array_equal(reach, z["reachability"])
+        # the canonical tie order is a permutation with the same core set
+        order1, reach1 = port.form_optics(core, cd, off, idx, dd, tie_mode=1)
+        assert sorted(order1.tolist()) == list(range(n))
+    else:
+        np.testing.assert_array_equal(deg[core == 1], z["core_degree"][core == 1])
+        labels, ncl = port.form_cluster(core, off, idx)
+        np.testing.assert_array_equal(labels, z["labels"])
+        assert ncl == int(z["n_clusters"])
+    port.graph_free()
+
+
+def test_whole_fit_matches_reference_fixture(port):
+    """orc_fit_sdbscan (the CPU baseline) reproduces a fixture end to end."""
+    z, meta = _load(os.path.join(os.path.dirname(__file__), "golden", "cosine_vmf_2000x32.npz"))
+    labels, ncl, core, _ = port.fit_sdbscan(z["X"], meta["eps"], meta["minPts"], n_proj=meta["n_proj"],
+                                            topK=meta["topK"], topM=meta["topM"], seed=7, threads=4)
+    np.testing.assert_array_equal(labels, z["labels"])
+    np.testing.assert_array_equal(core, z["core"])
+    assert ncl == int(z["n_clusters"])
+
+
+def test_transform_rejects_like_reference(port):
+    """Chi2/JS reject negative values and zero-sum columns (src/Utilities.h:308-324)."""
+    X = np.abs(np.random.default_rng(0).standard_normal((10, 4))).astype(np.float32)
+    assert port.transform(X, "Chi2")[1] == 0
+    Xn = X.copy()
+    Xn[3, 1] = -1e-3
+    assert port.transform(Xn, "Chi2")[1] == 1
+    Xz = X.copy()
+    Xz[5] = 0
+    assert port.transform(Xz, "JS")[1] == 2
