@@ -1,0 +1,148 @@
+/*
+ * sdbscan_gb300 — C ABI of the GB300 sDbscan / sOPTICS engine.
+ *
+ * A drop-in for the fit path of the reference's `sDbscan` class
+ * (src/sDbscan.h:10-223, bound to Python in python/python_wrapper.cpp:14-65).
+ * Each entry point below names the reference interface it replaces.  Plain C
+ * types only: pointers, sizes, one parameter struct and status codes.
+ *
+ * Conventions
+ *  - Data is d x n column-major float32 (one point per contiguous run of d
+ *    floats), exactly as the reference takes it (README.md:39-41,
+ *    src/Utilities.cpp:69-76).
+ *  - Every output buffer is owned by the caller.
+ *  - An engine owns its device buffers and one CUDA stream.  It is not
+ *    thread-safe; use one engine per host thread.
+ *  - Errors are returned as status codes, never by exiting; the message of
+ *    the last failure is available from sdb_last_error().
+ */
+#ifndef SDBSCAN_GB300_H
+#define SDBSCAN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sdb_engine sdb_engine;
+
+typedef enum {
+    SDB_OK = 0,
+    SDB_ERR_ARG = 1,        /* invalid argument or parameter combination          */
+    SDB_ERR_CUDA = 2,       /* CUDA runtime error (message in sdb_last_error)      */
+    SDB_ERR_NEGATIVE = 3,   /* Chi2/JS input has a negative value (src/Utilities.h:308-312) */
+    SDB_ERR_ZERO_POINT = 4, /* a point with zero sum (Chi2/JS, :318-325) or zero norm (Cosine) */
+    SDB_ERR_STATE = 5,      /* output requested before the matching fit            */
+    SDB_ERR_NOMEM = 6,      /* device allocation failed                            */
+    SDB_ERR_INTERNAL = 7    /* internal consistency check failed                   */
+} sdb_status;
+
+typedef enum { SDB_COSINE = 0, SDB_L1 = 1, SDB_L2 = 2, SDB_CHI2 = 3, SDB_JS = 4 } sdb_distance;
+
+typedef enum {
+    SDB_PREC_FP32 = 0,      /* plain FP32: results identical to the reference's CPU path */
+    SDB_PREC_BF16 = 1       /* BF16 tensor-core screening + FP32 re-decision near eps    */
+} sdb_precision;
+
+/* Parameters of sDbscan::set_params (src/sDbscan.h:79-108), same meaning and
+ * order; `precision` is this engine's addition.  Fill with
+ * sdb_params_default() to get the Python binding's defaults
+ * (python/python_wrapper.cpp:17-24). */
+typedef struct {
+    int32_t n_proj;               /* numProj: number of random vectors D          */
+    int32_t topK;                 /* k: close/far random vectors kept per point   */
+    int32_t topM;                 /* m: close/far points kept per random vector   */
+    int32_t distance;             /* sdb_distance                                 */
+    int32_t ker_n_features;       /* kerDim (forced to n_features for Cosine)     */
+    float ker_sigma;              /* kerSigma (L1/L2 random Fourier features)     */
+    float ker_intervalSampling;   /* kerSam (Chi2/JS embeddings)                  */
+    int32_t clusterNoise;         /* noiseClustering: only 0 is supported         */
+    float samplingProb;           /* prob (sDbscan-1NN; unused when clusterNoise=0) */
+    int32_t verbose;              /* ver: print per-stage times                   */
+    int32_t n_threads;            /* numThreads: accepted for API parity, unused  */
+    int32_t random_seed;          /* randomSeed: < 0 means seeded from the clock  */
+    int32_t precision;            /* sdb_precision                                */
+} sdb_params;
+
+/* Defaults of the Python binding (python/python_wrapper.cpp:17-24). */
+void sdb_params_default(sdb_params* p);
+
+/* sDbscan(int n, int d)  (src/sDbscan.h:74-77; python_wrapper.cpp:16).
+ * device: CUDA device ordinal. */
+sdb_status sdb_engine_create(int32_t n_points, int32_t n_features, int32_t device, sdb_engine** out);
+
+/* ~sDbscan()  (src/sDbscan.h:165-168). */
+void sdb_engine_destroy(sdb_engine* e);
+
+/* set_params / set_kernel_params / set_topK / set_topM / set_threads /
+ * set_clusterNoise  (src/sDbscan.h:79-124, :170-180). */
+sdb_status sdb_set_params(sdb_engine* e, const sdb_params* p);
+
+/* fit_sDbscan(const Ref<const MatrixXf>& X, float eps, int minPts)
+ * (src/sDbscan.h:183, src/sDbscan.cpp:830-890).  X_host: d x n column-major
+ * host memory (pinned memory makes the upload faster).  Results stay in the
+ * engine until read with sdb_get_*. */
+sdb_status sdb_fit_sdbscan(sdb_engine* e, const float* X_host, float eps, int32_t minPts);
+
+/* Same as sdb_fit_sdbscan with X already in device memory (d x n
+ * column-major, device pointer of the engine's device).  No reference
+ * counterpart: it is the same fit with the upload left out. */
+sdb_status sdb_fit_sdbscan_device(sdb_engine* e, const float* X_device, float eps, int32_t minPts);
+
+/* fit_sOptics(const Ref<const MatrixXf>& X, float eps, int minPts)
+ * (src/sDbscan.h:197, src/sDbscan.cpp:1711-1769).  minPts >= 2. */
+sdb_status sdb_fit_soptics(sdb_engine* e, const float* X_host, float eps, int32_t minPts);
+sdb_status sdb_fit_soptics_device(sdb_engine* e, const float* X_device, float eps, int32_t minPts);
+
+/* labels_ and n_clusters_  (src/sDbscan.h:67-68; python_wrapper.cpp:31-32).
+ * labels: n_points int32. */
+sdb_status sdb_get_labels(sdb_engine* e, int32_t* labels, int32_t* n_clusters);
+
+/* ordering_ and reachability_  (src/sDbscan.h:71-72; python_wrapper.cpp:33-34).
+ * ordering: n_points int32 (a permutation); reachability: n_points float,
+ * indexed by point id, -2^31 for points never reached (src/sDbscan.cpp:1590). */
+sdb_status sdb_get_optics(sdb_engine* e, int32_t* ordering, float* reachability);
+
+/* clear()  (src/sDbscan.h:142-163): drops results; device buffers are kept
+ * for the next fit. */
+sdb_status sdb_clear(sdb_engine* e);
+
+/* Intermediate state, for parity checks (protected members of the reference):
+ *   matrix_topK  (src/sDbscan.h:50): n x 2k int32, point-major, row 0 = most extreme
+ *   matrix_topM  (src/sDbscan.h:51): D x 2m int32, vector-major
+ *   bit_CorePoints (src/sDbscan.h:56): n uint8
+ *   |neighbourhood| per point (sizes of vec2D_Neighbors before the non-core
+ *       lists are cleared, src/sDbscan.cpp:378-382): n int32
+ *   vec_CoreDist (src/sDbscan.h:60): n float (sOPTICS fits only)
+ *   projections (MATRIX_FHT, src/sDbscan.cpp:31, :91): n x D float, point-major */
+sdb_status sdb_get_topk(sdb_engine* e, int32_t* topK);
+sdb_status sdb_get_topm(sdb_engine* e, int32_t* topM);
+sdb_status sdb_get_core(sdb_engine* e, uint8_t* core, int32_t* degree);
+sdb_status sdb_get_core_dist(sdb_engine* e, float* core_dist);
+sdb_status sdb_get_projections(sdb_engine* e, float* proj);
+
+/* Counters of the last fit: ties at the top-k / top-m selection boundary
+ * (where the reference's heap order decides), kernel launches, neighbour
+ * pairs within eps. out[0]=topk ties, out[1]=topm ties, out[2]=launches,
+ * out[3]=directed candidate pairs within eps (with duplicates). */
+sdb_status sdb_get_counters(sdb_engine* e, int64_t* out, int32_t n_out);
+
+/* Device time of each stage of the last fit in milliseconds (CUDA events):
+ * ms[0]=upload, [1]=transform+projection+top-k, [2]=top-m, [3]=index,
+ * [4]=distances, [5]=core, [6]=cluster/optics, [7]=download, [8]=total. */
+sdb_status sdb_get_stage_ms(sdb_engine* e, float* ms, int32_t n_ms);
+
+/* The CUDA stream the engine runs on (as a void*), for callers that want to
+ * order their own work after a fit. */
+void* sdb_engine_stream(sdb_engine* e);
+
+/* Message of the last error on this engine ("" if none). */
+const char* sdb_last_error(sdb_engine* e);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SDBSCAN_GB300_H */

@@ -1,0 +1,195 @@
+"""ctypes binding of the engine's C ABI (include/sdbscan_gb300.h).
+
+This is how the tests and bench.py drive the engine: through the same C
+entry points a foreign-language caller binds.  Importing this module loads
+``libsdbscan_gb300.so`` from the package folder and fails loudly if it is
+missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libsdbscan_gb300.so")
+
+DISTANCES = {"Cosine": 0, "L1": 1, "L2": 2, "Chi2": 3, "JS": 4}
+PREC_FP32, PREC_BF16 = 0, 1
+STATUS = {0: "SDB_OK", 1: "SDB_ERR_ARG", 2: "SDB_ERR_CUDA", 3: "SDB_ERR_NEGATIVE", 4: "SDB_ERR_ZERO_POINT",
+          5: "SDB_ERR_STATE", 6: "SDB_ERR_NOMEM", 7: "SDB_ERR_INTERNAL"}
+EXPORTS = ["sdb_params_default", "sdb_engine_create", "sdb_engine_destroy", "sdb_set_params", "sdb_fit_sdbscan",
+           "sdb_fit_sdbscan_device", "sdb_fit_soptics", "sdb_fit_soptics_device", "sdb_get_labels", "sdb_get_optics",
+           "sdb_clear", "sdb_get_topk", "sdb_get_topm", "sdb_get_core", "sdb_get_core_dist", "sdb_get_projections",
+           "sdb_get_counters", "sdb_get_stage_ms", "sdb_engine_stream", "sdb_last_error"]
+
+
+class SdbParams(ctypes.Structure):
+    _fields_ = [("n_proj", ctypes.c_int32), ("topK", ctypes.c_int32), ("topM", ctypes.c_int32),
+                ("distance", ctypes.c_int32), ("ker_n_features", ctypes.c_int32), ("ker_sigma", ctypes.c_float),
+                ("ker_intervalSampling", ctypes.c_float), ("clusterNoise", ctypes.c_int32),
+                ("samplingProb", ctypes.c_float), ("verbose", ctypes.c_int32), ("n_threads", ctypes.c_int32),
+                ("random_seed", ctypes.c_int32), ("precision", ctypes.c_int32)]
+
+
+class SdbError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+_LIB = None
+
+
+def load(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Loads the engine library (building it first if the sources are newer)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: run `python -c 'import __graft_entry__ as g; g.build()'` "
+                          "(the engine has no CPU fallback)")
+    L = ctypes.CDLL(path)
+    vp, i32, f32 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_float
+    L.sdb_params_default.argtypes = [ctypes.POINTER(SdbParams)]
+    L.sdb_engine_create.argtypes = [i32, i32, i32, ctypes.POINTER(vp)]
+    L.sdb_engine_destroy.argtypes = [vp]
+    L.sdb_set_params.argtypes = [vp, ctypes.POINTER(SdbParams)]
+    for f in ("sdb_fit_sdbscan", "sdb_fit_sdbscan_device", "sdb_fit_soptics", "sdb_fit_soptics_device"):
+        getattr(L, f).argtypes = [vp, vp, f32, i32]
+    L.sdb_get_labels.argtypes = [vp, vp, vp]
+    L.sdb_get_optics.argtypes = [vp, vp, vp]
+    L.sdb_clear.argtypes = [vp]
+    for f in ("sdb_get_topk", "sdb_get_topm", "sdb_get_core_dist", "sdb_get_projections"):
+        getattr(L, f).argtypes = [vp, vp]
+    L.sdb_get_core.argtypes = [vp, vp, vp]
+    L.sdb_get_counters.argtypes = [vp, vp, i32]
+    L.sdb_get_stage_ms.argtypes = [vp, vp, i32]
+    L.sdb_engine_stream.argtypes = [vp]
+    L.sdb_engine_stream.restype = vp
+    L.sdb_last_error.argtypes = [vp]
+    L.sdb_last_error.restype = ctypes.c_char_p
+    _LIB = L
+    return L
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+class Engine:
+    """One engine = one reference `sDbscan(n_points, n_features)` object."""
+
+    def __init__(self, n_points: int, n_features: int, device: int = 0):
+        self.L = load()
+        self.n, self.d = int(n_points), int(n_features)
+        h = ctypes.c_void_p()
+        s = self.L.sdb_engine_create(self.n, self.d, device, ctypes.byref(h))
+        if s != 0:
+            raise SdbError(s, "sdb_engine_create failed (no usable CUDA device?)")
+        self.h = h
+        self.params = SdbParams()
+        self.L.sdb_params_default(ctypes.byref(self.params))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sdb_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, s: int):
+        if s != 0:
+            raise SdbError(s, self.L.sdb_last_error(self.h).decode())
+
+    # set_params with the reference binding's keyword names (python/python_wrapper.cpp:17-24)
+    def set_params(self, n_proj=1024, topK=10, topM=50, distance="Cosine", ker_n_features=1024, ker_sigma=1.0,
+                   ker_intervalSampling=0.4, clusterNoise=0, samplingProb=0.01, verbose=False, output="",
+                   n_threads=-1, random_seed=-1, precision=PREC_FP32):
+        p = self.params
+        p.n_proj, p.topK, p.topM = n_proj, topK, topM
+        p.distance = DISTANCES[distance]
+        p.ker_n_features, p.ker_sigma, p.ker_intervalSampling = ker_n_features, ker_sigma, ker_intervalSampling
+        p.clusterNoise, p.samplingProb, p.verbose = clusterNoise, samplingProb, int(bool(verbose))
+        p.n_threads, p.random_seed, p.precision = n_threads, random_seed, precision
+        self._check(self.L.sdb_set_params(self.h, ctypes.byref(p)))
+
+    # fits -----------------------------------------------------------------------
+    def fit_sdbscan(self, X: np.ndarray, eps: float, minPts: int):
+        """X: (n, d) C-contiguous float32 = d x n column-major."""
+        X = self._host(X)
+        self._check(self.L.sdb_fit_sdbscan(self.h, _ptr(X), ctypes.c_float(eps), minPts))
+
+    def fit_sdbscan_device(self, x_dev_ptr: int, eps: float, minPts: int):
+        self._check(self.L.sdb_fit_sdbscan_device(self.h, ctypes.c_void_p(x_dev_ptr), ctypes.c_float(eps), minPts))
+
+    def fit_soptics(self, X: np.ndarray, eps: float, minPts: int):
+        X = self._host(X)
+        self._check(self.L.sdb_fit_soptics(self.h, _ptr(X), ctypes.c_float(eps), minPts))
+
+    def fit_soptics_device(self, x_dev_ptr: int, eps: float, minPts: int):
+        self._check(self.L.sdb_fit_soptics_device(self.h, ctypes.c_void_p(x_dev_ptr), ctypes.c_float(eps), minPts))
+
+    def _host(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        if X.shape != (self.n, self.d):
+            raise ValueError(f"X must be (n_points, n_features) = ({self.n}, {self.d}), got {X.shape}")
+        return X
+
+    # results ---------------------------------------------------------------------
+    def labels(self) -> tuple[np.ndarray, int]:
+        out = np.empty(self.n, np.int32)
+        nc = ctypes.c_int32()
+        self._check(self.L.sdb_get_labels(self.h, _ptr(out), ctypes.byref(nc)))
+        return out, nc.value
+
+    def optics(self) -> tuple[np.ndarray, np.ndarray]:
+        order = np.empty(self.n, np.int32)
+        reach = np.empty(self.n, np.float32)
+        self._check(self.L.sdb_get_optics(self.h, _ptr(order), _ptr(reach)))
+        return order, reach
+
+    def topk(self) -> np.ndarray:
+        out = np.empty((self.n, 2 * self.params.topK), np.int32)
+        self._check(self.L.sdb_get_topk(self.h, _ptr(out)))
+        return out
+
+    def topm(self) -> np.ndarray:
+        out = np.empty((self.params.n_proj, 2 * self.params.topM), np.int32)
+        self._check(self.L.sdb_get_topm(self.h, _ptr(out)))
+        return out
+
+    def core(self) -> tuple[np.ndarray, np.ndarray]:
+        core = np.empty(self.n, np.uint8)
+        deg = np.empty(self.n, np.int32)
+        self._check(self.L.sdb_get_core(self.h, _ptr(core), _ptr(deg)))
+        return core, deg
+
+    def core_dist(self) -> np.ndarray:
+        out = np.empty(self.n, np.float32)
+        self._check(self.L.sdb_get_core_dist(self.h, _ptr(out)))
+        return out
+
+    def projections(self) -> np.ndarray:
+        out = np.empty((self.n, self.params.n_proj), np.float32)
+        self._check(self.L.sdb_get_projections(self.h, _ptr(out)))
+        return out
+
+    def counters(self) -> dict:
+        out = np.zeros(4, np.int64)
+        self._check(self.L.sdb_get_counters(self.h, _ptr(out), 4))
+        return dict(topk_ties=int(out[0]), topm_ties=int(out[1]), launches=int(out[2]), pairs=int(out[3]))
+
+    def stage_ms(self) -> dict:
+        out = np.zeros(9, np.float32)
+        self._check(self.L.sdb_get_stage_ms(self.h, _ptr(out), 9))
+        names = ["upload", "project", "topm", "index", "distances", "core", "cluster", "readback", "total"]
+        return dict(zip(names, out.tolist()))
+
+    def stream(self) -> int:
+        return int(self.L.sdb_engine_stream(self.h) or 0)

@@ -1,0 +1,195 @@
+// Shared device helpers and the internal launcher interface between the
+// kernel translation units and the engine (engine.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define SDB_DEV __device__ __forceinline__
+
+namespace sdb {
+
+constexpr int kWarp = 32;
+constexpr float kNegInfReach = -2147483648.0f;  // NEG_INF of src/Header.h:20
+
+// Order-preserving map float -> uint32 (larger float -> larger key).  -0 is
+// folded onto +0 first so that keys are equal exactly when the floats compare
+// equal (the reference's heaps compare floats).
+SDB_DEV uint32_t key_of(float v) {
+    uint32_t u = __float_as_uint(v + 0.0f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+SDB_DEV float float_of_key(uint32_t k) {
+    uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(u);
+}
+
+SDB_DEV unsigned lane_id() { return threadIdx.x & 31u; }
+
+template <typename T> SDB_DEV T shfl_xor(T v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+
+SDB_DEV uint64_t shfl_xor_u64(uint64_t v, int m) {
+    uint32_t lo = (uint32_t)v, hi = (uint32_t)(v >> 32);
+    lo = __shfl_xor_sync(0xffffffffu, lo, m);
+    hi = __shfl_xor_sync(0xffffffffu, hi, m);
+    return ((uint64_t)hi << 32) | lo;
+}
+SDB_DEV uint64_t warp_max_u64(uint64_t v) {
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+        uint64_t o = shfl_xor_u64(v, m);
+        v = o > v ? o : v;
+    }
+    return v;
+}
+SDB_DEV int warp_sum(int v) {
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+    return v;
+}
+
+// Distance codes (sdb_distance in include/sdbscan_gb300.h).
+enum { DIST_COSINE = 0, DIST_L1 = 1, DIST_L2 = 2, DIST_CHI2 = 3, DIST_JS = 4 };
+
+}  // namespace sdb
+
+// -------------------------------------------------------------------------
+// Launchers (host functions) implemented by the kernel translation units.
+// All run on `st`; none synchronizes.  Each returns the number of kernel
+// launches it made (for the launch counter) or a negative value on a launch
+// error.
+// -------------------------------------------------------------------------
+namespace sdb {
+
+struct ProjectArgs {
+    const float* X;      // input rows (n x d, row stride ldx)
+    int ldx;
+    float* Xt;           // transformed rows out (n x ld), may alias nothing
+    int ld;              // padded row stride of Xt (multiple of 4)
+    int n, d, dist;
+    int ker;             // embedding width (== d for Cosine)
+    float kerSam;        // Chi2/JS interval sampling
+    const float* E;      // precomputed embedding rows (L1/L2), n x ker, or null
+    const uint32_t* signs;  // 3 x fhtDim/32 words of sign bits (bit = 1 -> +1)
+    int fhtDim, nproj, k;
+    float* P;            // n x nproj projections out
+    int32_t* topK;       // n x 2k out
+    float* chunkMax;     // G x nproj
+    float* chunkMin;     // G x nproj
+    int chunk;           // points per chunk (G = ceil(n / chunk))
+    int32_t* err;        // device flags: [0] negative input, [1] zero point
+    unsigned long long* ties;  // top-k boundary tie counter
+    int do_transform;    // 1: apply transformData; 0: X already transformed
+    float* scale;        // n: per-point norm / sum (scratch)
+    const double* compCosh;  // Chi2/JS: cosh(PI * c * L) for c = 1..components (host-computed)
+    double ln4;              // JS: log(4.0) as the host computes it
+};
+int launch_project(const ProjectArgs& a, cudaStream_t st);
+
+// Random Fourier features for L1/L2: E[p] = [cos(R x_p), sin(R x_p)].
+int launch_rff(const float* Xt, int ld, int n, int d, const float* R, int h, float* E, cudaStream_t st);
+
+struct TopMArgs {
+    const float* P;
+    int n, nproj, m;
+    const float* chunkMax;
+    const float* chunkMin;
+    int G;
+    float* thrMax;       // nproj
+    float* thrMin;       // nproj
+    uint64_t* cand;      // 2*nproj lists x cap entries of (key<<32 | ~index)
+    int32_t* candCount;  // 2*nproj
+    int cap;
+    int32_t* topM;       // nproj x 2m out
+    int32_t* overflow;   // list ids that overflowed (2*nproj), count in overflow_n
+    int32_t* overflow_n;
+    unsigned long long* ties;
+    int32_t* errFlag;    // set when an internal invariant fails
+};
+int launch_topm_thresholds(const TopMArgs& a, cudaStream_t st);
+int launch_topm_collect(const TopMArgs& a, cudaStream_t st);
+int launch_topm_select(const TopMArgs& a, cudaStream_t st);
+int launch_topm_fallback(const TopMArgs& a, int list, uint32_t* hist, cudaStream_t st);
+
+// Exclusive scan of n int64 values (in place allowed); tmp needs
+// scan_tmp_elems(n) entries.
+size_t scan_tmp_elems(size_t n);
+int launch_scan_i64(const int64_t* in, int64_t* out, size_t n, int64_t* tmp, cudaStream_t st);
+
+struct IndexArgs {
+    const int32_t* topK;  // n x 2k
+    int n, k, nproj, m;
+    const int32_t* topM;  // nproj x 2m
+    int64_t* listCount;   // 2*nproj + 1
+    int64_t* listOff;     // 2*nproj + 1
+    int64_t* listFill;    // 2*nproj
+    int2* members;        // n*2k (point, slot)
+    int TM;               // member rows per distance tile
+    int nct;              // candidate tiles per list
+    int64_t* tileOff;     // 2*nproj + 1 (tiles per list, scanned)
+    int32_t* tileList;    // total tiles
+    int32_t* hubCount;    // n: number of top-m lists containing the point
+    int64_t* hubOff;      // n + 1
+    int32_t* hubLists;    // 2*nproj*m: list ids per hub point
+    int64_t* scanTmp;
+};
+int launch_index_count(const IndexArgs& a, cudaStream_t st);
+int launch_index_scatter(const IndexArgs& a, cudaStream_t st);
+int launch_tiles(const IndexArgs& a, int64_t total_tiles, cudaStream_t st);
+int launch_hubs_count(const IndexArgs& a, cudaStream_t st);
+int launch_hubs_scatter(const IndexArgs& a, cudaStream_t st);
+
+struct DistArgs {
+    const float* Xt;
+    int ld, d, dist, n;
+    const int2* members;
+    const int64_t* listOff;
+    const int32_t* tileList;
+    const int64_t* tileOff;
+    int64_t nTiles;       // launch grid (an upper bound)
+    const int64_t* tileTotal;  // device: actual number of tiles
+    const int32_t* topM;
+    int nproj, m, k, W;   // W = 64-bit mask words per (point, slot)
+    int nct;              // candidate tiles per list
+    float eps;
+    uint64_t* masks;      // n x 2k x W
+    int32_t* inRaw;       // n
+    float* dists;         // n x 2k x m (optional)
+    unsigned long long* pairs;  // pass counter
+};
+int launch_dist(const DistArgs& a, cudaStream_t st);
+
+struct CoreArgs {
+    int n, k, m, W, nproj, minPts;
+    const uint64_t* masks;
+    const int32_t* topK;
+    const int32_t* topM;
+    const int32_t* hubCount;
+    const int64_t* hubOff;
+    const int32_t* hubLists;
+    int32_t* inRaw;
+    int32_t* aCount;
+    int32_t* degree;
+    uint8_t* core;
+    const float* dists;   // sOPTICS: n x 2k x m distances, or null
+    float* coreDist;      // sOPTICS: n (0 for non-core), or null
+};
+int launch_core_dedupe(const CoreArgs& a, cudaStream_t st);
+int launch_core_finish(const CoreArgs& a, cudaStream_t st);
+
+struct ClusterArgs {
+    int n, k, m, W;
+    const uint64_t* masks;
+    const int32_t* topK;
+    const int32_t* topM;
+    const uint8_t* core;
+    int32_t* parent;
+    int32_t* border;
+    int64_t* rootFlag;    // n + 1, scanned into cluster ids
+    int64_t* scanTmp;
+    int32_t* labels;
+    int32_t* nClusters;   // device scalar
+};
+int launch_cluster(const ClusterArgs& a, cudaStream_t st);
+
+}  // namespace sdb

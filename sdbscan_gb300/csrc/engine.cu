@@ -1,0 +1,625 @@
+// The engine behind the C ABI (include/sdbscan_gb300.h): device buffers,
+// host-side random numbers, the stage pipeline of fit_sDbscan / fit_sOptics,
+// and the output accessors.
+//
+// Pipeline of one fit (all on the engine's stream; the only host syncs are
+// at the end of the fit and in the accessors):
+//   upload X -> [L1/L2: pad copy, random Fourier features]
+//   -> k_colstats + k_project   transform, embedding, 3 x (signs + FWHT), top-k,
+//                               projections, chunk extremes
+//   -> top-m                    thresholds, collect, exact select (+ fallback)
+//   -> index                    list members (inverted top-k), tiles, hub lists
+//   -> k_dist                   grouped gathered distances, eps masks, in-counts
+//   -> core                     de-duplicated neighbourhood sizes, core flags
+//   -> cluster                  union-find labels   |  sOPTICS: core distance,
+//                                                    neighbour lists, ordering
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/sdbscan_gb300.h"
+#include "common.cuh"
+#include "engine_internal.h"
+
+namespace sdb {
+int launch_tile_offsets(const IndexArgs& a, cudaStream_t st);
+int launch_i32_to_i64(const int32_t* in, int64_t* out, int n, cudaStream_t st);
+int dist_tile_rows();
+int dist_tile_cols();
+int launch_pad_copy(const float* X, int n, int d, float* Xt, int ld, cudaStream_t st);
+}  // namespace sdb
+
+using namespace sdb;
+
+namespace {
+
+const char* dist_name(int d) {
+    switch (d) {
+        case SDB_COSINE: return "Cosine";
+        case SDB_L1: return "L1";
+        case SDB_L2: return "L2";
+        case SDB_CHI2: return "Chi2";
+        case SDB_JS: return "JS";
+    }
+    return "?";
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// device buffer helpers
+// ---------------------------------------------------------------------------
+bool sdb_engine::ensure(DevBuf& b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (b.bytes >= bytes) return true;
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+    cudaError_t e = cudaMalloc(&b.ptr, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        fail(SDB_ERR_NOMEM, std::string("device allocation of ") + std::to_string(bytes) + " bytes failed: " +
+                                cudaGetErrorString(e));
+        return false;
+    }
+    b.bytes = bytes;
+    return true;
+}
+
+sdb_status sdb_engine::fail(sdb_status s, const std::string& msg) {
+    err = msg;
+    return s;
+}
+
+sdb_status sdb_engine::cuda_fail(cudaError_t e, const char* where) {
+    return fail(SDB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+void sdb_engine::free_all() {
+    for (DevBuf* b : all_bufs())
+        if (b->ptr) {
+            cudaFree(b->ptr);
+            b->ptr = nullptr;
+            b->bytes = 0;
+        }
+}
+
+std::vector<DevBuf*> sdb_engine::all_bufs() {
+    return {&Xin, &Xt, &scale, &P, &topK, &chunkMax, &chunkMin, &thr, &cand, &candCount, &topM, &listCount,
+            &listOff, &listFill, &members, &tileOff, &tileList, &hubCount, &hubOff, &hubLists, &masks, &inRaw,
+            &aCount, &degree, &core, &parent, &border, &rootFlag, &labels, &nClusters, &scanTmp, &errFlags,
+            &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill};
+}
+
+// ---------------------------------------------------------------------------
+// parameters and host random numbers
+// ---------------------------------------------------------------------------
+sdb_status sdb_engine::derive() {
+    const sdb_params& p = prm;
+    if (p.n_proj < 1 || p.topK < 1 || p.topM < 1) return fail(SDB_ERR_ARG, "n_proj, topK and topM must be >= 1");
+    if (p.topK > p.n_proj) return fail(SDB_ERR_ARG, "topK must be <= n_proj");
+    if (p.topM > n) return fail(SDB_ERR_ARG, "topM must be <= n_points");
+    if (p.distance < SDB_COSINE || p.distance > SDB_JS) return fail(SDB_ERR_ARG, "unknown distance");
+    if (p.clusterNoise != 0) return fail(SDB_ERR_ARG, "clusterNoise != 0 (sDbscan-1NN noise labelling) is not supported");
+    if (p.precision != SDB_PREC_FP32 && p.precision != SDB_PREC_BF16) return fail(SDB_ERR_ARG, "unknown precision");
+    ker = p.distance == SDB_COSINE ? d : p.ker_n_features;  // src/sDbscan.h:102-104
+    if (ker < 1) return fail(SDB_ERR_ARG, "ker_n_features must be >= 1");
+    if ((p.distance == SDB_L1 || p.distance == SDB_L2) && ker % 2) return fail(SDB_ERR_ARG, "ker_n_features must be even for L1/L2");
+    const int mx = std::max(p.n_proj, ker);
+    fhtDim = 1 << (int)std::ceil(std::log2((double)mx));  // src/sDbscan.h:107
+    if (fhtDim < 16) return fail(SDB_ERR_ARG, "max(n_proj, ker_n_features) must be >= 9");
+    if (fhtDim > 2048) return fail(SDB_ERR_ARG, "max(n_proj, ker_n_features) must be <= 2048");
+    if (p.topK > 31) return fail(SDB_ERR_ARG, "topK must be <= 31");
+    ld = (d + 3) & ~3;
+    return SDB_OK;
+}
+
+void sdb_engine::host_random(int seedUsed) {
+    // bitHD3Generator (src/Utilities.h:47-64): fhtDim * 3 bits, one draw each.
+    std::default_random_engine gen((unsigned)seedUsed);
+    std::uniform_int_distribution<uint32_t> u(0, 1);
+    const int nbits = 3 * fhtDim;
+    hostSigns.assign((nbits + 31) / 32, 0u);
+    for (int i = 0; i < nbits; ++i)
+        if (u(gen) & 1) hostSigns[i >> 5] |= 1u << (i & 31);
+    // gaussGenerator / cauchyGenerator (src/Utilities.h:76-122), (ker/2) x d,
+    // column first; stored transposed (row r = R(r, :)) with row stride ld.
+    hostRt.clear();
+    if (prm.distance == SDB_L1 || prm.distance == SDB_L2) {
+        const int h = ker / 2;
+        hostRt.assign((size_t)h * ld, 0.0f);
+        std::default_random_engine g2((unsigned)seedUsed);
+        if (prm.distance == SDB_L2) {
+            std::normal_distribution<float> nd(0.0f, 1.0f / prm.ker_sigma);
+            for (int c = 0; c < d; ++c)
+                for (int r = 0; r < h; ++r) hostRt[(size_t)r * ld + c] = nd(g2);
+        } else {
+            std::cauchy_distribution<float> cd(0.0f, 1.0f / prm.ker_sigma);
+            for (int c = 0; c < d; ++c)
+                for (int r = 0; r < h; ++r) hostRt[(size_t)r * ld + c] = cd(g2);
+        }
+    }
+    // Chi2 / JS constants (src/Utilities.h:134-160, :176-204) evaluated on the host.
+    hostCosh.clear();
+    if (prm.distance == SDB_CHI2 || prm.distance == SDB_JS) {
+        const int comps = ((ker / d) - 1) / 2;
+        const double PI = 3.141592653589793238460;
+        for (int c = 1; c <= comps; ++c) hostCosh.push_back(std::cosh(PI * c * (double)prm.ker_intervalSampling));
+    }
+    ln4 = std::log(4.0);
+}
+
+// ---------------------------------------------------------------------------
+// the fit pipeline
+// ---------------------------------------------------------------------------
+sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts, bool optics) {
+    if (!paramsSet) return fail(SDB_ERR_STATE, "set_params must be called before a fit");
+    haveLabels = haveOptics = false;
+    if (optics && minPts < 2) return fail(SDB_ERR_ARG, "minPts must be >= 2 for sOPTICS");
+    if (X == nullptr) return fail(SDB_ERR_ARG, "X is null");
+    sdb_status s = derive();
+    if (s != SDB_OK) return s;
+    const sdb_params& p = prm;
+    const int k = p.topK, m = p.topM, D = p.n_proj;
+    seedUsed = p.random_seed >= 0 ? p.random_seed
+                                  : (int)(unsigned)std::chrono::system_clock::now().time_since_epoch().count();
+    host_random(seedUsed);
+    cudaError_t ce = cudaSetDevice(device);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
+
+    const int TMr = dist_tile_rows(), TNc = dist_tile_cols();
+    const int nct = (m + TNc - 1) / TNc;
+    const int W = (m + 63) / 64;
+    const int L = 2 * D;
+    const int chunk = std::max(8, (n + std::max(1024, 4 * m) - 1) / std::max(1024, 4 * m));
+    const int G = (n + chunk - 1) / chunk;
+    int cap = 256;
+    while (cap < 8 * m) cap <<= 1;
+    const int64_t maxTiles = ((int64_t)n * 2 * k / TMr + L) * nct;
+    const bool rff = p.distance == SDB_L1 || p.distance == SDB_L2;
+
+    // allocations (grow-only)
+    bool ok = true;
+    if (!xOnDevice) ok &= ensure(Xin, sizeof(float) * (size_t)n * d);
+    ok &= ensure(Xt, sizeof(float) * (size_t)n * ld) && ensure(scale, sizeof(float) * n) &&
+          ensure(P, sizeof(float) * (size_t)n * D) && ensure(topK, sizeof(int32_t) * (size_t)n * 2 * k) &&
+          ensure(chunkMax, sizeof(float) * (size_t)G * D) && ensure(chunkMin, sizeof(float) * (size_t)G * D) &&
+          ensure(thr, sizeof(float) * 2 * D) && ensure(cand, sizeof(uint64_t) * (size_t)L * cap) &&
+          ensure(candCount, sizeof(int32_t) * L) && ensure(topM, sizeof(int32_t) * (size_t)D * 2 * m) &&
+          ensure(listCount, sizeof(int64_t) * (L + 1)) && ensure(listOff, sizeof(int64_t) * (L + 1)) &&
+          ensure(listFill, sizeof(int64_t) * L) && ensure(members, sizeof(int2) * (size_t)n * 2 * k) &&
+          ensure(tileOff, sizeof(int64_t) * (L + 1)) && ensure(tileList, sizeof(int32_t) * (size_t)maxTiles) &&
+          ensure(hubCount, sizeof(int32_t) * n) && ensure(hubOff, sizeof(int64_t) * (n + 1)) &&
+          ensure(hubLists, sizeof(int32_t) * (size_t)L * m) &&
+          ensure(masks, sizeof(uint64_t) * (size_t)n * 2 * k * W) && ensure(inRaw, sizeof(int32_t) * n) &&
+          ensure(aCount, sizeof(int32_t) * n) && ensure(degree, sizeof(int32_t) * n) && ensure(core, n) &&
+          ensure(parent, sizeof(int32_t) * n) && ensure(border, sizeof(int32_t) * n) &&
+          ensure(rootFlag, sizeof(int64_t) * (n + 1)) && ensure(labels, sizeof(int32_t) * n) &&
+          ensure(nClusters, sizeof(int32_t) * 4) &&
+          ensure(scanTmp, sizeof(int64_t) * scan_tmp_elems((size_t)std::max(n + 1, L + 1))) &&
+          ensure(errFlags, sizeof(int32_t) * 8) && ensure(counters, sizeof(unsigned long long) * 8) &&
+          ensure(signs, sizeof(uint32_t) * hostSigns.size()) &&
+          ensure(compCosh, sizeof(double) * std::max<size_t>(1, hostCosh.size()));
+    if (rff) ok &= ensure(E, sizeof(float) * (size_t)n * ker) && ensure(Rt, sizeof(float) * hostRt.size());
+    if (optics) ok &= ensure(dists, sizeof(float) * (size_t)n * 2 * k * m) && ensure(coreDist, sizeof(float) * n);
+    if (!ok) return SDB_ERR_NOMEM;
+
+    cudaStream_t st = stream;
+    int launches = 0;
+    auto L_ = [&](int r) {
+        if (r < 0) ok = false;
+        else launches += r;
+    };
+#define SDB_CK(call)                                     \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+    SDB_CK(cudaEventRecord(ev[0], st));
+    const float* Xd = X;
+    if (!xOnDevice) {
+        SDB_CK(cudaMemcpyAsync(Xin.ptr, X, sizeof(float) * (size_t)n * d, cudaMemcpyHostToDevice, st));
+        Xd = static_cast<const float*>(Xin.ptr);
+    }
+    SDB_CK(cudaEventRecord(ev[1], st));
+    SDB_CK(cudaMemcpyAsync(signs.ptr, hostSigns.data(), sizeof(uint32_t) * hostSigns.size(), cudaMemcpyHostToDevice, st));
+    if (!hostCosh.empty())
+        SDB_CK(cudaMemcpyAsync(compCosh.ptr, hostCosh.data(), sizeof(double) * hostCosh.size(), cudaMemcpyHostToDevice, st));
+    SDB_CK(cudaMemsetAsync(errFlags.ptr, 0, sizeof(int32_t) * 8, st));
+    SDB_CK(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long) * 8, st));
+    unsigned long long* ctr = static_cast<unsigned long long*>(counters.ptr);
+
+    // ---- stage 1: transform, embedding, projection, top-k ------------------
+    ProjectArgs pa{};
+    pa.X = Xd;
+    pa.ldx = d;
+    pa.Xt = f32(Xt);
+    pa.ld = ld;
+    pa.n = n;
+    pa.d = d;
+    pa.dist = p.distance;
+    pa.ker = ker;
+    pa.kerSam = p.ker_intervalSampling;
+    pa.E = nullptr;
+    pa.signs = static_cast<const uint32_t*>(signs.ptr);
+    pa.fhtDim = fhtDim;
+    pa.nproj = D;
+    pa.k = k;
+    pa.P = f32(P);
+    pa.topK = i32(topK);
+    pa.chunkMax = f32(chunkMax);
+    pa.chunkMin = f32(chunkMin);
+    pa.chunk = chunk;
+    pa.err = i32(errFlags);
+    pa.ties = ctr + 0;
+    pa.do_transform = 1;
+    pa.scale = f32(scale);
+    pa.compCosh = static_cast<const double*>(compCosh.ptr);
+    pa.ln4 = ln4;
+    if (rff) {
+        SDB_CK(cudaMemcpyAsync(Rt.ptr, hostRt.data(), sizeof(float) * hostRt.size(), cudaMemcpyHostToDevice, st));
+        L_(launch_pad_copy(Xd, n, d, f32(Xt), ld, st));
+        L_(launch_rff(f32(Xt), ld, n, d, f32(Rt), ker / 2, f32(E), st));
+        pa.X = f32(Xt);
+        pa.ldx = ld;
+        pa.E = f32(E);
+        pa.do_transform = 0;
+    }
+    L_(launch_project(pa, st));
+    if (!ok) return fail(SDB_ERR_CUDA, std::string("projection launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+    SDB_CK(cudaEventRecord(ev[2], st));
+
+    // ---- stage 2: per-vector top-m -----------------------------------------
+    TopMArgs ta{};
+    ta.P = f32(P);
+    ta.n = n;
+    ta.nproj = D;
+    ta.m = m;
+    ta.chunkMax = f32(chunkMax);
+    ta.chunkMin = f32(chunkMin);
+    ta.G = G;
+    ta.thrMax = f32(thr);
+    ta.thrMin = f32(thr) + D;
+    ta.cand = static_cast<uint64_t*>(cand.ptr);
+    ta.candCount = i32(candCount);
+    ta.cap = cap;
+    ta.topM = i32(topM);
+    ta.ties = ctr + 1;
+    ta.errFlag = i32(errFlags) + 3;
+    SDB_CK(cudaMemsetAsync(candCount.ptr, 0, sizeof(int32_t) * L, st));
+    L_(launch_topm_thresholds(ta, st));
+    L_(launch_topm_collect(ta, st));
+    L_(launch_topm_select(ta, st));
+    if (!ok) return fail(SDB_ERR_CUDA, std::string("top-m launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+    SDB_CK(cudaEventRecord(ev[3], st));
+
+    // ---- stage 3: inverted index, tiles, hub lists ---------------------------
+    IndexArgs ia{};
+    ia.topK = i32(topK);
+    ia.n = n;
+    ia.k = k;
+    ia.nproj = D;
+    ia.m = m;
+    ia.topM = i32(topM);
+    ia.listCount = i64(listCount);
+    ia.listOff = i64(listOff);
+    ia.listFill = i64(listFill);
+    ia.members = static_cast<int2*>(members.ptr);
+    ia.TM = TMr;
+    ia.nct = nct;
+    ia.tileOff = i64(tileOff);
+    ia.tileList = i32(tileList);
+    ia.hubCount = i32(hubCount);
+    ia.hubOff = i64(hubOff);
+    ia.hubLists = i32(hubLists);
+    ia.scanTmp = i64(scanTmp);
+    SDB_CK(cudaMemsetAsync(listCount.ptr, 0, sizeof(int64_t) * (L + 1), st));
+    SDB_CK(cudaMemsetAsync(listFill.ptr, 0, sizeof(int64_t) * L, st));
+    SDB_CK(cudaMemsetAsync(hubCount.ptr, 0, sizeof(int32_t) * n, st));
+    SDB_CK(cudaMemsetAsync(hubOff.ptr, 0, sizeof(int64_t) * (n + 1), st));
+    L_(launch_index_count(ia, st));
+    L_(launch_scan_i64(i64(listCount), i64(listOff), (size_t)L + 1, i64(scanTmp), st));
+    L_(launch_index_scatter(ia, st));
+    L_(launch_tile_offsets(ia, st));
+    L_(launch_tiles(ia, 0, st));
+    L_(launch_hubs_count(ia, st));
+    L_(launch_i32_to_i64(i32(hubCount), i64(hubOff), n, st));
+    L_(launch_scan_i64(i64(hubOff), i64(hubOff), (size_t)n + 1, i64(scanTmp), st));
+    SDB_CK(cudaMemsetAsync(hubCount.ptr, 0, sizeof(int32_t) * n, st));
+    L_(launch_hubs_scatter(ia, st));
+    if (!ok) return fail(SDB_ERR_CUDA, std::string("index launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+    SDB_CK(cudaEventRecord(ev[4], st));
+
+    // ---- stage 4: distances + eps --------------------------------------------
+    DistArgs da{};
+    da.Xt = f32(Xt);
+    da.ld = ld;
+    da.d = d;
+    da.dist = p.distance;
+    da.n = n;
+    da.members = static_cast<const int2*>(members.ptr);
+    da.listOff = i64(listOff);
+    da.tileList = i32(tileList);
+    da.tileOff = i64(tileOff);
+    da.nTiles = maxTiles;
+    da.tileTotal = i64(tileOff) + L;
+    da.topM = i32(topM);
+    da.nproj = D;
+    da.m = m;
+    da.k = k;
+    da.W = W;
+    da.nct = nct;
+    da.eps = eps;
+    da.masks = static_cast<uint64_t*>(masks.ptr);
+    da.inRaw = i32(inRaw);
+    da.dists = optics ? f32(dists) : nullptr;
+    da.pairs = ctr + 3;
+    SDB_CK(cudaMemsetAsync(inRaw.ptr, 0, sizeof(int32_t) * n, st));
+    L_(launch_dist(da, st));
+    if (!ok) return fail(SDB_ERR_CUDA, std::string("distance launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+    SDB_CK(cudaEventRecord(ev[5], st));
+
+    // ---- stage 5: neighbourhood sizes, core flags -----------------------------
+    CoreArgs ca{};
+    ca.n = n;
+    ca.k = k;
+    ca.m = m;
+    ca.W = W;
+    ca.nproj = D;
+    ca.minPts = minPts;
+    ca.masks = static_cast<const uint64_t*>(masks.ptr);
+    ca.topK = i32(topK);
+    ca.topM = i32(topM);
+    ca.hubCount = i32(hubCount);
+    ca.hubOff = i64(hubOff);
+    ca.hubLists = i32(hubLists);
+    ca.inRaw = i32(inRaw);
+    ca.aCount = i32(aCount);
+    ca.degree = i32(degree);
+    ca.core = static_cast<uint8_t*>(core.ptr);
+    ca.dists = optics ? f32(dists) : nullptr;
+    ca.coreDist = optics ? f32(coreDist) : nullptr;
+    L_(launch_core_dedupe(ca, st));
+    L_(launch_core_finish(ca, st));
+    if (!ok) return fail(SDB_ERR_CUDA, std::string("core launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+    SDB_CK(cudaEventRecord(ev[6], st));
+
+    // ---- stage 6: clusters or sOPTICS ------------------------------------------
+    if (!optics) {
+        ClusterArgs ka{};
+        ka.n = n;
+        ka.k = k;
+        ka.m = m;
+        ka.W = W;
+        ka.masks = static_cast<const uint64_t*>(masks.ptr);
+        ka.topK = i32(topK);
+        ka.topM = i32(topM);
+        ka.core = static_cast<const uint8_t*>(core.ptr);
+        ka.parent = i32(parent);
+        ka.border = i32(border);
+        ka.rootFlag = i64(rootFlag);
+        ka.scanTmp = i64(scanTmp);
+        ka.labels = i32(labels);
+        ka.nClusters = i32(nClusters);
+        L_(launch_cluster(ka, st));
+        if (!ok) return fail(SDB_ERR_CUDA, std::string("cluster launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+    } else {
+        s = optics_stage(eps, minPts, launches);
+        if (s != SDB_OK) return s;
+    }
+    SDB_CK(cudaEventRecord(ev[7], st));
+    SDB_CK(cudaMemcpyAsync(hostErr, errFlags.ptr, sizeof(int32_t) * 8, cudaMemcpyDeviceToHost, st));
+    SDB_CK(cudaMemcpyAsync(hostCounters, counters.ptr, sizeof(unsigned long long) * 8, cudaMemcpyDeviceToHost, st));
+    SDB_CK(cudaEventRecord(ev[8], st));
+    SDB_CK(cudaStreamSynchronize(st));
+    launchCount = launches;
+#undef SDB_CK
+    for (int i = 0; i < 8; ++i) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+        stageMs[i] = ms;
+    }
+    {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ev[0], ev[8]);
+        stageMs[8] = ms;
+    }
+    if (hostErr[0]) return fail(SDB_ERR_NEGATIVE, "X is not non-negative (Chi2/JS need nonnegative data)");
+    if (hostErr[1])
+        return fail(SDB_ERR_ZERO_POINT, p.distance == SDB_COSINE ? "X has a point of zero norm (Cosine)"
+                                                                 : "X has a point of zero sum (Chi2/JS)");
+    if (hostErr[2]) return fail(SDB_ERR_ARG, "X has a non-finite value");
+    if (hostErr[3]) return fail(SDB_ERR_INTERNAL, "top-m selection found fewer candidates than topM");
+    if (optics) haveOptics = true;
+    else haveLabels = true;
+    haveFit = true;
+    lastOptics = optics;
+    if (p.verbose) {
+        std::printf("sdbscan_gb300 %s fit: n=%d d=%d D=%d k=%d m=%d dist=%s eps=%g minPts=%d\n",
+                    optics ? "sOPTICS" : "sDBSCAN", n, d, D, k, m, dist_name(p.distance), eps, minPts);
+        const char* names[9] = {"upload", "project+topk", "topm", "index", "distances", "core", "cluster/optics",
+                                "readback", "total"};
+        for (int i = 0; i < 9; ++i) std::printf("  %-14s %9.3f ms\n", names[i], stageMs[i]);
+    }
+    err.clear();
+    return SDB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void sdb_params_default(sdb_params* p) {
+    if (!p) return;
+    p->n_proj = 1024;
+    p->topK = 10;
+    p->topM = 50;
+    p->distance = SDB_COSINE;
+    p->ker_n_features = 1024;
+    p->ker_sigma = 1.0f;
+    p->ker_intervalSampling = 0.4f;
+    p->clusterNoise = 0;
+    p->samplingProb = 0.01f;
+    p->verbose = 0;
+    p->n_threads = -1;
+    p->random_seed = -1;
+    p->precision = SDB_PREC_FP32;
+}
+
+sdb_status sdb_engine_create(int32_t n_points, int32_t n_features, int32_t device, sdb_engine** out) {
+    if (!out) return SDB_ERR_ARG;
+    *out = nullptr;
+    if (n_points < 1 || n_features < 1) return SDB_ERR_ARG;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return SDB_ERR_CUDA;
+    }
+    if (device < 0 || device >= count) return SDB_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return SDB_ERR_CUDA;
+    sdb_engine* e = new sdb_engine();
+    e->n = n_points;
+    e->d = n_features;
+    e->device = device;
+    sdb_params_default(&e->prm);
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete e;
+        return SDB_ERR_CUDA;
+    }
+    for (int i = 0; i < 9; ++i)
+        if (cudaEventCreate(&e->ev[i]) != cudaSuccess) {
+            delete e;
+            return SDB_ERR_CUDA;
+        }
+    if (cudaMallocHost(&e->hostErr, sizeof(int32_t) * 8) != cudaSuccess ||
+        cudaMallocHost(&e->hostCounters, sizeof(unsigned long long) * 8) != cudaSuccess) {
+        delete e;
+        return SDB_ERR_CUDA;
+    }
+    *out = e;
+    return SDB_OK;
+}
+
+void sdb_engine_destroy(sdb_engine* e) {
+    if (!e) return;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    e->free_all();
+    for (int i = 0; i < 9; ++i)
+        if (e->ev[i]) cudaEventDestroy(e->ev[i]);
+    if (e->hostErr) cudaFreeHost(e->hostErr);
+    if (e->hostCounters) cudaFreeHost(e->hostCounters);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+}
+
+sdb_status sdb_set_params(sdb_engine* e, const sdb_params* p) {
+    if (!e || !p) return SDB_ERR_ARG;
+    e->prm = *p;
+    e->paramsSet = true;
+    sdb_status s = e->derive();
+    if (s != SDB_OK) e->paramsSet = false;
+    return s;
+}
+
+sdb_status sdb_fit_sdbscan(sdb_engine* e, const float* X, float eps, int32_t minPts) {
+    return e ? e->fit(X, false, eps, minPts, false) : SDB_ERR_ARG;
+}
+sdb_status sdb_fit_sdbscan_device(sdb_engine* e, const float* X, float eps, int32_t minPts) {
+    return e ? e->fit(X, true, eps, minPts, false) : SDB_ERR_ARG;
+}
+sdb_status sdb_fit_soptics(sdb_engine* e, const float* X, float eps, int32_t minPts) {
+    return e ? e->fit(X, false, eps, minPts, true) : SDB_ERR_ARG;
+}
+sdb_status sdb_fit_soptics_device(sdb_engine* e, const float* X, float eps, int32_t minPts) {
+    return e ? e->fit(X, true, eps, minPts, true) : SDB_ERR_ARG;
+}
+
+sdb_status sdb_get_labels(sdb_engine* e, int32_t* labels, int32_t* n_clusters) {
+    if (!e) return SDB_ERR_ARG;
+    if (!e->haveLabels) return e->fail(SDB_ERR_STATE, "no sDbscan result: call sdb_fit_sdbscan first");
+    cudaSetDevice(e->device);
+    if (labels) {
+        cudaError_t c = cudaMemcpyAsync(labels, e->labels.ptr, sizeof(int32_t) * e->n, cudaMemcpyDeviceToHost, e->stream);
+        if (c != cudaSuccess) return e->cuda_fail(c, "labels download");
+    }
+    int32_t nc = 0;
+    cudaError_t c = cudaMemcpyAsync(&nc, e->nClusters.ptr, sizeof(int32_t), cudaMemcpyDeviceToHost, e->stream);
+    if (c != cudaSuccess) return e->cuda_fail(c, "n_clusters download");
+    c = cudaStreamSynchronize(e->stream);
+    if (c != cudaSuccess) return e->cuda_fail(c, "labels sync");
+    if (n_clusters) *n_clusters = nc;
+    return SDB_OK;
+}
+
+sdb_status sdb_get_optics(sdb_engine* e, int32_t* ordering, float* reach) {
+    if (!e) return SDB_ERR_ARG;
+    if (!e->haveOptics) return e->fail(SDB_ERR_STATE, "no sOPTICS result: call sdb_fit_soptics first");
+    if (ordering) std::memcpy(ordering, e->hostOrdering.data(), sizeof(int32_t) * e->hostOrdering.size());
+    if (reach) std::memcpy(reach, e->hostReach.data(), sizeof(float) * e->hostReach.size());
+    return SDB_OK;
+}
+
+sdb_status sdb_clear(sdb_engine* e) {
+    if (!e) return SDB_ERR_ARG;
+    e->haveLabels = e->haveOptics = e->haveFit = false;
+    e->hostOrdering.clear();
+    e->hostReach.clear();
+    return SDB_OK;
+}
+
+static sdb_status download(sdb_engine* e, void* dst, const DevBuf& b, size_t bytes) {
+    if (!e->haveFit) return e->fail(SDB_ERR_STATE, "no fit yet");
+    if (!dst) return SDB_ERR_ARG;
+    cudaSetDevice(e->device);
+    cudaError_t c = cudaMemcpyAsync(dst, b.ptr, bytes, cudaMemcpyDeviceToHost, e->stream);
+    if (c == cudaSuccess) c = cudaStreamSynchronize(e->stream);
+    return c == cudaSuccess ? SDB_OK : e->cuda_fail(c, "download");
+}
+
+sdb_status sdb_get_topk(sdb_engine* e, int32_t* out) {
+    return e ? download(e, out, e->topK, sizeof(int32_t) * (size_t)e->n * 2 * e->prm.topK) : SDB_ERR_ARG;
+}
+sdb_status sdb_get_topm(sdb_engine* e, int32_t* out) {
+    return e ? download(e, out, e->topM, sizeof(int32_t) * (size_t)e->prm.n_proj * 2 * e->prm.topM) : SDB_ERR_ARG;
+}
+sdb_status sdb_get_core(sdb_engine* e, uint8_t* core, int32_t* degree) {
+    if (!e) return SDB_ERR_ARG;
+    sdb_status s = SDB_OK;
+    if (core) s = download(e, core, e->core, e->n);
+    if (s == SDB_OK && degree) s = download(e, degree, e->degree, sizeof(int32_t) * e->n);
+    return s;
+}
+sdb_status sdb_get_core_dist(sdb_engine* e, float* out) {
+    if (!e) return SDB_ERR_ARG;
+    if (!e->lastOptics) return e->fail(SDB_ERR_STATE, "core distances exist after sdb_fit_soptics only");
+    return download(e, out, e->coreDist, sizeof(float) * e->n);
+}
+sdb_status sdb_get_projections(sdb_engine* e, float* out) {
+    return e ? download(e, out, e->P, sizeof(float) * (size_t)e->n * e->prm.n_proj) : SDB_ERR_ARG;
+}
+sdb_status sdb_get_counters(sdb_engine* e, int64_t* out, int32_t n_out) {
+    if (!e || !out) return SDB_ERR_ARG;
+    int64_t v[4] = {(int64_t)e->hostCounters[0], (int64_t)e->hostCounters[1], (int64_t)e->launchCount,
+                    (int64_t)e->hostCounters[3]};
+    for (int i = 0; i < n_out && i < 4; ++i) out[i] = v[i];
+    return SDB_OK;
+}
+sdb_status sdb_get_stage_ms(sdb_engine* e, float* ms, int32_t n_ms) {
+    if (!e || !ms) return SDB_ERR_ARG;
+    for (int i = 0; i < n_ms && i < 9; ++i) ms[i] = e->stageMs[i];
+    return SDB_OK;
+}
+void* sdb_engine_stream(sdb_engine* e) { return e ? (void*)e->stream : nullptr; }
+const char* sdb_last_error(sdb_engine* e) { return e ? e->err.c_str() : "null engine"; }
+
+}  // extern "C"

@@ -1,0 +1,59 @@
+// The engine object behind the opaque sdb_engine handle of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/sdbscan_gb300.h"
+
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct sdb_engine {
+    int n = 0, d = 0, device = 0;
+    sdb_params prm{};
+    bool paramsSet = false;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[9] = {};
+    std::string err;
+
+    // derived from the parameters
+    int ker = 0, fhtDim = 0, ld = 0, seedUsed = 0;
+    double ln4 = 0.0;
+    std::vector<uint32_t> hostSigns;
+    std::vector<float> hostRt;
+    std::vector<double> hostCosh;
+
+    // device buffers (grow-only; kept across fits)
+    DevBuf Xin, Xt, scale, P, topK, chunkMax, chunkMin, thr, cand, candCount, topM, listCount, listOff, listFill,
+        members, tileOff, tileList, hubCount, hubOff, hubLists, masks, inRaw, aCount, degree, core, parent, border,
+        rootFlag, labels, nClusters, scanTmp, errFlags, counters, E, Rt, signs, compCosh, dists, coreDist, nbOff,
+        nbIdx, nbDist, nbFill;
+
+    // results
+    bool haveLabels = false, haveOptics = false, haveFit = false, lastOptics = false;
+    std::vector<int32_t> hostOrdering;
+    std::vector<float> hostReach;
+    int32_t* hostErr = nullptr;
+    unsigned long long* hostCounters = nullptr;
+    int launchCount = 0;
+    float stageMs[9] = {};
+
+    bool ensure(DevBuf& b, size_t bytes);
+    sdb_status fail(sdb_status s, const std::string& msg);
+    sdb_status cuda_fail(cudaError_t e, const char* where);
+    void free_all();
+    std::vector<DevBuf*> all_bufs();
+    sdb_status derive();
+    void host_random(int seed);
+    sdb_status fit(const float* X, bool xOnDevice, float eps, int minPts, bool optics);
+    sdb_status optics_stage(float eps, int minPts, int& launches);
+
+    static float* f32(DevBuf& b) { return static_cast<float*>(b.ptr); }
+    static int32_t* i32(DevBuf& b) { return static_cast<int32_t*>(b.ptr); }
+    static int64_t* i64(DevBuf& b) { return static_cast<int64_t*>(b.ptr); }
+};

@@ -1,0 +1,125 @@
+#include "sDbscan.h"
+
+#include <cmath>
+#include <fstream>
+#include <stdexcept>
+#include <string>
+
+namespace {
+
+int dist_code(const std::string& s) {
+    if (s == "Cosine") return SDB_COSINE;
+    if (s == "L1") return SDB_L1;
+    if (s == "L2") return SDB_L2;
+    if (s == "Chi2") return SDB_CHI2;
+    if (s == "JS") return SDB_JS;
+    throw std::invalid_argument("Error: The distance is not support: " + s);
+}
+
+const char* dist_str(int c) {
+    static const char* names[] = {"Cosine", "L1", "L2", "Chi2", "JS"};
+    return (c >= 0 && c <= 4) ? names[c] : "?";
+}
+
+std::string int2str(long x) { return std::to_string(x); }
+
+}  // namespace
+
+sDbscan::sDbscan(int n, int d, int device) : n_(n), d_(d) {
+    sdb_params_default(&prm_);
+    prm_.topK = 5;        // C++ default of set_params (src/sDbscan.h:79)
+    prm_.n_threads = 8;
+    check(sdb_engine_create(n, d, device, &eng_), "sDbscan(n, d)");
+}
+
+sDbscan::~sDbscan() {
+    if (eng_) sdb_engine_destroy(eng_);
+}
+
+void sDbscan::check(sdb_status s, const char* what) {
+    if (s == SDB_OK) return;
+    std::string msg = std::string(what) + " failed";
+    if (eng_) {
+        const char* e = sdb_last_error(eng_);
+        if (e && *e) msg += std::string(": ") + e;
+    } else {
+        msg += " (status " + std::to_string((int)s) + ")";
+    }
+    if (s == SDB_ERR_ARG || s == SDB_ERR_NEGATIVE || s == SDB_ERR_ZERO_POINT) throw std::invalid_argument(msg);
+    throw std::runtime_error(msg);
+}
+
+void sDbscan::push_params() { check(sdb_set_params(eng_, &prm_), "set_params"); }
+
+void sDbscan::set_params(int numProj, int k, int m, std::string dist, int kerDim, float kerSigma, float kerSam,
+                         int noiseClustering, float prob, bool ver, std::string filename, int numThreads,
+                         int randomSeed) {
+    prm_.n_proj = numProj;
+    prm_.topK = k;
+    prm_.topM = m;
+    prm_.distance = dist_code(dist);
+    prm_.ker_n_features = kerDim;
+    prm_.ker_sigma = kerSigma;
+    prm_.ker_intervalSampling = kerSam;
+    prm_.clusterNoise = noiseClustering;
+    prm_.samplingProb = prob;
+    prm_.verbose = ver ? 1 : 0;
+    prm_.n_threads = numThreads;
+    prm_.random_seed = randomSeed;
+    output_ = filename;
+    push_params();
+}
+
+void sDbscan::set_kernel_params(std::string dist, int kerDim, float kerSigma, float kerSam) {
+    prm_.distance = dist_code(dist);
+    prm_.ker_n_features = kerDim;
+    prm_.ker_sigma = kerSigma;
+    prm_.ker_intervalSampling = kerSam;
+    push_params();
+}
+
+void sDbscan::clear() {
+    labels_.clear();
+    n_clusters_ = 0;
+    ordering_.clear();
+    reachability_.clear();
+    sdb_clear(eng_);
+}
+
+void sDbscan::set_topM(int m) { prm_.topM = m; push_params(); }
+void sDbscan::set_topK(int k) { prm_.topK = k; push_params(); }
+void sDbscan::set_proj(int p) { prm_.n_proj = p; push_params(); }
+void sDbscan::set_clusterNoise(int c) { prm_.clusterNoise = c; push_params(); }
+void sDbscan::set_threads(int t) { prm_.n_threads = t; }
+void sDbscan::set_precision(int precision) { prm_.precision = precision; push_params(); }
+
+void sDbscan::fit_sDbscan(const float* X, float eps, int minPts) {
+    check(sdb_fit_sdbscan(eng_, X, eps, minPts), "fit_sDbscan");
+    labels_.assign(n_, -1);
+    int32_t nc = 0;
+    check(sdb_get_labels(eng_, labels_.data(), &nc), "fit_sDbscan (labels)");
+    n_clusters_ = nc;
+    if (prm_.verbose) {  // output file written when verbose (src/sDbscan.cpp:878-889)
+        const std::string f = output_ + "_" + dist_str(prm_.distance) + "_Eps_" + int2str(std::lround(1000 * eps)) +
+                              "_MinPts_" + int2str(minPts) + "_KerFeatures_" +
+                              int2str(prm_.distance == SDB_COSINE ? d_ : prm_.ker_n_features) + "_NumProj_" +
+                              int2str(prm_.n_proj) + "_TopM_" + int2str(prm_.topM) + "_TopK_" + int2str(prm_.topK);
+        std::ofstream out(f);
+        for (int v : labels_) out << v << '\n';
+    }
+}
+
+void sDbscan::fit_sOptics(const float* X, float eps, int minPts) {
+    check(sdb_fit_soptics(eng_, X, eps, minPts), "fit_sOptics");
+    ordering_.assign(n_, 0);
+    reachability_.assign(n_, 0.0f);
+    check(sdb_get_optics(eng_, ordering_.data(), reachability_.data()), "fit_sOptics (results)");
+    if (!output_.empty()) {  // src/sDbscan.cpp:1757-1768, format of src/Utilities.cpp:34-47
+        const std::string f = output_ + "_" + dist_str(prm_.distance) + "_Eps_" + int2str(std::lround(1000 * eps)) +
+                              "_MinPts_" + int2str(minPts) + "_NumEmbed_" +
+                              int2str(prm_.distance == SDB_COSINE ? d_ : prm_.ker_n_features) + "_NumProj_" +
+                              int2str(prm_.n_proj) + "_TopM_" + int2str(prm_.topM) + "_TopK_" + int2str(prm_.topK);
+        std::ofstream out(f);
+        for (size_t i = 0; i < ordering_.size(); ++i) out << ordering_[i] << " " << reachability_[i] << '\n';
+    }
+}

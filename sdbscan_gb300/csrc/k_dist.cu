@@ -1,0 +1,246 @@
+// Stage 4: candidate distances and the eps test — the dominant loop of
+// rp_findCorePoints / rp_findCoreDist (src/sDbscan.cpp:243-359, :1323-1412)
+// with computeDist (src/Utilities.h:212-287).
+//
+// Formulation: a grouped, gathered GEMM.  Tile = (list l, 128 member rows,
+// 64 candidate columns).  The member rows are gathered from the transformed
+// data by point id, the candidate rows are the list's top-m points; both are
+// staged through shared memory with cp.async (3 stages, 32 dimensions per
+// stage).  Each of the 256 threads owns an 8 x 4 block of (member, candidate)
+// pairs and accumulates over dimensions in ascending order with one fmaf per
+// dimension — the same sequence of roundings as the oracle's dot product — so
+// every distance, and so every eps decision, is bit-identical to the CPU path.
+//
+// Epilogue per tile:
+//  - mask word per (member point, slot): bit s set when candidate s is within
+//    eps and is not the point itself (src/sDbscan.cpp:272, :286);
+//  - inRaw[candidate] += number of members of this tile that pass (the
+//    reverse edges n -> candidate, src/sDbscan.cpp:293-294);
+//  - optionally the distance of every (member, candidate) pair (sOPTICS).
+#include "common.cuh"
+
+namespace sdb {
+namespace {
+
+constexpr int TM = 128, TN = 64, TK = 32, LDS = TK + 4, STAGES = 3, NT = 256;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    const int sz = valid ? 16 : 0;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(sz));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+template <int DIST> __device__ __forceinline__ float acc_step(float acc, float a, float b) {
+    if (DIST == DIST_COSINE) {
+        return __fmaf_rn(a, b, acc);
+    } else if (DIST == DIST_L2) {
+        const float t = __fsub_rn(a, b);
+        return __fmaf_rn(t, t, acc);
+    } else if (DIST == DIST_L1) {
+        return __fadd_rn(acc, fabsf(__fsub_rn(a, b)));
+    } else if (DIST == DIST_CHI2) {
+        if (a > 0.0f && b > 0.0f) acc = __fadd_rn(acc, __fdiv_rn(__fmul_rn(a, b), __fadd_rn(a, b)));
+        return acc;
+    } else {  // JS with EPSILON = 1e-6 added to both (src/Utilities.h:248-266)
+        const float x = __fadd_rn(a, 1e-6f), y = __fadd_rn(b, 1e-6f);
+        const float l2 = 0.693147182464599609375f;  // (float)log(2.0)
+        const float s = __fadd_rn(x, y);
+        const float t1 = __fmul_rn(__fdiv_rn(logf(__fdiv_rn(s, x)), l2), x);
+        const float t2 = __fmul_rn(__fdiv_rn(logf(__fdiv_rn(s, y)), l2), y);
+        return __fadd_rn(acc, __fadd_rn(t1, t2));
+    }
+}
+
+template <int DIST> __device__ __forceinline__ float finish(float acc) {
+    if (DIST == DIST_COSINE) return __fsub_rn(1.0f, acc);           // 1 - x.y
+    if (DIST == DIST_L2) return __fsqrt_rn(acc);                    // ||x - y||
+    if (DIST == DIST_L1) return acc;                                 // sum |x - y|
+    if (DIST == DIST_CHI2) return __fsub_rn(1.0f, __fmul_rn(2.0f, acc));  // == (float)(1.0 - 2.0*t), exact
+    return __fsub_rn(1.0f, __fmul_rn(acc, 0.5f));                    // == (float)(1.0 - t/2.0), exact
+}
+
+template <int DIST>
+__global__ void __launch_bounds__(NT, 2) k_dist(DistArgs a) {
+    extern __shared__ __align__(16) float sm[];
+    float* As = sm;                                   // STAGES x TM x LDS
+    float* Bs = As + STAGES * TM * LDS;               // STAGES x TN x LDS
+    int* rowPoint = reinterpret_cast<int*>(Bs + STAGES * TN * LDS);
+    int* rowSlot = rowPoint + TM;
+    int* colPoint = rowSlot + TM;
+    unsigned* smask = reinterpret_cast<unsigned*>(colPoint + TN);  // TM x 2
+    int* colCount = reinterpret_cast<int*>(smask + 2 * TM);          // TN
+    __shared__ int passTotal;
+
+    const int tid = threadIdx.x;
+    const int64_t t = blockIdx.x;
+    if (t >= *a.tileTotal) return;
+    const int l = a.tileList[t];
+    const int64_t ti = t - a.tileOff[l];
+    const int mt = (int)(ti / a.nct), ct = (int)(ti % a.nct);
+    const int64_t mbeg = a.listOff[l] + (int64_t)mt * TM;
+    const int64_t mend = a.listOff[l + 1];
+    const int r = l % a.nproj, side = l / a.nproj;
+    const int32_t* cand = a.topM + (size_t)r * 2 * a.m + side * a.m;
+
+    for (int i = tid; i < TM; i += NT) {
+        const int64_t q = mbeg + i;
+        if (q < mend) {
+            const int2 mb = a.members[q];
+            rowPoint[i] = mb.x;
+            rowSlot[i] = mb.y;
+        } else {
+            rowPoint[i] = -1;
+            rowSlot[i] = 0;
+        }
+        smask[2 * i] = 0;
+        smask[2 * i + 1] = 0;
+    }
+    for (int j = tid; j < TN; j += NT) {
+        const int c = ct * TN + j;
+        colPoint[j] = c < a.m ? cand[c] : -1;
+        colCount[j] = 0;
+    }
+    if (tid == 0) passTotal = 0;
+    __syncthreads();
+
+    const int nk = (a.d + TK - 1) / TK;
+    auto load_stage = [&](int stage, int kc) {
+        float* as = As + stage * TM * LDS;
+        float* bs = Bs + stage * TN * LDS;
+        const int k0 = kc * TK;
+#pragma unroll
+        for (int it = 0; it < (TM * TK / 4) / NT; ++it) {  // 4 per thread
+            const int idx = tid + it * NT;
+            const int row = idx >> 3, c4 = idx & 7;
+            const int p = rowPoint[row];
+            const int col = k0 + c4 * 4;
+            const bool ok = p >= 0 && col < a.ld;
+            const float* src = ok ? a.Xt + (size_t)p * a.ld + col : a.Xt;
+            cp_async16(as + row * LDS + c4 * 4, src, ok);
+        }
+#pragma unroll
+        for (int it = 0; it < (TN * TK / 4) / NT; ++it) {  // 2 per thread
+            const int idx = tid + it * NT;
+            const int row = idx >> 3, c4 = idx & 7;
+            const int p = colPoint[row];
+            const int col = k0 + c4 * 4;
+            const bool ok = p >= 0 && col < a.ld;
+            const float* src = ok ? a.Xt + (size_t)p * a.ld + col : a.Xt;
+            cp_async16(bs + row * LDS + c4 * 4, src, ok);
+        }
+    };
+
+    float acc[8][4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+
+    const int ty = tid >> 4, tx = tid & 15;
+#pragma unroll
+    for (int s = 0; s < STAGES - 1; ++s) {
+        if (s < nk) load_stage(s, s);
+        cp_async_commit();
+    }
+    for (int kc = 0; kc < nk; ++kc) {
+        cp_async_wait<STAGES - 2>();
+        __syncthreads();
+        const int nxt = kc + STAGES - 1;
+        if (nxt < nk) load_stage(nxt % STAGES, nxt);
+        cp_async_commit();
+        const float* as = As + (kc % STAGES) * TM * LDS;
+        const float* bs = Bs + (kc % STAGES) * TN * LDS;
+#pragma unroll
+        for (int kk = 0; kk < TK; kk += 4) {
+            float4 av[8], bv[4];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) av[i] = *reinterpret_cast<const float4*>(as + (ty + 16 * i) * LDS + kk);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) bv[j] = *reinterpret_cast<const float4*>(bs + (tx + 16 * j) * LDS + kk);
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    float c = acc[i][j];
+                    c = acc_step<DIST>(c, av[i].x, bv[j].x);
+                    c = acc_step<DIST>(c, av[i].y, bv[j].y);
+                    c = acc_step<DIST>(c, av[i].z, bv[j].z);
+                    c = acc_step<DIST>(c, av[i].w, bv[j].w);
+                    acc[i][j] = c;
+                }
+        }
+    }
+    cp_async_wait<0>();
+
+    // epilogue
+    int myPass = 0;
+    int colPass[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int row = ty + 16 * i;
+        const int p = rowPoint[row];
+        unsigned lo = 0, hi = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int col = tx + 16 * j;
+            const int q = colPoint[col];
+            const float dist = finish<DIST>(acc[i][j]);
+            const bool pass = p >= 0 && q >= 0 && p != q && dist <= a.eps;
+            if (pass) {
+                if (col < 32) lo |= 1u << col;
+                else hi |= 1u << (col - 32);
+                colPass[j] += 1;
+                ++myPass;
+            }
+            if (a.dists != nullptr && p >= 0 && q >= 0)
+                a.dists[((size_t)p * 2 * a.k + rowSlot[row]) * a.m + ct * TN + col] = dist;
+        }
+        if (lo) atomicOr(&smask[2 * row], lo);
+        if (hi) atomicOr(&smask[2 * row + 1], hi);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (colPass[j]) atomicAdd(&colCount[tx + 16 * j], colPass[j]);
+    const int wp = warp_sum(myPass);
+    if ((tid & 31) == 0 && wp) atomicAdd(&passTotal, wp);
+    __syncthreads();
+    for (int row = tid; row < TM; row += NT) {
+        const int p = rowPoint[row];
+        if (p >= 0) {
+            const uint64_t w = ((uint64_t)smask[2 * row + 1] << 32) | smask[2 * row];
+            a.masks[((size_t)p * 2 * a.k + rowSlot[row]) * a.W + ct] = w;
+        }
+    }
+    for (int j = tid; j < TN; j += NT)
+        if (colCount[j]) atomicAdd(a.inRaw + colPoint[j], colCount[j]);
+    if (tid == 0 && passTotal) atomicAdd(a.pairs, (unsigned long long)passTotal);
+}
+
+template <int DIST> int launch_dist_t(const DistArgs& a, cudaStream_t st) {
+    const size_t sm = sizeof(float) * (STAGES * (TM + TN) * LDS) + sizeof(int) * (3 * TM + 2 * TN + 2 * TM);
+    if (cudaFuncSetAttribute(k_dist<DIST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+        return -1;
+    if (a.nTiles <= 0) return 0;
+    k_dist<DIST><<<(unsigned)a.nTiles, NT, sm, st>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+}  // namespace
+
+int dist_tile_rows() { return TM; }
+int dist_tile_cols() { return TN; }
+
+int launch_dist(const DistArgs& a, cudaStream_t st) {
+    switch (a.dist) {
+        case DIST_COSINE: return launch_dist_t<DIST_COSINE>(a, st);
+        case DIST_L1: return launch_dist_t<DIST_L1>(a, st);
+        case DIST_L2: return launch_dist_t<DIST_L2>(a, st);
+        case DIST_CHI2: return launch_dist_t<DIST_CHI2>(a, st);
+        case DIST_JS: return launch_dist_t<DIST_JS>(a, st);
+    }
+    return -1;
+}
+
+}  // namespace sdb

@@ -1,0 +1,362 @@
+// Stage 1 of the fit: transformData + kernel embedding + the three rounds of
+// random sign flips and Walsh-Hadamard transforms + per-point top-k.
+//
+// Reference: transformData (src/Utilities.h:289-335), the per-point loop of
+// rp_parIndex (src/sDbscan.cpp:46-145) and the embeddings embedChi2 / embedJS
+// (src/Utilities.h:132-208).
+//
+// Layout: one warp per point.  Lane l holds elements e = l + 32*j of the
+// fhtDim-long rotation vector in register v[j].  Butterflies of stride < 32
+// run across lanes (shfl_xor), strides >= 32 inside a lane.  The stages run in
+// ascending stride order with (a + b, a - b) per butterfly, which is the exact
+// sequence of roundings of the reference's fht_float, so the projections are
+// bit-identical to the CPU path.
+//
+// Numerical contract of the transform (the oracle's and the shim's): the norm
+// and the sum are sequential over ascending index, computed by one thread per
+// point (k_colstats); the division is IEEE round-to-nearest.
+#include "common.cuh"
+
+#include <cuda_bf16.h>
+
+namespace sdb {
+namespace {
+
+// One thread per point: Cosine norm (sequential fmaf of squares) or Chi2/JS
+// column sum (sequential adds), plus the reference's input checks
+// (src/Utilities.h:308-324) and a finiteness check.
+__global__ void k_colstats(const float* __restrict__ X, int ldx, int n, int d, int dist, float* __restrict__ scale,
+                           int32_t* __restrict__ err) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float* x = X + (size_t)p * ldx;
+    float s = 0.0f;
+    bool neg = false, nonfinite = false;
+    if (dist == DIST_COSINE) {
+        for (int i = 0; i < d; ++i) {
+            const float t = __ldg(x + i);
+            nonfinite |= !isfinite(t);
+            s = __fmaf_rn(t, t, s);
+        }
+        s = __fsqrt_rn(s);
+        if (!(s > 0.0f)) atomicExch(err + 1, 1);
+    } else if (dist == DIST_CHI2 || dist == DIST_JS) {
+        for (int i = 0; i < d; ++i) {
+            const float t = __ldg(x + i);
+            nonfinite |= !isfinite(t);
+            neg |= t < 0.0f;
+            s = __fadd_rn(s, t);
+        }
+        if (neg) atomicExch(err + 0, 1);
+        else if (!(s > 0.0f)) atomicExch(err + 1, 1);
+    } else {
+        for (int i = 0; i < d; ++i) nonfinite |= !isfinite(__ldg(x + i));
+        s = 1.0f;
+    }
+    if (nonfinite) atomicExch(err + 2, 1);
+    scale[p] = s;
+}
+
+__device__ __forceinline__ float sign_apply(float v, const uint32_t* sw, int bitidx) {
+    return ((sw[bitidx >> 5] >> (bitidx & 31)) & 1u) ? v : -v;
+}
+
+// Warp bitonic sort of 32 u64 keys, one per lane, into descending lane order.
+__device__ __forceinline__ uint64_t warp_sort_desc(uint64_t x) {
+    const unsigned l = lane_id();
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            const uint64_t o = shfl_xor_u64(x, stride);
+            const bool up = ((l & size) == 0);          // descending blocks where bit `size` clear
+            const bool lower = ((l & stride) == 0);
+            const bool keep_max = (up == lower);
+            x = keep_max ? (o > x ? o : x) : (o < x ? o : x);
+        }
+    }
+    return x;
+}
+
+// Top-(k+1) of the warp's nproj keys (key[j] for element l + 32 j; invalid
+// elements hold key 0 and never win against a valid element since valid keys
+// are > 0 except -NaN).  Writes the k winners in descending order to out[0..k)
+// and returns whether the k-th and (k+1)-th values tie.  `e` ties break toward
+// the smaller vector index.
+template <int NJ>
+__device__ bool warp_topk(const float (&v)[NJ], bool far, int nproj, int k, int32_t* out, uint64_t* sbuf) {
+    const unsigned l = lane_id();
+    auto keyj = [&](int j) -> uint32_t {
+        const int e = (int)l + 32 * j;
+        return e < nproj ? key_of(far ? -v[j] : v[j]) : 0u;
+    };
+    const int want = k + 1 <= nproj ? k + 1 : k;
+    // Fast path: threshold from the lane maxima.
+    if (want <= 32) {
+        uint32_t lm = 0;
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) lm = max(lm, keyj(j));
+        const uint64_t lmk = ((uint64_t)lm << 32) | (uint64_t)l;
+        const uint64_t sorted = warp_sort_desc(lmk);
+        const uint32_t T = (uint32_t)(__shfl_sync(0xffffffffu, sorted, want - 1) >> 32);
+        // candidates: key >= T (at least `want` of them)
+        int cnt = 0;
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) cnt += (keyj(j) >= T && (l + 32 * j) < (unsigned)nproj) ? 1 : 0;
+        int incl = cnt;
+#pragma unroll
+        for (int s = 1; s < 32; s <<= 1) {
+            const int o = __shfl_up_sync(0xffffffffu, incl, s);
+            if ((int)l >= s) incl += o;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (total <= 32) {
+            int pos = incl - cnt;
+#pragma unroll
+            for (int j = 0; j < NJ; ++j) {
+                const int e = (int)l + 32 * j;
+                const uint32_t kj = keyj(j);
+                if (kj >= T && e < nproj) sbuf[pos++] = ((uint64_t)kj << 32) | (uint64_t)(0xffffffffu - (uint32_t)e);
+            }
+            __syncwarp();
+            const uint64_t mine = (int)l < total ? sbuf[l] : 0ull;
+            __syncwarp();
+            const uint64_t s = warp_sort_desc(mine);
+            if ((int)l < k) out[l] = (int32_t)(0xffffffffu - (uint32_t)s);
+            const uint64_t a = __shfl_sync(0xffffffffu, s, k - 1);
+            const uint64_t b = __shfl_sync(0xffffffffu, s, want - 1);
+            return want > k && (uint32_t)(a >> 32) == (uint32_t)(b >> 32);
+        }
+    }
+    // General path: repeated warp argmax.
+    uint32_t taken[(NJ + 31) / 32];
+#pragma unroll
+    for (int w = 0; w < (NJ + 31) / 32; ++w) taken[w] = 0;
+    uint32_t prev = 0, last = 0;
+    for (int it = 0; it < want; ++it) {
+        uint64_t best = 0;
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int e = (int)l + 32 * j;
+            if (e < nproj && !((taken[j >> 5] >> (j & 31)) & 1u)) {
+                const uint64_t pk = ((uint64_t)keyj(j) << 32) | (uint64_t)(0xffffffffu - (uint32_t)e);
+                best = pk > best ? pk : best;
+            }
+        }
+        best = warp_max_u64(best);
+        const int e = (int)(0xffffffffu - (uint32_t)best);
+        if ((e & 31) == (int)l) {
+            const int j = e >> 5;
+            taken[j >> 5] |= 1u << (j & 31);
+        }
+        if (it < k) {
+            if (l == 0) out[it] = e;
+            prev = (uint32_t)(best >> 32);
+        } else {
+            last = (uint32_t)(best >> 32);
+        }
+    }
+    return want > k && prev == last;
+}
+
+template <int NJ>
+__global__ void __launch_bounds__(256, (NJ >= 64 ? 1 : 2)) k_project(ProjectArgs a, const float* __restrict__ scale) {
+    extern __shared__ float smem[];
+    const int warps = blockDim.x >> 5;
+    const int w = threadIdx.x >> 5;
+    const unsigned l = lane_id();
+    const int FD = a.fhtDim;
+    const int nsw = (3 * FD + 31) / 32;
+    uint64_t* sbuf = reinterpret_cast<uint64_t*>(smem) + w * 32;     // per-warp top-k candidates
+    uint32_t* sw = reinterpret_cast<uint32_t*>(smem + warps * 64);   // sign words
+    const int rowLen = (a.dist == DIST_CHI2 || a.dist == DIST_JS) ? ((a.d + 3) & ~3) : 0;
+    float* base = smem + warps * 64 + ((nsw + 3) & ~3);
+    float* rowbuf = base + w * rowLen;                                // per-warp copy of the row (Chi2/JS)
+    float* red = base + warps * rowLen;                               // warps x nproj x 2 chunk extremes
+    for (int i = threadIdx.x; i < nsw; i += blockDim.x) sw[i] = a.signs[i];
+    __syncthreads();
+
+    // Per vector: (max v, max -v) over the warp's points, as bf16 rounded
+    // toward -inf.  A rounded-down maximum is still a lower bound on a value
+    // attained by a point of the chunk, which is all the top-m threshold needs.
+    __nv_bfloat162 ext[NJ];
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) ext[j] = __floats2bfloat162_rn(-INFINITY, -INFINITY);
+    const int p0 = blockIdx.x * a.chunk;
+    const int p1 = min(a.n, p0 + a.chunk);
+    int localTies = 0;
+    for (int p = p0 + w; p < p1; p += warps) {
+        const float* x = a.X + (size_t)p * a.ldx;
+        const float sc = scale[p];
+        float v[NJ];
+        // transformed row -> Xt, and the embedding into v
+        if (a.dist == DIST_CHI2 || a.dist == DIST_JS) {
+            for (int i = (int)l; i < a.d; i += 32) {
+                float t = __ldg(x + i);
+                if (a.do_transform) t = __fdiv_rn(t, sc);
+                rowbuf[i] = t;
+            }
+            __syncwarp();
+        }
+        // write Xt (padded with zeros up to ld)
+        for (int i = (int)l; i < a.ld; i += 32) {
+            float t = 0.0f;
+            if (i < a.d) {
+                t = __ldg(x + i);
+                if (a.do_transform && (a.dist == DIST_COSINE || a.dist == DIST_CHI2 || a.dist == DIST_JS))
+                    t = __fdiv_rn(t, sc);
+            }
+            a.Xt[(size_t)p * a.ld + i] = t;
+        }
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int e = (int)l + 32 * j;
+            float t = 0.0f;
+            if (e < FD && e < a.ker) {
+                if (a.dist == DIST_COSINE) {
+                    t = __fdiv_rn(__ldg(x + e), sc);
+                    if (!a.do_transform) t = __ldg(x + e);
+                } else if (a.dist == DIST_L1 || a.dist == DIST_L2) {
+                    t = a.E[(size_t)p * a.ker + e];
+                } else {  // Chi2 / JS embedding (src/Utilities.h:132-208)
+                    const float L = a.kerSam;
+                    if (e < a.d) {
+                        const float xv = rowbuf[e];
+                        if (xv > 0.0f) {
+                            if (a.dist == DIST_CHI2) t = __fsqrt_rn(__fmul_rn(xv, L));
+                            else t = (float)__dsqrt_rn(__ddiv_rn(__dmul_rn((double)__fmul_rn(xv, L), 2.0), a.ln4));
+                        }
+                    } else {
+                        const int q = e - a.d;
+                        const int c = q / (2 * a.d) + 1;  // component index
+                        const int r = q % (2 * a.d);
+                        const int i = r % a.d;
+                        const bool isSin = r >= a.d;
+                        const int comps = ((a.ker / a.d) - 1) / 2;
+                        const float xv = rowbuf[i];
+                        if (c <= comps && xv > 0.0f) {
+                            float f;
+                            const double ch = a.compCosh[c - 1];  // cosh(PI*c*L), computed on the host
+                            if (a.dist == DIST_CHI2) {
+                                f = (float)__dsqrt_rn(__ddiv_rn(__dmul_rn(__dmul_rn(2.0, (double)xv), (double)L), ch));
+                            } else {
+                                const float cl = __fmul_rn((float)c, L);
+                                const float qq = __fadd_rn(1.0f, __fmul_rn(__fmul_rn(4.0f, cl), cl));
+                                f = (float)__ddiv_rn(2.0, __dmul_rn(__dmul_rn(a.ln4, (double)qq), ch));
+                                f = (float)__dsqrt_rn(
+                                    __dmul_rn(__dmul_rn(__dmul_rn(2.0, (double)xv), (double)L), (double)f));
+                            }
+                            const float ang = __fmul_rn(__fmul_rn((float)c, L), logf(xv));
+                            t = __fmul_rn(f, isSin ? sinf(ang) : cosf(ang));
+                        }
+                    }
+                }
+            }
+            v[j] = t;
+        }
+        // three rounds: random signs, then the Walsh-Hadamard transform
+#pragma unroll 1
+        for (int r = 0; r < 3; ++r) {
+#pragma unroll
+            for (int j = 0; j < NJ; ++j) {
+                const int e = (int)l + 32 * j;
+                if (e < FD) v[j] = sign_apply(v[j], sw, r * FD + e);
+            }
+#pragma unroll
+            for (int s = 1; s < 32; s <<= 1) {
+                if (s >= FD) break;
+#pragma unroll
+                for (int j = 0; j < NJ; ++j) {
+                    const float o = __shfl_xor_sync(0xffffffffu, v[j], s);
+                    v[j] = (l & s) ? __fsub_rn(o, v[j]) : __fadd_rn(v[j], o);
+                }
+            }
+#pragma unroll
+            for (int h = 1; h < NJ; h <<= 1) {
+#pragma unroll
+                for (int j = 0; j < NJ; ++j) {
+                    if ((j & h) == 0) {
+                        const float x0 = v[j], x1 = v[j + h];
+                        v[j] = __fadd_rn(x0, x1);
+                        v[j + h] = __fsub_rn(x0, x1);
+                    }
+                }
+            }
+        }
+        // projections (the first nproj entries) and per-vector chunk extremes
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int e = (int)l + 32 * j;
+            if (e < a.nproj) {
+                a.P[(size_t)p * a.nproj + e] = v[j];
+                __nv_bfloat162 b;
+                b.x = __float2bfloat16_rd(v[j]);
+                b.y = __float2bfloat16_rd(-v[j]);
+                ext[j] = __hmax2(ext[j], b);
+            }
+        }
+        int32_t* tk = a.topK + (size_t)p * 2 * a.k;
+        localTies += warp_topk<NJ>(v, false, a.nproj, a.k, tk, sbuf) ? 1 : 0;
+        localTies += warp_topk<NJ>(v, true, a.nproj, a.k, tk + a.k, sbuf) ? 1 : 0;
+        __syncwarp();
+    }
+    if (l == 0 && localTies) atomicAdd(a.ties, (unsigned long long)localTies);
+    // chunk extremes: reduce across the CTA's warps through shared memory
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+        const int e = (int)l + 32 * j;
+        if (e < a.nproj) {
+            red[(size_t)(w * 2) * a.nproj + e] = __bfloat162float(ext[j].x);
+            red[(size_t)(w * 2 + 1) * a.nproj + e] = -__bfloat162float(ext[j].y);
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < a.nproj; e += blockDim.x) {
+        float mx = -INFINITY, mn = INFINITY;
+        for (int ww = 0; ww < warps; ++ww) {
+            mx = fmaxf(mx, red[(size_t)(ww * 2) * a.nproj + e]);
+            mn = fminf(mn, red[(size_t)(ww * 2 + 1) * a.nproj + e]);
+        }
+        a.chunkMax[(size_t)blockIdx.x * a.nproj + e] = mx;
+        a.chunkMin[(size_t)blockIdx.x * a.nproj + e] = mn;
+    }
+}
+
+template <int NJ>
+int launch_project_nj(const ProjectArgs& a, const float* scale, cudaStream_t st) {
+    const int warps = 8;
+    const int G = (a.n + a.chunk - 1) / a.chunk;
+    const int nsw = (3 * a.fhtDim + 31) / 32;
+    const int rowLen = (a.dist == DIST_CHI2 || a.dist == DIST_JS) ? ((a.d + 3) & ~3) : 0;
+    size_t sm = sizeof(float) * (warps * 64 + ((nsw + 3) & ~3) + (size_t)warps * rowLen + (size_t)warps * 2 * a.nproj);
+    if (sm > 227 * 1024) return -1;
+    if (sm > 48 * 1024) {
+        if (cudaFuncSetAttribute(k_project<NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+            return -1;
+    }
+    k_project<NJ><<<G, warps * 32, sm, st>>>(a, scale);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+}  // namespace
+
+int launch_project(const ProjectArgs& a, cudaStream_t st) {
+    float* scale = a.scale;
+    k_colstats<<<(a.n + 255) / 256, 256, 0, st>>>(a.X, a.ldx, a.n, a.d, a.dist, scale, a.err);
+    if (cudaPeekAtLastError() != cudaSuccess) return -1;
+    int r;
+    switch (a.fhtDim) {
+        case 16:
+        case 32: r = launch_project_nj<1>(a, scale, st); break;
+        case 64: r = launch_project_nj<2>(a, scale, st); break;
+        case 128: r = launch_project_nj<4>(a, scale, st); break;
+        case 256: r = launch_project_nj<8>(a, scale, st); break;
+        case 512: r = launch_project_nj<16>(a, scale, st); break;
+        case 1024: r = launch_project_nj<32>(a, scale, st); break;
+        case 2048: r = launch_project_nj<64>(a, scale, st); break;
+        default: return -1;
+    }
+    return r < 0 ? -1 : r + 1;
+}
+
+}  // namespace sdb

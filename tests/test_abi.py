@@ -1,0 +1,53 @@
+"""The C ABI library loads and exports every entry point declared in
+include/*.h (no compute call: this runs without a GPU)."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(sdb_[a-z0-9_]+)\s*\(", src))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from sdbscan_gb300 import _build
+    _build.build_lib()
+    from sdbscan_gb300 import capi
+    return capi.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    declared = _declared()
+    assert {"sdb_engine_create", "sdb_fit_sdbscan", "sdb_fit_soptics", "sdb_get_labels"} <= declared
+    for name in sorted(declared):
+        assert hasattr(lib, name), name
+    from sdbscan_gb300 import capi
+    assert declared == set(capi.EXPORTS) | (declared - set(capi.EXPORTS))
+    assert set(capi.EXPORTS) <= declared
+
+
+def test_params_default_matches_python_binding(lib):
+    """sdb_params_default gives python/python_wrapper.cpp:17-24's defaults."""
+    from sdbscan_gb300 import capi
+    p = capi.SdbParams()
+    lib.sdb_params_default(ctypes.byref(p))
+    assert (p.n_proj, p.topK, p.topM, p.distance, p.ker_n_features) == (1024, 10, 50, 0, 1024)
+    assert abs(p.ker_sigma - 1.0) < 1e-7 and abs(p.ker_intervalSampling - 0.4) < 1e-7
+    assert (p.clusterNoise, p.verbose, p.n_threads, p.random_seed, p.precision) == (0, 0, -1, -1, 0)
+
+
+def test_null_engine_is_rejected(lib):
+    assert lib.sdb_set_params(None, None) == 1
+    assert lib.sdb_fit_sdbscan(None, None, ctypes.c_float(0.1), 5) == 1
+    assert lib.sdb_last_error(None) == b"null engine"
