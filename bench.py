@@ -1,0 +1,280 @@
+"""Benchmark: points/sec of fit_sDbscan on the 1M x 784 Cosine workload.
+
+One step = one full fit_sDbscan (transform, index, distances, core points,
+clusters) of the whole workload through the engine's C ABI.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` times fits on data already resident in HBM with CUDA events on the
+engine's stream; `e2e` times the public call with host (pinned) input, i.e.
+the upload, the fit and the label download.  The reference arm
+(`--impl reference`) times the CPU restatement of the reference (oracle/) on
+all host cores, on a bounded sample of the same matrix.  Multi-GPU runs are
+independent replicas of the workload (the path has no data exchange at this
+tier), one process per GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "points/sec fit_sDbscan: plain FP32 vs BF16+recheck & batched, at ARI≥0.99"
+WORKLOADS = {
+    2: dict(workload="cfg2_cosine_1Mx784", n=1_000_000, d=784, distance="Cosine", n_proj=1024, topK=10, topM=50,
+            eps=0.25, minPts=50, seed=2007),
+    1: dict(workload="cfg1_cosine_50Kx128", n=50_000, d=128, distance="Cosine", n_proj=1024, topK=5, topM=50,
+            eps=0.15, minPts=20, seed=1007),
+}
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # nominal FP32 CUDA-core peak at max SM clock
+
+
+def _dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _make_data(cfg, device):
+    import torch
+    from sdbscan_gb300 import datasets
+    if cfg["workload"].startswith("cfg2"):
+        X, _ = datasets.cfg2_mnist_like_torch(cfg["n"], cfg["d"], seed=cfg["seed"], device=device)
+    else:
+        Xn, _ = datasets.cfg1_cosine(cfg["n"], cfg["d"], seed=cfg["seed"])
+        X = torch.from_numpy(Xn).to(device)
+    return X.contiguous()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu_index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        rows = [r.split(", ") for r in open(self.path).read().strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def _cpu_sample_rate(Xh, cfg, n_sample):
+    """The oracle (CPU restatement of the reference) on the first n_sample
+    points, all host threads.  Returns (points/s, threads, seconds)."""
+    from oracle.oracle import Port, build_port
+    build_port()
+    port = Port()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    port.fit_sdbscan(Xh[:n_sample], cfg["eps"], cfg["minPts"], dist=cfg["distance"], n_proj=cfg["n_proj"],
+                     topK=cfg["topK"], topM=cfg["topM"], seed=42, threads=threads)
+    dt = time.perf_counter() - t0
+    return n_sample / dt, threads, dt
+
+
+def run_reference(args, cfg):
+    """CPU reference arm: the oracle restatement of the reference's fit path,
+    each step a bounded sample of the workload."""
+    ws, rank, _ = _dist_env()
+    if rank != 0:
+        return 0
+    import numpy as np
+    from sdbscan_gb300 import datasets
+    n_sample = args.cpu_sample
+    if cfg["workload"].startswith("cfg2"):
+        Xh, _ = datasets.cfg2_mnist_like(n_sample, cfg["d"], seed=cfg["seed"])
+    else:
+        Xh, _ = datasets.cfg1_cosine(n_sample, cfg["d"], seed=cfg["seed"])
+    rates = []
+    for i in range(args.warmup + args.steps):
+        r, threads, dt = _cpu_sample_rate(Xh, cfg, n_sample)
+        if i >= args.warmup:
+            rates.append((r, dt))
+    total_pts = n_sample * args.steps
+    total_s = sum(dt for _, dt in rates)
+    value = total_pts / total_s
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (config-2 law, numpy, seed 2007)",
+        "config": {"workload": cfg["workload"], "n": cfg["n"], "d": cfg["d"], "n_proj": cfg["n_proj"],
+                   "topK": cfg["topK"], "topM": cfg["topM"], "eps": cfg["eps"], "minPts": cfg["minPts"]},
+        "cpu_baseline": {"value": value, "unit": "points/s", "cores": threads, "kind": "port",
+                         "sample": f"full fit_sDbscan on {n_sample} points of the workload's law per step "
+                                   f"(oracle/ restatement, OpenMP, {threads} threads)"},
+        "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args, cfg):
+    import numpy as np
+    import torch
+    ws, rank, local = _dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from sdbscan_gb300 import capi
+
+    n, d = cfg["n"], cfg["d"]
+    X = _make_data(cfg, f"cuda:{local}")
+    torch.cuda.synchronize()
+    eng = capi.Engine(n, d, device=local)
+    eng.set_params(n_proj=cfg["n_proj"], topK=cfg["topK"], topM=cfg["topM"], distance=cfg["distance"],
+                   random_seed=42)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=f"cuda:{local}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        eng.fit_sdbscan_device(X.data_ptr(), cfg["eps"], cfg["minPts"])
+    barrier()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    stage_sum = {}
+    launches = 0
+    with ClockSampler(local) as clk:
+        start.record(stream)
+        for _ in range(args.steps):
+            eng.fit_sdbscan_device(X.data_ptr(), cfg["eps"], cfg["minPts"])
+            for k_, v_ in eng.stage_ms().items():
+                stage_sum[k_] = stage_sum.get(k_, 0.0) + v_
+            launches += eng.counters()["launches"]
+        end.record(stream)
+        barrier()
+    ms = start.elapsed_time(end)
+    if ws > 1:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * n * args.steps / (ms / 1e3)
+    counters = eng.counters()
+    labels, ncl = eng.labels()
+
+    # end to end through the public call: pinned host input, labels back
+    Xh_t = torch.empty((n, d), dtype=torch.float32, pin_memory=True)
+    Xh_t.copy_(X)
+    Xh = Xh_t.numpy()
+    for _ in range(min(args.warmup, 2)):
+        eng.fit_sdbscan(Xh, cfg["eps"], cfg["minPts"])
+        eng.labels()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.fit_sdbscan(Xh, cfg["eps"], cfg["minPts"])
+        lab_e2e, _ = eng.labels()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = ws * n * args.steps / e2e_s
+    assert np.array_equal(lab_e2e, labels), "host-input and device-input fits disagree"
+
+    if rank != 0:
+        return 0
+    # dominant kernel: the distance stage (one k_dist launch per fit)
+    dist_ms = stage_sum["distances"] / args.steps
+    flops = 2.0 * (2 * cfg["topK"] * cfg["topM"]) * d * n
+    achieved = flops / (dist_ms / 1e3) / 1e12
+    roofline = {"bound": "fp32", "kernel": "k_dist<Cosine>", "achieved": achieved, "peak": FP32_PEAK_TFLOPS,
+                "unit": "TFLOP/s", "frac": achieved / FP32_PEAK_TFLOPS, "traffic": None,
+                "peak_source": "nominal FP32 CUDA-core peak (152 SMs x 128 lanes x 2 flop x 2.07 GHz); "
+                               "MEASURED_PEAKS.json has no FP32 figure",
+                "flops_per_launch": flops, "kernel_ms": dist_ms}
+    stages = {k_: v_ / args.steps for k_, v_ in stage_sum.items()}
+    cpu = None
+    if ws == 1 and not args.no_cpu:
+        Xs = Xh[: args.cpu_sample].copy()
+        rate, threads, dt = _cpu_sample_rate(Xs, cfg, args.cpu_sample)
+        cpu = {"value": rate, "unit": "points/s", "cores": threads, "kind": "port",
+               "sample": f"full fit_sDbscan on the first {args.cpu_sample} points of the same matrix "
+                         f"(oracle/ restatement, OpenMP, {threads} threads, {dt:.1f} s)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (config-2 law: Bernoulli(0.2) x U(0.3,1) prototypes, 10% redraw, L2-normalised; "
+                "drawn on device, seed 2007)",
+        "config": {"workload": cfg["workload"], "n": n, "d": d, "n_proj": cfg["n_proj"], "topK": cfg["topK"],
+                   "topM": cfg["topM"], "eps": cfg["eps"], "minPts": cfg["minPts"], "precision": "fp32",
+                   "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2 (3.1 GB per step)"},
+        "clocks": clk.summary(),
+        "e2e": {"value": e2e_value, "unit": "points/s", "h2d_bytes_per_step": n * d * 4,
+                "d2h_bytes_per_step": n * 4 + 4},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "stage_ms": stages,
+        "result": {"n_clusters": ncl, "noise": int((labels < 0).sum()), "topk_ties": counters["topk_ties"],
+                   "topm_ties": counters["topm_ties"], "pairs_within_eps": counters["pairs"]},
+    }
+    print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=2, choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-sample", type=int, default=20000)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    cfg = WORKLOADS[args.config]
+    if args.impl == "reference":
+        return run_reference(args, cfg)
+    return run_ours(args, cfg)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

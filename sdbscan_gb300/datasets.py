@@ -15,6 +15,7 @@ import math
 import numpy as np
 
 __all__ = [
+    "cfg2_mnist_like_torch",
     "vmf_mixture", "cfg1_cosine", "cfg2_mnist_like", "cfg3_aniso_l2", "cfg4_dirichlet", "cfg5_batch",
     "CONFIGS",
 ]
@@ -68,17 +69,11 @@ def cfg2_mnist_like(n: int = 1_000_000, d: int = 784, n_comp: int = 10, seed: in
     X = np.empty((n, d), np.float32)
     for s in range(0, n, chunk):
         e = min(n, s + chunk)
-        blk = protos[y[s:e]].copy()
-        redraw = rng.random((e - s, d), dtype=np.float32) < 0.1
-        fresh = (rng.random((e - s, d), dtype=np.float32) < 0.2) * rng.uniform(0.3, 1.0, (e - s, d)).astype(np.float32)
-        blk[redraw] = fresh[redraw]
-        nrm = np.linalg.norm(blk, axis=1, keepdims=True)
-        nrm[nrm == 0] = 1.0
-        X[s:e] = blk / nrm
-    # a row that redraws to all zeros would have no direction; give it one pixel
-    zero = ~np.any(X > 0, axis=1)
-    if zero.any():
-        X[zero, 0] = 1.0
+        u = rng.random((3, e - s, d), dtype=np.float32)
+        fresh = np.where(u[1] < 0.2, np.float32(0.3) + np.float32(0.7) * u[2], np.float32(0.0))
+        blk = np.where(u[0] < 0.1, fresh, protos[y[s:e]])
+        blk[:, 0] += np.float32(1e-3)  # keeps every row nonzero
+        X[s:e] = blk / np.sqrt(np.einsum("ij,ij->i", blk, blk))[:, None]
     return X, y
 
 
@@ -149,3 +144,25 @@ CONFIGS = {
     4: dict(name="cfg4_chi2_soptics_500Kx512", gen=cfg4_dirichlet, distance="Chi2", n_proj=1024, topK=10, topM=50,
             eps=0.1, minPts=50, ker_n_features=1024),
 }
+
+
+def cfg2_mnist_like_torch(n: int = 1_000_000, d: int = 784, n_comp: int = 10, seed: int = 2007,
+                          device: str = "cuda", chunk: int = 1 << 17):
+    """The config-2 law of cfg2_mnist_like, drawn on the GPU with torch (for
+    the full-size benchmark, where numpy generation would take minutes).
+    Returns a (n, d) float32 tensor on `device` and the component labels."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    protos = ((torch.rand(n_comp, d, generator=g, device=device) < 0.2).float() *
+              (0.3 + 0.7 * torch.rand(n_comp, d, generator=g, device=device)))
+    y = torch.randint(0, n_comp, (n,), generator=g, device=device)
+    X = torch.empty(n, d, dtype=torch.float32, device=device)
+    for s in range(0, n, chunk):
+        e = min(n, s + chunk)
+        u = torch.rand(3, e - s, d, generator=g, device=device)
+        fresh = torch.where(u[1] < 0.2, 0.3 + 0.7 * u[2], torch.zeros((), device=device))
+        blk = torch.where(u[0] < 0.1, fresh, protos[y[s:e]])
+        blk[:, 0] += 1e-3
+        X[s:e] = blk / blk.norm(dim=1, keepdim=True)
+    return X, y

