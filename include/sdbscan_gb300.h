@@ -141,6 +141,24 @@ void* sdb_engine_stream(sdb_engine* e);
 /* Message of the last error on this engine ("" if none). */
 const char* sdb_last_error(sdb_engine* e);
 
+/* Per-vector top-m selection (the top-m stage of a fit) that allocates no
+ * device memory.  No counterpart in the reference: it exists for callers that
+ * cannot call cudaMalloc while they run -- a serving loop whose memory pool
+ * already owns the GPU's memory, code that must avoid the implicit
+ * synchronisation of an allocation, or work issued during stream capture.
+ *   proj_device : n_points x n_proj projections, point-major, device memory
+ *                 (the layout sdb_get_projections returns)
+ *   topM_device : n_proj x 2*topM int32 output, device memory, same layout
+ *                 and content as sdb_get_topm
+ *   stream      : cudaStream_t to run on (NULL = legacy default stream)
+ * Limits: n_proj <= 1024, topM <= 64, topM <= n_points; larger sizes return
+ * SDB_ERR_ARG.  Scratch is one fixed __device__ array (about 12 MiB) held by
+ * every GPU that loads this library until it is unloaded.  The first call on
+ * a device looks up that array's device address; make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race. */
+sdb_status sdb_topm_noalloc(const float* proj_device, int32_t n_points, int32_t n_proj, int32_t topM,
+                            int32_t* topM_device, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

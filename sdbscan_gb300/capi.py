@@ -22,7 +22,7 @@ STATUS = {0: "SDB_OK", 1: "SDB_ERR_ARG", 2: "SDB_ERR_CUDA", 3: "SDB_ERR_NEGATIVE
 EXPORTS = ["sdb_params_default", "sdb_engine_create", "sdb_engine_destroy", "sdb_set_params", "sdb_fit_sdbscan",
            "sdb_fit_sdbscan_device", "sdb_fit_soptics", "sdb_fit_soptics_device", "sdb_get_labels", "sdb_get_optics",
            "sdb_clear", "sdb_get_topk", "sdb_get_topm", "sdb_get_core", "sdb_get_core_dist", "sdb_get_projections",
-           "sdb_get_counters", "sdb_get_stage_ms", "sdb_engine_stream", "sdb_last_error"]
+           "sdb_get_counters", "sdb_get_stage_ms", "sdb_engine_stream", "sdb_last_error", "sdb_topm_noalloc"]
 
 
 class SdbParams(ctypes.Structure):
@@ -70,6 +70,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.sdb_engine_stream.restype = vp
     L.sdb_last_error.argtypes = [vp]
     L.sdb_last_error.restype = ctypes.c_char_p
+    L.sdb_topm_noalloc.argtypes = [vp, i32, i32, i32, vp, vp]
     _LIB = L
     return L
 
@@ -193,3 +194,13 @@ class Engine:
 
     def stream(self) -> int:
         return int(self.L.sdb_engine_stream(self.h) or 0)
+
+
+def topm_noalloc(proj_dev_ptr: int, n_points: int, n_proj: int, topM: int, out_dev_ptr: int, stream: int = 0) -> None:
+    """sdb_topm_noalloc: top-m selection on device projections, no device
+    allocation (scratch is a fixed __device__ array in the library)."""
+    L = load()
+    s = L.sdb_topm_noalloc(ctypes.c_void_p(proj_dev_ptr), n_points, n_proj, topM, ctypes.c_void_p(out_dev_ptr),
+                           ctypes.c_void_p(stream) if stream else None)
+    if s != 0:
+        raise SdbError(s, "sdb_topm_noalloc failed")
