@@ -48,6 +48,51 @@ SDB_DEV int warp_sum(int v) {
     return v;
 }
 
+// Calls f(i) on the warp's lanes for every candidate i of point p that passed
+// eps (bit set in p's mask words).  The 2k top-k ids and mask words are
+// fetched up front, two slots per lane; candidates come in lane-parallel
+// batches of up to 32.
+template <typename F>
+SDB_DEV void for_each_passing(const int32_t* __restrict__ topK, const int32_t* __restrict__ topM,
+                              const uint64_t* __restrict__ masks, int k, int m, int W, int p, F&& f) {
+    const unsigned l = lane_id();
+    const int slots = 2 * k;
+    const unsigned long long* mk64 = reinterpret_cast<const unsigned long long*>(masks);
+    int rA = 0, rB = 0;
+    uint64_t mA = 0, mB = 0;
+    if ((int)l < slots) {
+        rA = __ldg(topK + (size_t)p * slots + l);
+        mA = __ldg(mk64 + ((size_t)p * slots + l) * W);
+    }
+    if ((int)l + 32 < slots) {
+        rB = __ldg(topK + (size_t)p * slots + l + 32);
+        mB = __ldg(mk64 + ((size_t)p * slots + l + 32) * W);
+    }
+    for (int jj = 0; jj < slots; ++jj) {
+        const int src = jj & 31;
+        const int r = __shfl_sync(0xffffffffu, jj < 32 ? rA : rB, src);
+        const int side = jj >= k;
+        const int32_t* lst = topM + (size_t)r * 2 * m + side * m;
+        for (int wd = 0; wd < W; ++wd) {
+            uint64_t mk;
+            if (wd == 0) {
+                const uint64_t mine = jj < 32 ? mA : mB;
+                const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)mine, src);
+                const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(mine >> 32), src);
+                mk = ((uint64_t)hi << 32) | lo;
+            } else {
+                mk = __ldg(mk64 + ((size_t)p * slots + jj) * W + wd);
+            }
+            if (!mk) continue;
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                const int bit = half * 32 + (int)l;
+                if ((mk >> bit) & 1ull) f(__ldg(lst + wd * 64 + bit));
+            }
+        }
+    }
+}
+
 // Distance codes (sdb_distance in include/sdbscan_gb300.h).
 enum { DIST_COSINE = 0, DIST_L1 = 1, DIST_L2 = 2, DIST_CHI2 = 3, DIST_JS = 4 };
 
@@ -173,8 +218,13 @@ struct CoreArgs {
     uint8_t* core;
     const float* dists;   // sOPTICS: n x 2k x m distances, or null
     float* coreDist;      // sOPTICS: n (0 for non-core), or null
+    const int32_t* hubIdx;   // n: dense index of hub points, -1 for others
+    const uint32_t* kMask;   // hubs x ceil(2D/32): bit l set when the hub meets list l (its top-k)
 };
 int launch_core_dedupe(const CoreArgs& a, cudaStream_t st);
+// hubIdx from hubOff (a scan of hub flags into idxTmp) and the hubs' list masks.
+int launch_hub_masks(const CoreArgs& a, int32_t* hubIdx, int64_t* idxTmp, uint32_t* kMask, int64_t* scanTmp,
+                     int64_t* nHubsDev, cudaStream_t st);
 int launch_core_finish(const CoreArgs& a, cudaStream_t st);
 
 struct ClusterArgs {

@@ -95,7 +95,8 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
     return {&Xin, &Xt, &scale, &P, &topK, &chunkMax, &chunkMin, &thr, &cand, &candCount, &topM, &listCount,
             &listOff, &listFill, &members, &tileOff, &tileList, &hubCount, &hubOff, &hubLists, &masks, &inRaw,
             &aCount, &degree, &core, &parent, &border, &rootFlag, &labels, &nClusters, &scanTmp, &errFlags,
-            &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill};
+            &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
+            &kMask};
 }
 
 // ---------------------------------------------------------------------------
@@ -207,6 +208,9 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
           ensure(errFlags, sizeof(int32_t) * 8) && ensure(counters, sizeof(unsigned long long) * 8) &&
           ensure(signs, sizeof(uint32_t) * hostSigns.size()) &&
           ensure(compCosh, sizeof(double) * std::max<size_t>(1, hostCosh.size()));
+    const int maskWords = (L + 31) / 32;
+    const size_t maxHubs = std::min<size_t>((size_t)n, (size_t)L * m);
+    ok &= ensure(hubIdx, sizeof(int32_t) * n) && ensure(kMask, sizeof(uint32_t) * maxHubs * maskWords);
     if (rff) ok &= ensure(E, sizeof(float) * (size_t)n * ker) && ensure(Rt, sizeof(float) * hostRt.size());
     if (optics) ok &= ensure(dists, sizeof(float) * (size_t)n * 2 * k * m) && ensure(coreDist, sizeof(float) * n);
     if (!ok) return SDB_ERR_NOMEM;
@@ -387,6 +391,11 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     ca.core = static_cast<uint8_t*>(core.ptr);
     ca.dists = optics ? f32(dists) : nullptr;
     ca.coreDist = optics ? f32(coreDist) : nullptr;
+    ca.hubIdx = i32(hubIdx);
+    ca.kMask = static_cast<const uint32_t*>(kMask.ptr);
+    SDB_CK(cudaMemsetAsync(kMask.ptr, 0, sizeof(uint32_t) * maxHubs * maskWords, st));
+    L_(launch_hub_masks(ca, i32(hubIdx), i64(rootFlag), static_cast<uint32_t*>(kMask.ptr), i64(scanTmp),
+                        reinterpret_cast<int64_t*>(ctr + 5), st));
     L_(launch_core_dedupe(ca, st));
     L_(launch_core_finish(ca, st));
     if (!ok) return fail(SDB_ERR_CUDA, std::string("core launch failed: ") + cudaGetErrorString(cudaGetLastError()));
@@ -412,7 +421,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         L_(launch_cluster(ka, st));
         if (!ok) return fail(SDB_ERR_CUDA, std::string("cluster launch failed: ") + cudaGetErrorString(cudaGetLastError()));
     } else {
-        s = optics_stage(eps, minPts, launches);
+        s = optics_stage(ca, launches);
         if (s != SDB_OK) return s;
     }
     SDB_CK(cudaEventRecord(ev[7], st));

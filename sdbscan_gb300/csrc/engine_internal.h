@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "../../include/sdbscan_gb300.h"
+#include "common.cuh"
 
 struct DevBuf {
     void* ptr = nullptr;
@@ -32,7 +33,7 @@ struct sdb_engine {
     DevBuf Xin, Xt, scale, P, topK, chunkMax, chunkMin, thr, cand, candCount, topM, listCount, listOff, listFill,
         members, tileOff, tileList, hubCount, hubOff, hubLists, masks, inRaw, aCount, degree, core, parent, border,
         rootFlag, labels, nClusters, scanTmp, errFlags, counters, E, Rt, signs, compCosh, dists, coreDist, nbOff,
-        nbIdx, nbDist, nbFill;
+        nbIdx, nbDist, nbFill, hubIdx, kMask;
 
     // results
     bool haveLabels = false, haveOptics = false, haveFit = false, lastOptics = false;
@@ -51,7 +52,7 @@ struct sdb_engine {
     sdb_status derive();
     void host_random(int seed);
     sdb_status fit(const float* X, bool xOnDevice, float eps, int minPts, bool optics);
-    sdb_status optics_stage(float eps, int minPts, int& launches);
+    sdb_status optics_stage(const sdb::CoreArgs& ca, int& launches);
 
     static float* f32(DevBuf& b) { return static_cast<float*>(b.ptr); }
     static int32_t* i32(DevBuf& b) { return static_cast<int32_t*>(b.ptr); }

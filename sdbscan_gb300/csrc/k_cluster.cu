@@ -53,26 +53,9 @@ __global__ void k_init(int32_t* parent, int32_t* border, int n) {
     border[p] = INT_MAX;
 }
 
-// Visits, for point p (one warp), every candidate that passed eps.
 template <typename F>
 __device__ __forceinline__ void for_passing(const ClusterArgs& a, int p, F&& f) {
-    const unsigned l = lane_id();
-    const int slots = 2 * a.k;
-    for (int jj = 0; jj < slots; ++jj) {
-        const int r = __ldg(a.topK + (size_t)p * slots + jj);
-        const int side = jj >= a.k;
-        const int32_t* lst = a.topM + (size_t)r * 2 * a.m + side * a.m;
-        for (int wd = 0; wd < a.W; ++wd) {
-            const uint64_t mk = __ldg(reinterpret_cast<const unsigned long long*>(a.masks) +
-                                      ((size_t)p * slots + jj) * a.W + wd);
-            if (!mk) continue;
-#pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                const int bit = half * 32 + (int)l;
-                if ((mk >> bit) & 1ull) f(__ldg(lst + wd * 64 + bit));
-            }
-        }
-    }
+    for_each_passing(a.topK, a.topM, a.masks, a.k, a.m, a.W, p, f);
 }
 
 __global__ void k_union(ClusterArgs a) {

@@ -24,33 +24,54 @@ namespace {
 
 // One thread per point: Cosine norm (sequential fmaf of squares) or Chi2/JS
 // column sum (sequential adds), plus the reference's input checks
-// (src/Utilities.h:308-324) and a finiteness check.
-__global__ void k_colstats(const float* __restrict__ X, int ldx, int n, int d, int dist, float* __restrict__ scale,
-                           int32_t* __restrict__ err) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    const float* x = X + (size_t)p * ldx;
+// (src/Utilities.h:308-324) and a finiteness check.  The CTA's 256 rows are
+// staged through shared memory 32 dimensions at a time (coalesced 128-byte
+// row segments, transposed so each thread reads its own point's column
+// without bank conflicts); each thread then runs its point's sequential chain.
+constexpr int kCsPoints = 256, kCsDims = 32;
+
+__global__ void __launch_bounds__(kCsPoints) k_colstats(const float* __restrict__ X, int ldx, int n, int d, int dist,
+                                                        float* __restrict__ scale, int32_t* __restrict__ err) {
+    __shared__ float tile[kCsDims][kCsPoints + 1];
+    const int p0 = blockIdx.x * kCsPoints;
+    const int p = p0 + threadIdx.x;
     float s = 0.0f;
     bool neg = false, nonfinite = false;
-    if (dist == DIST_COSINE) {
-        for (int i = 0; i < d; ++i) {
-            const float t = __ldg(x + i);
-            nonfinite |= !isfinite(t);
-            s = __fmaf_rn(t, t, s);
+    for (int c0 = 0; c0 < d; c0 += kCsDims) {
+        __syncthreads();
+        // 256 rows x 32 dims: each warp loads rows with lanes along the dims
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        for (int row = w; row < kCsPoints; row += kCsPoints / 32) {
+            const int pr = p0 + row, c = c0 + lane;
+            tile[lane][row] = (pr < n && c < d) ? __ldcs(X + (size_t)pr * ldx + c) : 0.0f;
         }
+        __syncthreads();
+        const int cn = min(kCsDims, d - c0);
+        if (dist == DIST_COSINE) {
+            for (int i = 0; i < cn; ++i) {
+                const float t = tile[i][threadIdx.x];
+                nonfinite |= !isfinite(t);
+                s = __fmaf_rn(t, t, s);
+            }
+        } else if (dist == DIST_CHI2 || dist == DIST_JS) {
+            for (int i = 0; i < cn; ++i) {
+                const float t = tile[i][threadIdx.x];
+                nonfinite |= !isfinite(t);
+                neg |= t < 0.0f;
+                s = __fadd_rn(s, t);
+            }
+        } else {
+            for (int i = 0; i < cn; ++i) nonfinite |= !isfinite(tile[i][threadIdx.x]);
+        }
+    }
+    if (p >= n) return;
+    if (dist == DIST_COSINE) {
         s = __fsqrt_rn(s);
         if (!(s > 0.0f)) atomicExch(err + 1, 1);
     } else if (dist == DIST_CHI2 || dist == DIST_JS) {
-        for (int i = 0; i < d; ++i) {
-            const float t = __ldg(x + i);
-            nonfinite |= !isfinite(t);
-            neg |= t < 0.0f;
-            s = __fadd_rn(s, t);
-        }
         if (neg) atomicExch(err + 0, 1);
         else if (!(s > 0.0f)) atomicExch(err + 1, 1);
     } else {
-        for (int i = 0; i < d; ++i) nonfinite |= !isfinite(__ldg(x + i));
         s = 1.0f;
     }
     if (nonfinite) atomicExch(err + 2, 1);
@@ -159,8 +180,8 @@ __device__ bool warp_topk(const float (&v)[NJ], bool far, int nproj, int k, int3
     return want > k && prev == last;
 }
 
-template <int NJ>
-__global__ void __launch_bounds__(256, (NJ >= 64 ? 1 : 2)) k_project(ProjectArgs a, const float* __restrict__ scale) {
+template <int NJ, int EMB>
+__global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs a, const float* __restrict__ scale) {
     extern __shared__ float smem[];
     const int warps = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
@@ -169,57 +190,45 @@ __global__ void __launch_bounds__(256, (NJ >= 64 ? 1 : 2)) k_project(ProjectArgs
     const int nsw = (3 * FD + 31) / 32;
     uint64_t* sbuf = reinterpret_cast<uint64_t*>(smem) + w * 32;     // per-warp top-k candidates
     uint32_t* sw = reinterpret_cast<uint32_t*>(smem + warps * 64);   // sign words
-    const int rowLen = (a.dist == DIST_CHI2 || a.dist == DIST_JS) ? ((a.d + 3) & ~3) : 0;
+    const int rowLen = EMB == 2 ? ((a.d + 3) & ~3) + FD : 0;
     float* base = smem + warps * 64 + ((nsw + 3) & ~3);
     float* rowbuf = base + w * rowLen;                                // per-warp copy of the row (Chi2/JS)
-    float* red = base + warps * rowLen;                               // warps x nproj x 2 chunk extremes
+    // per-warp running (max v, max -v) per vector, bf16x2 rounded toward -inf
+    __nv_bfloat162* ext = reinterpret_cast<__nv_bfloat162*>(base + warps * rowLen) + (size_t)w * a.nproj;
     for (int i = threadIdx.x; i < nsw; i += blockDim.x) sw[i] = a.signs[i];
     __syncthreads();
 
     // Per vector: (max v, max -v) over the warp's points, as bf16 rounded
     // toward -inf.  A rounded-down maximum is still a lower bound on a value
     // attained by a point of the chunk, which is all the top-m threshold needs.
-    __nv_bfloat162 ext[NJ];
-#pragma unroll
-    for (int j = 0; j < NJ; ++j) ext[j] = __floats2bfloat162_rn(-INFINITY, -INFINITY);
+    for (int e = (int)l; e < a.nproj; e += 32) ext[e] = __floats2bfloat162_rn(-INFINITY, -INFINITY);
+    __syncwarp();
     const int p0 = blockIdx.x * a.chunk;
     const int p1 = min(a.n, p0 + a.chunk);
     int localTies = 0;
     for (int p = p0 + w; p < p1; p += warps) {
         const float* x = a.X + (size_t)p * a.ldx;
         const float sc = scale[p];
-        float v[NJ];
-        // transformed row -> Xt, and the embedding into v
-        if (a.dist == DIST_CHI2 || a.dist == DIST_JS) {
-            for (int i = (int)l; i < a.d; i += 32) {
-                float t = __ldg(x + i);
-                if (a.do_transform) t = __fdiv_rn(t, sc);
-                rowbuf[i] = t;
-            }
-            __syncwarp();
-        }
-        // write Xt (padded with zeros up to ld)
+        // transformed row -> Xt (zero padded to ld)
         for (int i = (int)l; i < a.ld; i += 32) {
             float t = 0.0f;
             if (i < a.d) {
                 t = __ldg(x + i);
-                if (a.do_transform && (a.dist == DIST_COSINE || a.dist == DIST_CHI2 || a.dist == DIST_JS))
-                    t = __fdiv_rn(t, sc);
+                if (a.do_transform && EMB != 1) t = __fdiv_rn(t, sc);
             }
             a.Xt[(size_t)p * a.ld + i] = t;
+            if (EMB == 2 && i < a.d) rowbuf[i] = t;
         }
-#pragma unroll
-        for (int j = 0; j < NJ; ++j) {
-            const int e = (int)l + 32 * j;
-            float t = 0.0f;
-            if (e < FD && e < a.ker) {
-                if (a.dist == DIST_COSINE) {
-                    t = __fdiv_rn(__ldg(x + e), sc);
-                    if (!a.do_transform) t = __ldg(x + e);
-                } else if (a.dist == DIST_L1 || a.dist == DIST_L2) {
-                    t = a.E[(size_t)p * a.ker + e];
-                } else {  // Chi2 / JS embedding (src/Utilities.h:132-208)
-                    const float L = a.kerSam;
+        if (EMB == 2) {
+            // Chi2 / JS embedding (src/Utilities.h:132-208) into the warp's row
+            // buffer, lane-strided, then picked up per register below.
+            __syncwarp();
+            const float L = a.kerSam;
+            const int comps = ((a.ker / a.d) - 1) / 2;
+            float* emb = rowbuf + ((a.d + 3) & ~3);
+            for (int e = (int)l; e < FD; e += 32) {
+                float t = 0.0f;
+                if (e < a.ker) {
                     if (e < a.d) {
                         const float xv = rowbuf[e];
                         if (xv > 0.0f) {
@@ -232,7 +241,6 @@ __global__ void __launch_bounds__(256, (NJ >= 64 ? 1 : 2)) k_project(ProjectArgs
                         const int r = q % (2 * a.d);
                         const int i = r % a.d;
                         const bool isSin = r >= a.d;
-                        const int comps = ((a.ker / a.d) - 1) / 2;
                         const float xv = rowbuf[i];
                         if (c <= comps && xv > 0.0f) {
                             float f;
@@ -251,9 +259,25 @@ __global__ void __launch_bounds__(256, (NJ >= 64 ? 1 : 2)) k_project(ProjectArgs
                         }
                     }
                 }
+                emb[e] = t;
+            }
+            __syncwarp();
+        }
+        float v[NJ];
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int e = (int)l + 32 * j;
+            float t = 0.0f;
+            if (EMB == 0) {
+                if (e < a.d) t = a.do_transform ? __fdiv_rn(__ldg(x + e), sc) : __ldg(x + e);
+            } else if (EMB == 1) {
+                if (e < a.ker) t = a.E[(size_t)p * a.ker + e];
+            } else {
+                if (e < FD) t = rowbuf[((a.d + 3) & ~3) + e];
             }
             v[j] = t;
         }
+        if (EMB == 2) __syncwarp();
         // three rounds: random signs, then the Walsh-Hadamard transform
 #pragma unroll 1
         for (int r = 0; r < 3; ++r) {
@@ -292,57 +316,56 @@ __global__ void __launch_bounds__(256, (NJ >= 64 ? 1 : 2)) k_project(ProjectArgs
                 __nv_bfloat162 b;
                 b.x = __float2bfloat16_rd(v[j]);
                 b.y = __float2bfloat16_rd(-v[j]);
-                ext[j] = __hmax2(ext[j], b);
+                ext[e] = __hmax2(ext[e], b);
             }
         }
         int32_t* tk = a.topK + (size_t)p * 2 * a.k;
-        localTies += warp_topk<NJ>(v, false, a.nproj, a.k, tk, sbuf) ? 1 : 0;
-        localTies += warp_topk<NJ>(v, true, a.nproj, a.k, tk + a.k, sbuf) ? 1 : 0;
+#pragma unroll 1
+        for (int side = 0; side < 2; ++side)
+            localTies += warp_topk<NJ>(v, side == 1, a.nproj, a.k, tk + side * a.k, sbuf) ? 1 : 0;
         __syncwarp();
     }
     if (l == 0 && localTies) atomicAdd(a.ties, (unsigned long long)localTies);
-    // chunk extremes: reduce across the CTA's warps through shared memory
-#pragma unroll
-    for (int j = 0; j < NJ; ++j) {
-        const int e = (int)l + 32 * j;
-        if (e < a.nproj) {
-            red[(size_t)(w * 2) * a.nproj + e] = __bfloat162float(ext[j].x);
-            red[(size_t)(w * 2 + 1) * a.nproj + e] = -__bfloat162float(ext[j].y);
-        }
-    }
+    // chunk extremes: reduce the warps' rows
     __syncthreads();
+    const __nv_bfloat162* ext0 = reinterpret_cast<const __nv_bfloat162*>(base + warps * rowLen);
     for (int e = threadIdx.x; e < a.nproj; e += blockDim.x) {
-        float mx = -INFINITY, mn = INFINITY;
-        for (int ww = 0; ww < warps; ++ww) {
-            mx = fmaxf(mx, red[(size_t)(ww * 2) * a.nproj + e]);
-            mn = fminf(mn, red[(size_t)(ww * 2 + 1) * a.nproj + e]);
-        }
-        a.chunkMax[(size_t)blockIdx.x * a.nproj + e] = mx;
-        a.chunkMin[(size_t)blockIdx.x * a.nproj + e] = mn;
+        __nv_bfloat162 m2 = ext0[e];
+        for (int ww = 1; ww < warps; ++ww) m2 = __hmax2(m2, ext0[(size_t)ww * a.nproj + e]);
+        a.chunkMax[(size_t)blockIdx.x * a.nproj + e] = __bfloat162float(m2.x);
+        a.chunkMin[(size_t)blockIdx.x * a.nproj + e] = -__bfloat162float(m2.y);
     }
+}
+
+template <int NJ, int EMB>
+int launch_project_nje(const ProjectArgs& a, const float* scale, cudaStream_t st) {
+    const int warps = 4;
+    const int G = (a.n + a.chunk - 1) / a.chunk;
+    const int nsw = (3 * a.fhtDim + 31) / 32;
+    const int rowLen = EMB == 2 ? ((a.d + 3) & ~3) + a.fhtDim : 0;
+    size_t sm = sizeof(float) * (warps * 64 + ((nsw + 3) & ~3) + (size_t)warps * rowLen + (size_t)warps * a.nproj);
+    if (sm > 227 * 1024) return -1;
+    if (sm > 48 * 1024) {
+        if (cudaFuncSetAttribute(k_project<NJ, EMB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+            cudaSuccess)
+            return -1;
+    }
+    k_project<NJ, EMB><<<G, warps * 32, sm, st>>>(a, scale);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
 template <int NJ>
 int launch_project_nj(const ProjectArgs& a, const float* scale, cudaStream_t st) {
-    const int warps = 8;
-    const int G = (a.n + a.chunk - 1) / a.chunk;
-    const int nsw = (3 * a.fhtDim + 31) / 32;
-    const int rowLen = (a.dist == DIST_CHI2 || a.dist == DIST_JS) ? ((a.d + 3) & ~3) : 0;
-    size_t sm = sizeof(float) * (warps * 64 + ((nsw + 3) & ~3) + (size_t)warps * rowLen + (size_t)warps * 2 * a.nproj);
-    if (sm > 227 * 1024) return -1;
-    if (sm > 48 * 1024) {
-        if (cudaFuncSetAttribute(k_project<NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-            return -1;
-    }
-    k_project<NJ><<<G, warps * 32, sm, st>>>(a, scale);
-    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+    if (a.dist == DIST_COSINE) return launch_project_nje<NJ, 0>(a, scale, st);
+    if (a.dist == DIST_L1 || a.dist == DIST_L2) return launch_project_nje<NJ, 1>(a, scale, st);
+    return launch_project_nje<NJ, 2>(a, scale, st);
 }
 
 }  // namespace
 
 int launch_project(const ProjectArgs& a, cudaStream_t st) {
     float* scale = a.scale;
-    k_colstats<<<(a.n + 255) / 256, 256, 0, st>>>(a.X, a.ldx, a.n, a.d, a.dist, scale, a.err);
+    k_colstats<<<(a.n + kCsPoints - 1) / kCsPoints, kCsPoints, 0, st>>>(a.X, a.ldx, a.n, a.d, a.dist, scale, a.err);
     if (cudaPeekAtLastError() != cudaSuccess) return -1;
     int r;
     switch (a.fhtDim) {

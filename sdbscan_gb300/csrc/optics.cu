@@ -1,7 +1,116 @@
-// sOPTICS stage: placeholder until the neighbour-list and ordering kernels land.
+// sOPTICS stage: neighbour lists with distances and core distances on the
+// GPU (rp_findCoreDist, src/sDbscan.cpp:1314-1474), then the ordering and
+// reachability (formOptics_scikit, src/sDbscan.cpp:1588-1703).
+//
+// The ordering is a priority flood: each step pops the unprocessed point of
+// least reachability, so it is inherently sequential.  It runs here in host
+// C++ over the CSR the GPU produced.  Ties between equal reachability values,
+// which the reference's value-only heap resolves by heap order, are resolved
+// by the smaller point id, so the ordering does not depend on the order of
+// the neighbour lists.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <queue>
+#include <vector>
+
 #include "common.cuh"
 #include "engine_internal.h"
 
-sdb_status sdb_engine::optics_stage(float, int, int&) {
-    return fail(SDB_ERR_INTERNAL, "sOPTICS is not implemented yet");
+namespace sdb {
+int launch_core_emit(const CoreArgs& a, const int64_t* nbOff, int32_t* nbIdx, float* nbDist, int32_t* nbFill,
+                     cudaStream_t st);
+int launch_core_dist(const CoreArgs& a, const int64_t* nbOff, const float* nbDist, cudaStream_t st);
+int launch_i32_to_i64(const int32_t* in, int64_t* out, int n, cudaStream_t st);
+}  // namespace sdb
+
+using namespace sdb;
+
+namespace {
+
+// formOptics_scikit with (reachability, point id) order.  reach[] holds
+// NEG_INF (-2^31) for points never reached (src/sDbscan.cpp:1590).
+void form_optics(int n, const uint8_t* core, const float* coreDist, const int64_t* off, const int32_t* idx,
+                 const float* dist, int32_t* ordering, float* reach) {
+    std::fill(reach, reach + n, kNegInfReach);
+    std::vector<uint8_t> done(n, 0);
+    typedef std::pair<float, int> E;
+    std::priority_queue<E, std::vector<E>, std::greater<E>> heap;
+    int64_t no = 0;
+    auto relax = [&](int x) {
+        const float cd = coreDist[x];
+        for (int64_t t = off[x]; t < off[x + 1]; ++t) {
+            const int y = idx[t];
+            if (done[y]) continue;
+            const float r = std::max(cd, dist[t]);
+            if (reach[y] == kNegInfReach || reach[y] > r) {
+                reach[y] = r;
+                heap.push(E(r, y));
+            }
+        }
+    };
+    for (int p = 0; p < n; ++p) {
+        if (done[p]) continue;
+        done[p] = 1;
+        ordering[no++] = p;
+        if (!core[p]) continue;
+        relax(p);
+        while (!heap.empty()) {
+            const int y = heap.top().second;
+            heap.pop();
+            if (done[y]) continue;
+            done[y] = 1;
+            ordering[no++] = y;
+            if (core[y]) relax(y);
+        }
+    }
+}
+
+}  // namespace
+
+sdb_status sdb_engine::optics_stage(const CoreArgs& ca, int& launches) {
+    cudaStream_t st = stream;
+    if (!ensure(nbOff, sizeof(int64_t) * (n + 1)) || !ensure(nbFill, sizeof(int32_t) * n)) return SDB_ERR_NOMEM;
+    cudaError_t e = cudaMemsetAsync(nbOff.ptr, 0, sizeof(int64_t) * (n + 1), st);
+    if (e != cudaSuccess) return cuda_fail(e, "memset");
+    int r = launch_i32_to_i64(ca.degree, i64(nbOff), n, st);
+    if (r < 0) return fail(SDB_ERR_CUDA, "degree conversion launch failed");
+    launches += r;
+    r = launch_scan_i64(i64(nbOff), i64(nbOff), (size_t)n + 1, i64(scanTmp), st);
+    if (r < 0) return fail(SDB_ERR_CUDA, "scan launch failed");
+    launches += r;
+    int64_t total = 0;
+    e = cudaMemcpyAsync(&total, i64(nbOff) + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "neighbour count");
+    if (!ensure(nbIdx, sizeof(int32_t) * std::max<int64_t>(total, 1)) ||
+        !ensure(nbDist, sizeof(float) * std::max<int64_t>(total, 1)))
+        return SDB_ERR_NOMEM;
+    e = cudaMemsetAsync(nbFill.ptr, 0, sizeof(int32_t) * n, st);
+    if (e != cudaSuccess) return cuda_fail(e, "memset");
+    r = launch_core_emit(ca, i64(nbOff), i32(nbIdx), f32(nbDist), i32(nbFill), st);
+    if (r < 0) return fail(SDB_ERR_CUDA, "neighbour list launch failed");
+    launches += r;
+    r = launch_core_dist(ca, i64(nbOff), f32(nbDist), st);
+    if (r < 0) return fail(SDB_ERR_CUDA, "core distance launch failed");
+    launches += r;
+
+    std::vector<int64_t> hOff(n + 1);
+    std::vector<int32_t> hIdx(total);
+    std::vector<float> hDist(total), hCd(n);
+    std::vector<uint8_t> hCore(n);
+    e = cudaMemcpyAsync(hOff.data(), nbOff.ptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && total)
+        e = cudaMemcpyAsync(hIdx.data(), nbIdx.ptr, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && total)
+        e = cudaMemcpyAsync(hDist.data(), nbDist.ptr, sizeof(float) * total, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hCd.data(), coreDist.ptr, sizeof(float) * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hCore.data(), core.ptr, n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "neighbour list download");
+    hostOrdering.assign(n, 0);
+    hostReach.assign(n, 0.0f);
+    form_optics(n, hCore.data(), hCd.data(), hOff.data(), hIdx.data(), hDist.data(), hostOrdering.data(),
+                hostReach.data());
+    return SDB_OK;
 }

@@ -173,3 +173,57 @@ def test_pybind_dropin_matches_capi():
     labels, ncl = eng.labels()
     np.testing.assert_array_equal(np.asarray(dbs.labels_), labels)
     assert dbs.n_clusters_ == ncl
+
+
+OPTICS_FIXTURES = [p for p in GOLDEN if _fixture(p)[1]["optics"]]
+
+
+@pytest.mark.parametrize("path", OPTICS_FIXTURES, ids=[os.path.basename(p)[:-4] for p in OPTICS_FIXTURES])
+def test_fit_soptics_matches_reference(port, path):
+    """Core flags, neighbourhood sizes and core distances equal the
+    reference's; the ordering equals the oracle's with the canonical tie order
+    (reachability, then point id), and reachability agrees with it exactly."""
+    z, meta = _fixture(path)
+    X = z["X"]
+    eng = _engine(X, meta)
+    eng.fit_soptics(X, meta["eps"], meta["minPts"])
+    order, reach = eng.optics()
+    core, deg = eng.core()
+    cd = eng.core_dist()
+    exact = meta["distance"] == "Cosine" or meta.get("ker_n_features", 1024) // X.shape[1] < 3
+    if exact:
+        np.testing.assert_array_equal(core, z["core"])
+        np.testing.assert_array_equal(deg, z["degree"])
+        np.testing.assert_array_equal(cd, z["core_dist"])
+    assert sorted(order.tolist()) == list(range(X.shape[0]))
+    # canonical ordering from the oracle on the same data and parameters
+    from oracle.oracle import fht_dim
+    dist = meta["distance"]
+    ker = X.shape[1] if dist == "Cosine" else meta.get("ker_n_features", 1024)
+    o_order, o_reach, o_core, o_cd, _ = port.fit_soptics(X, meta["eps"], meta["minPts"], dist=dist,
+                                                         n_proj=meta["n_proj"], topK=meta["topK"],
+                                                         topM=meta["topM"], ker=ker, seed=meta["random_seed"],
+                                                         threads=4, tie_mode=1)
+    if exact:
+        np.testing.assert_array_equal(order, o_order)
+        np.testing.assert_array_equal(reach, o_reach)
+
+
+@pytest.mark.parametrize("n,d,k,m,eps,minPts", [(8000, 64, 5, 30, 0.2, 10), (6000, 196, 10, 50, 0.25, 30)])
+def test_fit_soptics_matches_oracle(port, n, d, k, m, eps, minPts):
+    from sdbscan_gb300 import capi, datasets
+    if d == 196:
+        X, _ = datasets.cfg2_mnist_like(n, d, seed=61)
+    else:
+        X, _ = datasets.cfg1_cosine(n, d, seed=62)
+    eng = capi.Engine(n, d)
+    eng.set_params(n_proj=512, topK=k, topM=m, distance="Cosine", random_seed=13)
+    eng.fit_soptics(X, eps, minPts)
+    order, reach = eng.optics()
+    core, deg = eng.core()
+    o_order, o_reach, o_core, o_cd, _ = port.fit_soptics(X, eps, minPts, n_proj=512, topK=k, topM=m, seed=13,
+                                                         threads=4, tie_mode=1)
+    np.testing.assert_array_equal(core, o_core)
+    np.testing.assert_array_equal(eng.core_dist(), o_cd)
+    np.testing.assert_array_equal(order, o_order)
+    np.testing.assert_array_equal(reach, o_reach)
