@@ -220,6 +220,7 @@ struct CoreArgs {
     float* coreDist;      // sOPTICS: n (0 for non-core), or null
     const int32_t* hubIdx;   // n: dense index of hub points, -1 for others
     const uint32_t* kMask;   // hubs x ceil(2D/32): bit l set when the hub meets list l (its top-k)
+    uint64_t* firstMasks;    // n x 2k x W: the mask bits of each point's first occurrence of a candidate
 };
 int launch_core_dedupe(const CoreArgs& a, cudaStream_t st);
 // hubIdx from hubOff (a scan of hub flags into idxTmp) and the hubs' list masks.
@@ -229,7 +230,7 @@ int launch_core_finish(const CoreArgs& a, cudaStream_t st);
 
 struct ClusterArgs {
     int n, k, m, W;
-    const uint64_t* masks;
+    const uint64_t* masks;   // first-occurrence masks: each distinct candidate once per point
     const int32_t* topK;
     const int32_t* topM;
     const uint8_t* core;

@@ -96,7 +96,7 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &listOff, &listFill, &members, &tileOff, &tileList, &hubCount, &hubOff, &hubLists, &masks, &inRaw,
             &aCount, &degree, &core, &parent, &border, &rootFlag, &labels, &nClusters, &scanTmp, &errFlags,
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
-            &kMask};
+            &kMask, &firstMasks};
 }
 
 // ---------------------------------------------------------------------------
@@ -200,6 +200,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
           ensure(hubCount, sizeof(int32_t) * n) && ensure(hubOff, sizeof(int64_t) * (n + 1)) &&
           ensure(hubLists, sizeof(int32_t) * (size_t)L * m) &&
           ensure(masks, sizeof(uint64_t) * (size_t)n * 2 * k * W) && ensure(inRaw, sizeof(int32_t) * n) &&
+          ensure(firstMasks, sizeof(uint64_t) * (size_t)n * 2 * k * W) &&
           ensure(aCount, sizeof(int32_t) * n) && ensure(degree, sizeof(int32_t) * n) && ensure(core, n) &&
           ensure(parent, sizeof(int32_t) * n) && ensure(border, sizeof(int32_t) * n) &&
           ensure(rootFlag, sizeof(int64_t) * (n + 1)) && ensure(labels, sizeof(int32_t) * n) &&
@@ -393,6 +394,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     ca.coreDist = optics ? f32(coreDist) : nullptr;
     ca.hubIdx = i32(hubIdx);
     ca.kMask = static_cast<const uint32_t*>(kMask.ptr);
+    ca.firstMasks = static_cast<uint64_t*>(firstMasks.ptr);
     SDB_CK(cudaMemsetAsync(kMask.ptr, 0, sizeof(uint32_t) * maxHubs * maskWords, st));
     L_(launch_hub_masks(ca, i32(hubIdx), i64(rootFlag), static_cast<uint32_t*>(kMask.ptr), i64(scanTmp),
                         reinterpret_cast<int64_t*>(ctr + 5), st));
@@ -408,7 +410,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         ka.k = k;
         ka.m = m;
         ka.W = W;
-        ka.masks = static_cast<const uint64_t*>(masks.ptr);
+        ka.masks = static_cast<const uint64_t*>(firstMasks.ptr);
         ka.topK = i32(topK);
         ka.topM = i32(topM);
         ka.core = static_cast<const uint8_t*>(core.ptr);

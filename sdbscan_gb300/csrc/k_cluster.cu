@@ -62,10 +62,13 @@ __global__ void k_union(ClusterArgs a) {
     const int warps = blockDim.x >> 5;
     const int p = blockIdx.x * warps + (threadIdx.x >> 5);
     if (p >= a.n || !a.core[p]) return;
+    int rp = find_root(a.parent, p);
     for_passing(a, p, [&](int i) {
         if (!a.core[i]) return;
-        if (load_parent(a.parent, i) == load_parent(a.parent, p)) return;
-        unite(a.parent, p, i);
+        const int pi = load_parent(a.parent, i);
+        if (pi == rp || load_parent(a.parent, pi) == rp) return;  // already joined (common case)
+        unite(a.parent, rp, i);
+        rp = find_root(a.parent, rp);
     });
 }
 

@@ -82,21 +82,24 @@ struct WarpSet {
     int* keys;
     int* cnts;
     float* dsts;
-    int* used;
+    uint16_t* used;
     uint32_t* listMask;
     int* nUsed;
 };
 
+__host__ __device__ inline int warp_set_words(int T, int maskWords, bool withDist) {
+    return 2 * T + T / 2 + maskWords + 1 + (withDist ? T : 0);
+}
+
 __device__ __forceinline__ WarpSet warp_set(int* sh, int w, int T, int maskWords, bool withDist) {
-    const int per = 3 * T + maskWords + 1 + (withDist ? T : 0);
-    int* b = sh + (size_t)w * per;
+    int* b = sh + (size_t)w * warp_set_words(T, maskWords, withDist);
     WarpSet ws;
     ws.keys = b;
     ws.cnts = b + T;
-    ws.used = b + 2 * T;
-    ws.listMask = reinterpret_cast<uint32_t*>(b + 3 * T);
-    ws.nUsed = b + 3 * T + maskWords;
-    ws.dsts = withDist ? reinterpret_cast<float*>(b + 3 * T + maskWords + 1) : nullptr;
+    ws.used = reinterpret_cast<uint16_t*>(b + 2 * T);
+    ws.listMask = reinterpret_cast<uint32_t*>(b + 2 * T + T / 2);
+    ws.nUsed = b + 2 * T + T / 2 + maskWords;
+    ws.dsts = withDist ? reinterpret_cast<float*>(b + 2 * T + T / 2 + maskWords + 1) : nullptr;
     return ws;
 }
 
@@ -104,19 +107,21 @@ __device__ __forceinline__ WarpSet warp_set(int* sh, int w, int T, int maskWords
 // warp's set; returns the number of distinct ids.  The 2k top-k ids and mask
 // words of p are fetched up front (two slots per lane), so the only
 // dependent loads left are the candidate ids themselves.
-__device__ int build_set(const CoreArgs& a, const WarpSet& ws, int p, unsigned tmask) {
+__device__ int build_set(const CoreArgs& a, const WarpSet& ws, int p, unsigned tmask, uint64_t* firstOut) {
     const unsigned l = lane_id();
     const int slots = 2 * a.k;
     int rA = 0, rB = 0;
-    uint64_t mA[2] = {0, 0}, mB[2] = {0, 0};
+    uint64_t mA0 = 0, mA1 = 0, mB0 = 0, mB1 = 0;
     const unsigned long long* mk64 = reinterpret_cast<const unsigned long long*>(a.masks);
     if ((int)l < slots) {
         rA = __ldg(a.topK + (size_t)p * slots + l);
-        for (int wd = 0; wd < a.W && wd < 2; ++wd) mA[wd] = __ldg(mk64 + ((size_t)p * slots + l) * a.W + wd);
+        mA0 = __ldg(mk64 + ((size_t)p * slots + l) * a.W);
+        if (a.W > 1) mA1 = __ldg(mk64 + ((size_t)p * slots + l) * a.W + 1);
     }
     if ((int)l + 32 < slots) {
         rB = __ldg(a.topK + (size_t)p * slots + l + 32);
-        for (int wd = 0; wd < a.W && wd < 2; ++wd) mB[wd] = __ldg(mk64 + ((size_t)p * slots + l + 32) * a.W + wd);
+        mB0 = __ldg(mk64 + ((size_t)p * slots + l + 32) * a.W);
+        if (a.W > 1) mB1 = __ldg(mk64 + ((size_t)p * slots + l + 32) * a.W + 1);
     }
     if (l == 0) *ws.nUsed = 0;
     __syncwarp();
@@ -128,37 +133,44 @@ __device__ int build_set(const CoreArgs& a, const WarpSet& ws, int p, unsigned t
         for (int wd = 0; wd < a.W; ++wd) {
             uint64_t mk;
             if (wd < 2) {
-                const uint64_t mine = jj < 32 ? mA[wd] : mB[wd];
+                const uint64_t mine = jj < 32 ? (wd == 0 ? mA0 : mA1) : (wd == 0 ? mB0 : mB1);
                 const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)mine, src);
                 const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(mine >> 32), src);
                 mk = ((uint64_t)hi << 32) | lo;
             } else {
                 mk = __ldg(mk64 + ((size_t)p * slots + jj) * a.W + wd);
             }
-            if (!mk) continue;
+            uint32_t fresh[2] = {0u, 0u};
+            if (mk) {
 #pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                const int bit = half * 32 + (int)l;
-                if ((mk >> bit) & 1ull) {
-                    const int s = wd * 64 + bit;
-                    const int i = __ldg(lst + s);
-                    unsigned h = hash_pt(i, tmask);
-                    while (true) {
-                        const int old = atomicCAS(&ws.keys[h], kEmpty, i);
-                        if (old == kEmpty) {
-                            ws.used[atomicAdd(ws.nUsed, 1)] = (int)h;
-                            atomicAdd(&ws.cnts[h], 1);
-                            if (ws.dsts) ws.dsts[h] = a.dists[((size_t)p * slots + jj) * a.m + s];
-                            break;
+                for (int half = 0; half < 2; ++half) {
+                    const int bit = half * 32 + (int)l;
+                    bool isNew = false;
+                    if ((mk >> bit) & 1ull) {
+                        const int s = wd * 64 + bit;
+                        const int i = __ldg(lst + s);
+                        unsigned h = hash_pt(i, tmask);
+                        while (true) {
+                            const int old = atomicCAS(&ws.keys[h], kEmpty, i);
+                            if (old == kEmpty) {
+                                ws.used[atomicAdd(ws.nUsed, 1)] = (uint16_t)h;
+                                atomicAdd(&ws.cnts[h], 1);
+                                if (ws.dsts) ws.dsts[h] = a.dists[((size_t)p * slots + jj) * a.m + s];
+                                isNew = true;
+                                break;
+                            }
+                            if (old == i) {
+                                atomicAdd(&ws.cnts[h], 1);
+                                break;
+                            }
+                            h = (h + 1) & tmask;
                         }
-                        if (old == i) {
-                            atomicAdd(&ws.cnts[h], 1);
-                            break;
-                        }
-                        h = (h + 1) & tmask;
                     }
+                    fresh[half] = __ballot_sync(0xffffffffu, isNew);
                 }
             }
+            if (firstOut && l == 0)
+                firstOut[((size_t)p * slots + jj) * a.W + wd] = ((uint64_t)fresh[1] << 32) | fresh[0];
         }
     }
     __syncwarp();
@@ -203,7 +215,7 @@ __global__ void k_core_dedupe(CoreArgs a, int T) {
     const int gw = blockIdx.x * (blockDim.x >> 5) + w;
     const int nw = gridDim.x * (blockDim.x >> 5);
     for (int p = gw; p < a.n; p += nw) {
-        const int nd = build_set(a, ws, p, tmask);
+        const int nd = build_set(a, ws, p, tmask, a.firstMasks);
         const int64_t h0 = a.hubOff[p], h1 = a.hubOff[p + 1];
         const bool hub = h1 > h0;
         if (hub) mark_lists(a, ws, h0, h1, maskWords);
@@ -249,7 +261,7 @@ __global__ void k_core_emit(CoreArgs a, int T, const int64_t* __restrict__ nbOff
     const int gw = blockIdx.x * (blockDim.x >> 5) + w;
     const int nw = gridDim.x * (blockDim.x >> 5);
     for (int p = gw; p < a.n; p += nw) {
-        const int nd = build_set(a, ws, p, tmask);
+        const int nd = build_set(a, ws, p, tmask, nullptr);
         const int64_t h0 = a.hubOff[p], h1 = a.hubOff[p + 1];
         const bool hub = h1 > h0;
         if (hub) mark_lists(a, ws, h0, h1, maskWords);
@@ -318,14 +330,16 @@ __global__ void k_core_dist(CoreArgs a, const int64_t* __restrict__ nbOff, const
 
 }  // namespace
 
+// Table slots: a power of two above the most candidates a point can insert
+// (2km), so probing always ends; typical fill is well under half.
 int core_table_size(int k, int m) {
     int t = 64;
-    while (t < 2 * 2 * k * m) t <<= 1;
+    while (t < 2 * k * m + 1) t <<= 1;
     return t;
 }
 
 static size_t core_warp_bytes(const CoreArgs& a, int T, bool withDist) {
-    return sizeof(int) * (3 * (size_t)T + (2 * a.nproj + 31) / 32 + 1 + (withDist ? T : 0));
+    return sizeof(int) * (size_t)warp_set_words(T, (2 * a.nproj + 31) / 32, withDist);
 }
 
 static int core_grid(int n, int warps) {
@@ -336,7 +350,7 @@ static int core_grid(int n, int warps) {
 int launch_core_dedupe(const CoreArgs& a, cudaStream_t st) {
     const int T = core_table_size(a.k, a.m);
     const size_t perWarp = core_warp_bytes(a, T, a.dists != nullptr);
-    const int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (72 * 1024) / perWarp));
+    const int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (100 * 1024) / perWarp));
     const size_t sm = perWarp * warps;
     if (sm > 48 * 1024 &&
         cudaFuncSetAttribute(k_core_dedupe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
@@ -364,7 +378,7 @@ int launch_core_emit(const CoreArgs& a, const int64_t* nbOff, int32_t* nbIdx, fl
                      cudaStream_t st) {
     const int T = core_table_size(a.k, a.m);
     const size_t perWarp = core_warp_bytes(a, T, true);
-    const int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (72 * 1024) / perWarp));
+    const int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (100 * 1024) / perWarp));
     const size_t sm = perWarp * warps;
     if (sm > 48 * 1024 &&
         cudaFuncSetAttribute(k_core_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)

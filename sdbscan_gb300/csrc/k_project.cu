@@ -78,10 +78,6 @@ __global__ void __launch_bounds__(kCsPoints) k_colstats(const float* __restrict_
     scale[p] = s;
 }
 
-__device__ __forceinline__ float sign_apply(float v, const uint32_t* sw, int bitidx) {
-    return ((sw[bitidx >> 5] >> (bitidx & 31)) & 1u) ? v : -v;
-}
-
 // Warp bitonic sort of 32 u64 keys, one per lane, into descending lane order.
 __device__ __forceinline__ uint64_t warp_sort_desc(uint64_t x) {
     const unsigned l = lane_id();
@@ -197,6 +193,18 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
     __nv_bfloat162* ext = reinterpret_cast<__nv_bfloat162*>(base + warps * rowLen) + (size_t)w * a.nproj;
     for (int i = threadIdx.x; i < nsw; i += blockDim.x) sw[i] = a.signs[i];
     __syncthreads();
+    // Lane l's sign bits for its elements e = l + 32 j, one 32-bit mask per
+    // round (bit j): a set bit keeps the value, a clear bit negates it.
+    uint64_t laneSigns[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        uint64_t msk = 0;
+        for (int j = 0; j < NJ; ++j) {
+            const int e = (int)l + 32 * j;
+            if (e < FD) msk |= (uint64_t)((sw[(r * FD + e) >> 5] >> ((r * FD + e) & 31)) & 1u) << j;
+        }
+        laneSigns[r] = msk;
+    }
 
     // Per vector: (max v, max -v) over the warp's points, as bf16 rounded
     // toward -inf.  A rounded-down maximum is still a lower bound on a value
@@ -210,7 +218,24 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
         const float* x = a.X + (size_t)p * a.ldx;
         const float sc = scale[p];
         // transformed row -> Xt (zero padded to ld)
-        for (int i = (int)l; i < a.ld; i += 32) {
+        float v[NJ];
+        if (EMB == 0) {
+            // Cosine: the transformed row is the embedding; one division per element
+#pragma unroll
+            for (int j = 0; j < NJ; ++j) {
+                const int e = (int)l + 32 * j;
+                float t = 0.0f;
+                if (e < a.d) t = a.do_transform ? __fdiv_rn(__ldg(x + e), sc) : __ldg(x + e);
+                if (e < a.ld) a.Xt[(size_t)p * a.ld + e] = t;
+                v[j] = t;
+            }
+            for (int e = (int)l + 32 * NJ; e < a.ld; e += 32) {
+                float t = 0.0f;
+                if (e < a.d) t = a.do_transform ? __fdiv_rn(__ldg(x + e), sc) : __ldg(x + e);
+                a.Xt[(size_t)p * a.ld + e] = t;
+            }
+        }
+        for (int i = (int)l; EMB != 0 && i < a.ld; i += 32) {
             float t = 0.0f;
             if (i < a.d) {
                 t = __ldg(x + i);
@@ -263,14 +288,11 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
             }
             __syncwarp();
         }
-        float v[NJ];
 #pragma unroll
-        for (int j = 0; j < NJ; ++j) {
+        for (int j = 0; j < NJ && EMB != 0; ++j) {
             const int e = (int)l + 32 * j;
             float t = 0.0f;
-            if (EMB == 0) {
-                if (e < a.d) t = a.do_transform ? __fdiv_rn(__ldg(x + e), sc) : __ldg(x + e);
-            } else if (EMB == 1) {
+            if (EMB == 1) {
                 if (e < a.ker) t = a.E[(size_t)p * a.ker + e];
             } else {
                 if (e < FD) t = rowbuf[((a.d + 3) & ~3) + e];
@@ -281,18 +303,20 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
         // three rounds: random signs, then the Walsh-Hadamard transform
 #pragma unroll 1
         for (int r = 0; r < 3; ++r) {
+            const uint64_t sgn = ~laneSigns[r];  // bit j set: negate element j
 #pragma unroll
-            for (int j = 0; j < NJ; ++j) {
-                const int e = (int)l + 32 * j;
-                if (e < FD) v[j] = sign_apply(v[j], sw, r * FD + e);
-            }
+            for (int j = 0; j < NJ; ++j)
+                v[j] = __int_as_float(__float_as_int(v[j]) ^ (int)((uint32_t)((sgn >> j) & 1u) << 31));
 #pragma unroll
             for (int s = 1; s < 32; s <<= 1) {
                 if (s >= FD) break;
+                // lower element a: a + b; upper element b: a - b, i.e. fma(-1, b, a),
+                // exactly the reference's rounding either way
+                const float mul = (l & s) ? -1.0f : 1.0f;
 #pragma unroll
                 for (int j = 0; j < NJ; ++j) {
                     const float o = __shfl_xor_sync(0xffffffffu, v[j], s);
-                    v[j] = (l & s) ? __fsub_rn(o, v[j]) : __fadd_rn(v[j], o);
+                    v[j] = __fmaf_rn(mul, v[j], o);
                 }
             }
 #pragma unroll
