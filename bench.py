@@ -199,6 +199,34 @@ def run_ours(args, cfg):
     counters = eng.counters()
     labels, ncl = eng.labels()
 
+    # the BF16 screening mode on the same data: same eps decisions, tensor cores
+    bf16 = None
+    if not args.no_bf16:
+        eng.set_params(n_proj=cfg["n_proj"], topK=cfg["topK"], topM=cfg["topM"], distance=cfg["distance"],
+                       random_seed=42, precision=capi.PREC_BF16)
+        for _ in range(args.warmup):
+            eng.fit_sdbscan_device(X.data_ptr(), cfg["eps"], cfg["minPts"])
+        barrier()
+        sb, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        bstages = {}
+        sb.record(stream)
+        for _ in range(args.steps):
+            eng.fit_sdbscan_device(X.data_ptr(), cfg["eps"], cfg["minPts"])
+            for k_, v_ in eng.stage_ms().items():
+                bstages[k_] = bstages.get(k_, 0.0) + v_
+        eb.record(stream)
+        barrier()
+        bms = sb.elapsed_time(eb)
+        blabels, bncl = eng.labels()
+        bc = eng.counters()
+        from tests._metrics import adjusted_rand_score
+        bf16 = {"value": ws * n * args.steps / (bms / 1e3), "unit": "points/s", "ms_per_step": bms / args.steps,
+                "ari_vs_plain": adjusted_rand_score(labels, blabels), "labels_identical": bool(np.array_equal(labels, blabels)),
+                "rechecked_pairs": bc["rechecked"], "fallbacks": bc["fallbacks"],
+                "stage_ms": {k_: v_ / args.steps for k_, v_ in bstages.items()}}
+        eng.set_params(n_proj=cfg["n_proj"], topK=cfg["topK"], topM=cfg["topM"], distance=cfg["distance"],
+                       random_seed=42)
+
     # end to end through the public call: pinned host input, labels back
     Xh_t = torch.empty((n, d), dtype=torch.float32, pin_memory=True)
     Xh_t.copy_(X)
@@ -251,6 +279,7 @@ def run_ours(args, cfg):
         "roofline": roofline,
         "cpu_baseline": cpu,
         "stage_ms": stages,
+        "bf16_screening": bf16,
         "result": {"n_clusters": ncl, "noise": int((labels < 0).sum()), "topk_ties": counters["topk_ties"],
                    "topm_ties": counters["topm_ties"], "pairs_within_eps": counters["pairs"]},
     }
@@ -269,6 +298,7 @@ def main():
     ap.add_argument("--config", type=int, default=2, choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-sample", type=int, default=20000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-bf16", action="store_true")
     args = ap.parse_args()
     cfg = WORKLOADS[args.config]
     if args.impl == "reference":

@@ -201,8 +201,15 @@ struct DistArgs {
     int32_t* inRaw;       // n
     float* dists;         // n x 2k x m (optional)
     unsigned long long* pairs;  // pass counter
+    const int32_t* topKmat;     // n x 2k (the re-decision kernel maps slots back to lists)
 };
 int launch_dist(const DistArgs& a, cudaStream_t st);
+int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream_t st);
+int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, uint64_t* queue, int64_t qcap,
+                   unsigned long long* qcount, int32_t* err, int grid, cudaStream_t st,
+                   float* dbgAcc = nullptr);
+int launch_recheck(const DistArgs& a, const uint64_t* queue, const unsigned long long* qcount, int64_t qcap,
+                   cudaStream_t st);
 
 struct CoreArgs {
     int n, k, m, W, nproj, minPts;

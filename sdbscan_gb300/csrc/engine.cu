@@ -96,7 +96,7 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &listOff, &listFill, &members, &tileOff, &tileList, &hubCount, &hubOff, &hubLists, &masks, &inRaw,
             &aCount, &degree, &core, &parent, &border, &rootFlag, &labels, &nClusters, &scanTmp, &errFlags,
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
-            &kMask, &firstMasks};
+            &kMask, &firstMasks, &Xb, &queue};
 }
 
 // ---------------------------------------------------------------------------
@@ -367,8 +367,33 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     da.inRaw = i32(inRaw);
     da.dists = optics ? f32(dists) : nullptr;
     da.pairs = ctr + 3;
+    da.topKmat = i32(topK);
     SDB_CK(cudaMemsetAsync(inRaw.ptr, 0, sizeof(int32_t) * n, st));
-    L_(launch_dist(da, st));
+    bool screened = false;
+    if (p.precision == SDB_PREC_BF16 && p.distance == SDB_COSINE) {
+        // BF16 tensor-core screening + exact FP32 re-decision near eps
+        const int ldb = (d + 63) / 64 * 64;
+        const int64_t qcap = std::max<int64_t>(1 << 20, (int64_t)n * 2 * k * m / 8);
+        if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * ldb) || !ensure(queue, sizeof(uint64_t) * (size_t)qcap))
+            return SDB_ERR_NOMEM;
+        L_(launch_to_bf16(f32(Xt), ld, n, Xb.ptr, ldb, st));
+        const int grid = (int)std::min<int64_t>(maxTiles, 152 * 2);
+        L_(launch_dist_tc(da, Xb.ptr, ldb, static_cast<uint64_t*>(queue.ptr), qcap, ctr + 4,
+                          i32(errFlags) + 4, grid, st));
+        L_(launch_recheck(da, static_cast<const uint64_t*>(queue.ptr), ctr + 4, qcap, st));
+        if (!ok) return fail(SDB_ERR_CUDA, std::string("tensor-core distance launch failed: ") +
+                                               cudaGetErrorString(cudaGetLastError()));
+        int32_t tcErr = 0;
+        SDB_CK(cudaMemcpyAsync(&tcErr, i32(errFlags) + 4, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        SDB_CK(cudaStreamSynchronize(st));
+        screened = tcErr == 0;
+        if (!screened) {  // queue overflow or a timed-out wait: redo this stage on the plain path
+            SDB_CK(cudaMemsetAsync(inRaw.ptr, 0, sizeof(int32_t) * n, st));
+            SDB_CK(cudaMemsetAsync(ctr + 3, 0, sizeof(unsigned long long), st));
+            fallbacks += 1;
+        }
+    }
+    if (!screened) L_(launch_dist(da, st));
     if (!ok) return fail(SDB_ERR_CUDA, std::string("distance launch failed: ") + cudaGetErrorString(cudaGetLastError()));
     SDB_CK(cudaEventRecord(ev[5], st));
 
@@ -620,9 +645,9 @@ sdb_status sdb_get_projections(sdb_engine* e, float* out) {
 }
 sdb_status sdb_get_counters(sdb_engine* e, int64_t* out, int32_t n_out) {
     if (!e || !out) return SDB_ERR_ARG;
-    int64_t v[4] = {(int64_t)e->hostCounters[0], (int64_t)e->hostCounters[1], (int64_t)e->launchCount,
-                    (int64_t)e->hostCounters[3]};
-    for (int i = 0; i < n_out && i < 4; ++i) out[i] = v[i];
+    int64_t v[6] = {(int64_t)e->hostCounters[0], (int64_t)e->hostCounters[1], (int64_t)e->launchCount,
+                    (int64_t)e->hostCounters[3], (int64_t)e->hostCounters[4], (int64_t)e->fallbacks};
+    for (int i = 0; i < n_out && i < 6; ++i) out[i] = v[i];
     return SDB_OK;
 }
 sdb_status sdb_get_stage_ms(sdb_engine* e, float* ms, int32_t n_ms) {

@@ -33,7 +33,7 @@ struct sdb_engine {
     DevBuf Xin, Xt, scale, P, topK, chunkMax, chunkMin, thr, cand, candCount, topM, listCount, listOff, listFill,
         members, tileOff, tileList, hubCount, hubOff, hubLists, masks, inRaw, aCount, degree, core, parent, border,
         rootFlag, labels, nClusters, scanTmp, errFlags, counters, E, Rt, signs, compCosh, dists, coreDist, nbOff,
-        nbIdx, nbDist, nbFill, hubIdx, kMask, firstMasks;
+        nbIdx, nbDist, nbFill, hubIdx, kMask, firstMasks, Xb, queue;
 
     // results
     bool haveLabels = false, haveOptics = false, haveFit = false, lastOptics = false;
@@ -42,6 +42,7 @@ struct sdb_engine {
     int32_t* hostErr = nullptr;
     unsigned long long* hostCounters = nullptr;
     int launchCount = 0;
+    int64_t fallbacks = 0;  // BF16 screening fits redone on the plain path
     float stageMs[9] = {};
 
     bool ensure(DevBuf& b, size_t bytes);

@@ -1,0 +1,361 @@
+// Stage 4, BF16 screening mode: candidate dot products on the tcgen05 tensor
+// cores, with an exact FP32 re-decision of every pair near eps.
+//
+// Same grouped, gathered formulation as k_dist (tile = list l, 128 member rows,
+// 64 candidate columns), but the operands are BF16 copies of the unit-norm
+// rows and the products accumulate in FP32 in tensor memory:
+//   - operands are staged by cp.async into shared memory in the 128-byte
+//     swizzled K-major layout the MMA reads (8-row x 128-byte atoms, 16-byte
+//     chunk c of row r stored at chunk c ^ (r & 7)), 4 stages of 64 dimensions;
+//   - one thread issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=64,
+//     K=16) into a 128 x 64 FP32 accumulator in TMEM, and tcgen05.commit
+//     arrives on the stage's mbarrier when the MMAs have read it;
+//   - the epilogue reads the accumulator with tcgen05.ld (thread t = row t).
+//
+// Decision rule.  For unit vectors x, y and their BF16 roundings x', y'
+// (relative error <= 2^-8 each), |x'.y' - x.y| <= (2^-7 + 2^-16) * sum|x_i y_i|
+// <= 0.00783; FP32 accumulation of 784 exact products adds < 2^-10, and the
+// FP32 reference's own rounding < 5e-5.  A pair whose screened distance is
+// farther than kMargin = 0.0125 from eps is therefore on the same side of eps
+// as the reference's FP32 distance; every other pair goes to a queue and is
+// recomputed by k_recheck with the plain path's exact sequential FP32 dot.
+// The resulting masks are identical to the plain FP32 path's.
+//
+// Every wait on an mbarrier is bounded; on timeout the CTA records an error,
+// stops issuing work, drains its own copies, frees its TMEM and returns.
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+
+namespace sdb {
+namespace {
+
+constexpr int TM = 128, TN = 64, TKB = 64;  // rows, candidate columns, bf16 per stage row (128 B)
+constexpr int STAGES = 4, NT = 128;
+constexpr int A_BYTES = TM * 128, B_BYTES = TN * 128, STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr float kMargin = 0.0125f;
+constexpr uint32_t kTmemCols = 64;
+constexpr long long kWaitLimit = 1LL << 22;  // bounded spins on an mbarrier
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait; returns false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (long long it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
+// core matrices 1024 bytes apart (SBO), start address in 16-byte units.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFF) >> 4);          // start address
+    d |= (uint64_t)1 << 16;                          // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;                // stride byte offset
+    d |= (uint64_t)1 << 46;                          // descriptor version
+    d |= (uint64_t)2 << 61;                          // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, M = 128, N = 64.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
+                            ((uint32_t)(TM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Swizzled byte offset of 16-byte chunk c (0..7) of row r in an operand tile.
+__device__ __forceinline__ uint32_t sw128(int r, int c) {
+    return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
+}
+
+__global__ void __launch_bounds__(NT, 1) k_dist_tc(DistArgs a, const __nv_bfloat16* __restrict__ Xb, int ldb,
+                                                  uint64_t* __restrict__ queue, int64_t qcap,
+                                                  unsigned long long* __restrict__ qcount, int32_t* __restrict__ err,
+                                                  float* __restrict__ dbgAcc) {
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    __shared__ uint64_t bars[STAGES];
+    __shared__ uint32_t tmemBase;
+    __shared__ int rowPoint[TM], rowSlot[TM], colPoint[TN], colCount[TN];
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t base = (smem_u32(smraw) + 1023u) & ~1023u;  // 1024-aligned operand tiles
+
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmemBase)),
+                     "r"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmemBase;
+    uint32_t phaseBits = 0;  // bit s: parity of the next completion of stage s's barrier
+    bool timedOut = false;
+    const int nk = ldb / TKB;
+    const int64_t total = *a.tileTotal;
+
+    for (int64_t t = blockIdx.x; t < total; t += gridDim.x) {
+        const int l = a.tileList[t];
+        const int64_t ti = t - a.tileOff[l];
+        const int mt = (int)(ti / a.nct), ct = (int)(ti % a.nct);
+        const int64_t mbeg = a.listOff[l] + (int64_t)mt * TM, mend = a.listOff[l + 1];
+        const int r = l % a.nproj, side = l / a.nproj;
+        const int32_t* cand = a.topM + (size_t)r * 2 * a.m + side * a.m;
+        for (int i = tid; i < TM; i += NT) {
+            const int64_t q = mbeg + i;
+            if (q < mend) {
+                const int2 mb = a.members[q];
+                rowPoint[i] = mb.x;
+                rowSlot[i] = mb.y;
+            } else {
+                rowPoint[i] = -1;
+                rowSlot[i] = 0;
+            }
+        }
+        for (int j = tid; j < TN; j += NT) {
+            const int c = ct * TN + j;
+            colPoint[j] = c < a.m ? cand[c] : -1;
+            colCount[j] = 0;
+        }
+        __syncthreads();
+
+        auto load_stage = [&](int stage, int kc) {
+            const uint32_t sA = base + stage * STAGE_BYTES, sB = sA + A_BYTES;
+            const int k0 = kc * TKB;
+#pragma unroll
+            for (int it = 0; it < (TM * 8) / NT; ++it) {  // 8 per thread
+                const int idx = tid + it * NT, row = idx >> 3, c = idx & 7;
+                const int p = rowPoint[row];
+                const bool ok = p >= 0;
+                cp_async16(sA + sw128(row, c), ok ? Xb + (size_t)p * ldb + k0 + c * 8 : Xb, ok);
+            }
+#pragma unroll
+            for (int it = 0; it < (TN * 8) / NT; ++it) {  // 4 per thread
+                const int idx = tid + it * NT, row = idx >> 3, c = idx & 7;
+                const int p = colPoint[row];
+                const bool ok = p >= 0;
+                cp_async16(sB + sw128(row, c), ok ? Xb + (size_t)p * ldb + k0 + c * 8 : Xb, ok);
+            }
+        };
+
+        // prologue
+        for (int s = 0; s < STAGES - 1; ++s) {
+            if (s < nk) load_stage(s, s);
+            asm volatile("cp.async.commit_group;\n" ::);
+        }
+        for (int kc = 0; kc < nk; ++kc) {
+            const int stage = kc % STAGES;
+            asm volatile("cp.async.wait_group %0;\n" ::"n"(STAGES - 2));
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // cp.async data -> async proxy
+            __syncthreads();
+            if (tid == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t sA = base + stage * STAGE_BYTES, sB = sA + A_BYTES;
+#pragma unroll
+                for (int k = 0; k < TKB / 16; ++k)
+                    mma_bf16(tmem, smem_desc(sA + k * 32), smem_desc(sB + k * 32), (kc > 0 || k > 0) ? 1u : 0u);
+                mma_commit(smem_u32(&bars[stage]));
+            }
+            const int nxt = kc + STAGES - 1;
+            if (nxt < nk) {
+                const int ns = nxt % STAGES;
+                if (kc >= 1) {  // stage ns was read by the MMAs of chunk kc - 1
+                    if (!mbar_wait(smem_u32(&bars[ns]), (phaseBits >> ns) & 1u)) timedOut = true;
+                    phaseBits ^= 1u << ns;
+                }
+                load_stage(ns, nxt);
+            }
+            asm volatile("cp.async.commit_group;\n" ::);
+        }
+        // chunks [0, nk - STAGES) were waited on inside the loop; wait for the rest
+        for (int c = (nk > STAGES ? nk - STAGES : 0); c < nk; ++c) {
+            const int s = c % STAGES;
+            if (!mbar_wait(smem_u32(&bars[s]), (phaseBits >> s) & 1u)) timedOut = true;
+            phaseBits ^= 1u << s;
+        }
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+
+        // epilogue: thread tid owns row tid
+        const int row = tid;
+        const int p = rowPoint[row];
+        uint64_t bits = 0;
+        int nPass = 0;
+#pragma unroll
+        for (int c16 = 0; c16 < TN / 16; ++c16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c16 * 16), v);
+            if (dbgAcc != nullptr && t == 0) {  // accumulator of the first tile, for layout checks
+#pragma unroll
+                for (int j = 0; j < 16; ++j) dbgAcc[row * TN + c16 * 16 + j] = v[j];
+            }
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int col = c16 * 16 + j;
+                const int q = colPoint[col];
+                bool pass = false, unsure = false;
+                if (p >= 0 && q >= 0 && p != q) {
+                    const float dist = 1.0f - v[j];
+                    pass = dist <= a.eps - kMargin;
+                    unsure = !pass && dist <= a.eps + kMargin;
+                }
+                const unsigned um = __ballot_sync(0xffffffffu, unsure);
+                if (um) {
+                    const int leader = __ffs(um) - 1;
+                    unsigned long long at0 = 0;
+                    if (lane == leader) at0 = atomicAdd(qcount, (unsigned long long)__popc(um));
+                    at0 = __shfl_sync(0xffffffffu, at0, leader);
+                    if (unsure) {
+                        const unsigned long long at = at0 + __popc(um & ((1u << lane) - 1u));
+                        if ((int64_t)at < qcap)
+                            queue[at] = ((uint64_t)(uint32_t)p << 32) | ((uint32_t)rowSlot[row] << 16) |
+                                        (uint32_t)(ct * TN + col);
+                        else
+                            atomicExch(err, 2);
+                    }
+                }
+                if (pass) {
+                    bits |= 1ull << col;
+                    ++nPass;
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, pass);
+                if (lane == 0 && b) atomicAdd(&colCount[col], __popc(b));
+            }
+        }
+        if (p >= 0) a.masks[((size_t)p * 2 * a.k + rowSlot[row]) * a.W + ct] = bits;
+        const int wp = warp_sum(nPass);
+        if (lane == 0 && wp) atomicAdd(a.pairs, (unsigned long long)wp);
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        for (int j = tid; j < TN; j += NT)
+            if (colCount[j]) atomicAdd(a.inRaw + colPoint[j], colCount[j]);
+        // a timed-out wait anywhere in the CTA ends the CTA's work (uniformly)
+        if (__syncthreads_or(timedOut ? 1 : 0)) {
+            if (tid == 0) atomicExch(err, 1);
+            break;
+        }
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
+}
+
+// Exact FP32 re-decision of the queued pairs: the plain path's sequential
+// fmaf dot over ascending dimensions, so the decision equals k_dist's.
+__global__ void k_recheck(DistArgs a, const uint64_t* __restrict__ queue, const unsigned long long* __restrict__ qcount,
+                          int64_t qcap) {
+    const int64_t nq = (int64_t)min((unsigned long long)qcap, *qcount);
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nq; e += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t v = queue[e];
+        const int p = (int)(v >> 32), slot = (int)((v >> 16) & 0xFFFF), col = (int)(v & 0xFFFF);
+        const int r = __ldg(a.topKmat + (size_t)p * 2 * a.k + slot);
+        const int side = slot >= a.k;
+        const int q = __ldg(a.topM + (size_t)r * 2 * a.m + side * a.m + col);
+        const float4* x = reinterpret_cast<const float4*>(a.Xt + (size_t)p * a.ld);
+        const float4* y = reinterpret_cast<const float4*>(a.Xt + (size_t)q * a.ld);
+        float s = 0.0f;
+        for (int i = 0; i < a.ld / 4; ++i) {
+            const float4 xa = __ldg(x + i), ya = __ldg(y + i);
+            s = __fmaf_rn(xa.x, ya.x, s);
+            s = __fmaf_rn(xa.y, ya.y, s);
+            s = __fmaf_rn(xa.z, ya.z, s);
+            s = __fmaf_rn(xa.w, ya.w, s);
+        }
+        const float dist = __fsub_rn(1.0f, s);
+        if (dist <= a.eps) {
+            atomicOr(reinterpret_cast<unsigned long long*>(a.masks) + ((size_t)p * 2 * a.k + slot) * a.W + col / 64,
+                     1ull << (col % 64));
+            atomicAdd(a.inRaw + q, 1);
+            atomicAdd(a.pairs, 1ull);
+        }
+    }
+}
+
+// Xt (FP32, row stride ld) -> Xb (BF16, row stride ldb, zero padded).
+__global__ void k_to_bf16(const float* __restrict__ Xt, int ld, int n, __nv_bfloat16* __restrict__ Xb, int ldb) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t per = (size_t)ldb / 8;
+    if (q >= (size_t)n * per) return;
+    const int p = (int)(q / per), c0 = (int)(q % per) * 8;
+    __align__(16) __nv_bfloat16 out[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int c = c0 + i;
+        out[i] = __float2bfloat16_rn(c < ld ? Xt[(size_t)p * ld + c] : 0.0f);
+    }
+    *reinterpret_cast<uint4*>(Xb + (size_t)p * ldb + c0) = *reinterpret_cast<const uint4*>(out);
+}
+
+}  // namespace
+
+int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream_t st) {
+    const size_t total = (size_t)n * (ldb / 8);
+    k_to_bf16<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(Xt, ld, n, static_cast<__nv_bfloat16*>(Xb), ldb);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, uint64_t* queue, int64_t qcap,
+                   unsigned long long* qcount, int32_t* err, int grid, cudaStream_t st, float* dbgAcc) {
+    const size_t sm = (size_t)STAGES * STAGE_BYTES + 1024;
+    if (cudaFuncSetAttribute(k_dist_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+        return -1;
+    k_dist_tc<<<grid, NT, sm, st>>>(a, static_cast<const __nv_bfloat16*>(Xb), ldb, queue, qcap, qcount, err, dbgAcc);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int launch_recheck(const DistArgs& a, const uint64_t* queue, const unsigned long long* qcount, int64_t qcap,
+                   cudaStream_t st) {
+    k_recheck<<<152 * 16, 256, 0, st>>>(a, queue, qcount, qcap);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int dist_tc_tile_rows() { return TM; }
+
+}  // namespace sdb

@@ -227,3 +227,34 @@ def test_fit_soptics_matches_oracle(port, n, d, k, m, eps, minPts):
     np.testing.assert_array_equal(eng.core_dist(), o_cd)
     np.testing.assert_array_equal(order, o_order)
     np.testing.assert_array_equal(reach, o_reach)
+
+
+@pytest.mark.parametrize("gen,n,d,k,m,eps,minPts", [
+    ("vmf", 3000, 64, 5, 20, 0.15, 10),
+    ("vmf", 30000, 128, 5, 50, 0.15, 20),
+    ("mnist", 20000, 784, 10, 50, 0.25, 50),
+])
+def test_bf16_screening_equals_plain(gen, n, d, k, m, eps, minPts):
+    """BF16 tensor-core screening with FP32 re-decision near eps gives the
+    plain FP32 path's eps decisions, hence identical core flags,
+    neighbourhood sizes, labels and n_clusters_."""
+    from sdbscan_gb300 import capi, datasets
+    if gen == "mnist":
+        X, _ = datasets.cfg2_mnist_like(n, d, seed=71)
+    else:
+        X, _ = datasets.cfg1_cosine(n, d, seed=72)
+    res = {}
+    for prec in (capi.PREC_FP32, capi.PREC_BF16):
+        eng = capi.Engine(n, d)
+        eng.set_params(n_proj=1024, topK=k, topM=m, distance="Cosine", random_seed=17, precision=prec)
+        eng.fit_sdbscan(X, eps, minPts)
+        res[prec] = (eng.labels(), eng.core(), eng.counters())
+    (l32, c32, k32), (l16, c16, k16) = res[capi.PREC_FP32], res[capi.PREC_BF16]
+    assert k16["fallbacks"] == 0
+    if gen == "mnist":  # distances spread across eps there, so some pairs are re-decided
+        assert k16["rechecked"] > 0
+    assert k16["pairs"] == k32["pairs"]
+    np.testing.assert_array_equal(c16[0], c32[0])
+    np.testing.assert_array_equal(c16[1], c32[1])
+    np.testing.assert_array_equal(l16[0], l32[0])
+    assert l16[1] == l32[1]
