@@ -151,6 +151,34 @@ def run_reference(args, cfg):
     return 0
 
 
+def run_batched(args, local):
+    """Config 5: 64 vMF mixtures (n log-uniform 2K..200K, d in {64,128,256}),
+    an 8-value eps sweep each (0.05 .. 0.40), minPts 20, D 1024, k 5, m 50,
+    as one CUDA graph.  Rate = sum(n) * 8 / graph time."""
+    import torch
+    from sdbscan_gb300 import capi, datasets
+    sets = datasets.cfg5_batch_torch(64, seed=5007, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+    eps_list = [0.05 * (i + 1) for i in range(8)]
+    ptrs = [(X.data_ptr(), X.shape[0], X.shape[1]) for X, _ in sets]
+    t0 = time.perf_counter()
+    b = capi.Batch(ptrs, eps_list, 20, device=local, n_proj=1024, topK=5, topM=50, distance="Cosine",
+                   random_seed=42)
+    setup_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        b.run()
+    times = [b.run() for _ in range(args.steps)]
+    total_n = sum(X.shape[0] for X, _ in sets)
+    ms = sum(times) / len(times)
+    ncl = [b.labels(i, 3)[1] for i in range(4)]
+    out = {"workload": "cfg5_64sets_x8eps", "value": total_n * len(eps_list) / (ms / 1e3),
+           "unit": "point-clusterings/s", "ms_per_batch": ms, "sets": len(sets), "points": total_n,
+           "eps": [round(e, 2) for e in eps_list], "launches_per_batch": 1, "graph_lanes": b.lanes(),
+           "setup_s": setup_s, "n_clusters_eps0.20_first4": ncl}
+    b.close()
+    return out
+
+
 def run_ours(args, cfg):
     import numpy as np
     import torch
@@ -244,6 +272,7 @@ def run_ours(args, cfg):
     e2e_value = ws * n * args.steps / e2e_s
     assert np.array_equal(lab_e2e, labels), "host-input and device-input fits disagree"
 
+    batched = None if args.no_batched else run_batched(args, local)
     if rank != 0:
         return 0
     # dominant kernel: the distance stage (one k_dist launch per fit)
@@ -280,6 +309,7 @@ def run_ours(args, cfg):
         "cpu_baseline": cpu,
         "stage_ms": stages,
         "bf16_screening": bf16,
+        "batched": batched,
         "result": {"n_clusters": ncl, "noise": int((labels < 0).sum()), "topk_ties": counters["topk_ties"],
                    "topm_ties": counters["topm_ties"], "pairs_within_eps": counters["pairs"]},
     }
@@ -299,6 +329,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=20000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-bf16", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     cfg = WORKLOADS[args.config]
     if args.impl == "reference":

@@ -96,6 +96,15 @@ sdb_status sdb_fit_sdbscan_device(sdb_engine* e, const float* X_device, float ep
 sdb_status sdb_fit_soptics(sdb_engine* e, const float* X_host, float eps, int32_t minPts);
 sdb_status sdb_fit_soptics_device(sdb_engine* e, const float* X_device, float eps, int32_t minPts);
 
+/* test_sDbscan(X, eps, rangeEps, n_tests, minPts)  (src/sDbscan.h:187,
+ * src/sDbscan.cpp:980-1039): the index and the candidate distances are built
+ * once, then core points and clusters for every eps in eps[0..n_eps).
+ * labels: n_eps x n_points int32 (row i for eps[i]); n_clusters: n_eps.  The
+ * reference derives its list as eps + i * rangeEps and writes each labelling
+ * to a file; here the caller passes the list and gets the labellings back. */
+sdb_status sdb_fit_sdbscan_sweep(sdb_engine* e, const float* X_host, const float* eps, int32_t n_eps, int32_t minPts,
+                                 int32_t* labels, int32_t* n_clusters);
+
 /* labels_ and n_clusters_  (src/sDbscan.h:67-68; python_wrapper.cpp:31-32).
  * labels: n_points int32. */
 sdb_status sdb_get_labels(sdb_engine* e, int32_t* labels, int32_t* n_clusters);
@@ -142,6 +151,25 @@ void* sdb_engine_stream(sdb_engine* e);
 
 /* Message of the last error on this engine ("" if none). */
 const char* sdb_last_error(sdb_engine* e);
+
+/* Many independent datasets, each with the same eps sweep, recorded once into
+ * one CUDA graph and replayed with a single launch.  No reference counterpart
+ * (the reference runs test_sDbscan per dataset, src/sDbscan.cpp:980-1039).
+ *   X_device[i]: d_i x n_i column-major data of set i, device memory, kept
+ *                valid for the batch's lifetime
+ * The batch plans every set once (sizing run), then times graphs with 4, 8,
+ * 16, 32 and 64 sets in flight and keeps the fastest (sdb_batch_lanes).
+ * sdb_batch_run replays it; sdb_batch_labels reads set i's labelling for eps
+ * index j. */
+typedef struct sdb_batch sdb_batch;
+sdb_status sdb_batch_create(int32_t n_sets, const int32_t* n_points, const int32_t* n_features,
+                            const float* const* X_device, const sdb_params* p, const float* eps, int32_t n_eps,
+                            int32_t minPts, int32_t device, sdb_batch** out);
+sdb_status sdb_batch_run(sdb_batch* b, float* elapsed_ms);
+sdb_status sdb_batch_labels(sdb_batch* b, int32_t set, int32_t eps_index, int32_t* labels, int32_t* n_clusters);
+int32_t sdb_batch_lanes(sdb_batch* b);
+void sdb_batch_destroy(sdb_batch* b);
+const char* sdb_batch_last_error(sdb_batch* b);
 
 /* Per-vector top-m selection (the top-m stage of a fit) that allocates no
  * device memory.  No counterpart in the reference: it exists for callers that

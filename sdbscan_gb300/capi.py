@@ -22,7 +22,9 @@ STATUS = {0: "SDB_OK", 1: "SDB_ERR_ARG", 2: "SDB_ERR_CUDA", 3: "SDB_ERR_NEGATIVE
 EXPORTS = ["sdb_params_default", "sdb_engine_create", "sdb_engine_destroy", "sdb_set_params", "sdb_fit_sdbscan",
            "sdb_fit_sdbscan_device", "sdb_fit_soptics", "sdb_fit_soptics_device", "sdb_get_labels", "sdb_get_optics",
            "sdb_clear", "sdb_get_topk", "sdb_get_topm", "sdb_get_core", "sdb_get_core_dist", "sdb_get_projections",
-           "sdb_get_counters", "sdb_get_stage_ms", "sdb_engine_stream", "sdb_last_error", "sdb_topm_noalloc"]
+           "sdb_get_counters", "sdb_get_stage_ms", "sdb_engine_stream", "sdb_last_error", "sdb_topm_noalloc",
+           "sdb_fit_sdbscan_sweep", "sdb_batch_create", "sdb_batch_run", "sdb_batch_labels", "sdb_batch_lanes",
+           "sdb_batch_destroy", "sdb_batch_last_error"]
 
 
 class SdbParams(ctypes.Structure):
@@ -71,6 +73,16 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.sdb_last_error.argtypes = [vp]
     L.sdb_last_error.restype = ctypes.c_char_p
     L.sdb_topm_noalloc.argtypes = [vp, i32, i32, i32, vp, vp]
+    L.sdb_fit_sdbscan_sweep.argtypes = [vp, vp, vp, i32, i32, vp, vp]
+    L.sdb_batch_create.argtypes = [i32, vp, vp, vp, ctypes.POINTER(SdbParams), vp, i32, i32, i32,
+                                   ctypes.POINTER(vp)]
+    L.sdb_batch_run.argtypes = [vp, ctypes.POINTER(f32)]
+    L.sdb_batch_labels.argtypes = [vp, i32, i32, vp, vp]
+    L.sdb_batch_lanes.argtypes = [vp]
+    L.sdb_batch_lanes.restype = i32
+    L.sdb_batch_destroy.argtypes = [vp]
+    L.sdb_batch_last_error.argtypes = [vp]
+    L.sdb_batch_last_error.restype = ctypes.c_char_p
     _LIB = L
     return L
 
@@ -128,6 +140,17 @@ class Engine:
 
     def fit_sdbscan_device(self, x_dev_ptr: int, eps: float, minPts: int):
         self._check(self.L.sdb_fit_sdbscan_device(self.h, ctypes.c_void_p(x_dev_ptr), ctypes.c_float(eps), minPts))
+
+    def fit_sdbscan_sweep(self, X: np.ndarray, eps_list, minPts: int):
+        """test_sDbscan: index and distances once, labels for every eps.
+        Returns (labels [n_eps, n], n_clusters [n_eps])."""
+        X = self._host(X)
+        eps = np.ascontiguousarray(eps_list, dtype=np.float32)
+        labels = np.empty((eps.shape[0], self.n), np.int32)
+        ncl = np.empty(eps.shape[0], np.int32)
+        self._check(self.L.sdb_fit_sdbscan_sweep(self.h, _ptr(X), _ptr(eps), eps.shape[0], minPts, _ptr(labels),
+                                                 _ptr(ncl)))
+        return labels, ncl
 
     def fit_soptics(self, X: np.ndarray, eps: float, minPts: int):
         X = self._host(X)
@@ -205,3 +228,58 @@ def topm_noalloc(proj_dev_ptr: int, n_points: int, n_proj: int, topM: int, out_d
                            ctypes.c_void_p(stream) if stream else None)
     if s != 0:
         raise SdbError(s, "sdb_topm_noalloc failed")
+
+
+class Batch:
+    """sdb_batch_*: many datasets, one eps sweep each, replayed as one CUDA graph.
+    X_device: list of (data_ptr, n, d) of device-resident (n, d) float32 rows."""
+
+    def __init__(self, X_device, eps_list, minPts: int, device: int = 0, **params):
+        self.L = load()
+        p = SdbParams()
+        self.L.sdb_params_default(ctypes.byref(p))
+        for k_, v_ in params.items():
+            setattr(p, k_, DISTANCES[v_] if k_ == "distance" else v_)
+        self.ns = len(X_device)
+        self.sizes = [int(n) for _, n, _ in X_device]
+        n_arr = (ctypes.c_int32 * self.ns)(*[int(n) for _, n, _ in X_device])
+        d_arr = (ctypes.c_int32 * self.ns)(*[int(d) for _, _, d in X_device])
+        x_arr = (ctypes.c_void_p * self.ns)(*[int(ptr) for ptr, _, _ in X_device])
+        self.eps = np.ascontiguousarray(eps_list, dtype=np.float32)
+        h = ctypes.c_void_p()
+        s = self.L.sdb_batch_create(self.ns, n_arr, d_arr, x_arr, ctypes.byref(p), _ptr(self.eps),
+                                    self.eps.shape[0], minPts, device, ctypes.byref(h))
+        self.h = h
+        if s != 0:
+            msg = self.L.sdb_batch_last_error(h).decode() if h.value else ""
+            self.close()
+            raise SdbError(s, "sdb_batch_create: " + msg)
+
+    def run(self) -> float:
+        ms = ctypes.c_float()
+        s = self.L.sdb_batch_run(self.h, ctypes.byref(ms))
+        if s != 0:
+            raise SdbError(s, self.L.sdb_batch_last_error(self.h).decode())
+        return ms.value
+
+    def labels(self, set_index: int, eps_index: int):
+        out = np.empty(self.sizes[set_index], np.int32)
+        nc = ctypes.c_int32()
+        s = self.L.sdb_batch_labels(self.h, set_index, eps_index, _ptr(out), ctypes.byref(nc))
+        if s != 0:
+            raise SdbError(s, self.L.sdb_batch_last_error(self.h).decode())
+        return out, nc.value
+
+    def lanes(self) -> int:
+        return int(self.L.sdb_batch_lanes(self.h))
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.sdb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -204,6 +204,7 @@ struct DistArgs {
     const int32_t* topKmat;     // n x 2k (the re-decision kernel maps slots back to lists)
 };
 int launch_dist(const DistArgs& a, cudaStream_t st);
+int launch_masks_from_dists(const DistArgs& a, cudaStream_t st);
 int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream_t st);
 int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, uint64_t* queue, int64_t qcap,
                    unsigned long long* qcount, int32_t* err, int grid, cudaStream_t st,

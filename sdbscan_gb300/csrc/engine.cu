@@ -96,7 +96,7 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &listOff, &listFill, &members, &tileOff, &tileList, &hubCount, &hubOff, &hubLists, &masks, &inRaw,
             &aCount, &degree, &core, &parent, &border, &rootFlag, &labels, &nClusters, &scanTmp, &errFlags,
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
-            &kMask, &firstMasks, &Xb, &queue};
+            &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl};
 }
 
 // ---------------------------------------------------------------------------
@@ -160,8 +160,11 @@ void sdb_engine::host_random(int seedUsed) {
 // ---------------------------------------------------------------------------
 // the fit pipeline
 // ---------------------------------------------------------------------------
-sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts, bool optics) {
+sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts, bool optics, const SweepSpec* sw) {
     if (!paramsSet) return fail(SDB_ERR_STATE, "set_params must be called before a fit");
+    const bool sweep = sw != nullptr, capture = sw != nullptr && sw->capture;
+    if (sweep && (optics || sw->nEps < 1 || !sw->eps || !sw->labelsDev || !sw->nclDev))
+        return fail(SDB_ERR_ARG, "invalid eps sweep");
     haveLabels = haveOptics = false;
     if (optics && minPts < 2) return fail(SDB_ERR_ARG, "minPts must be >= 2 for sOPTICS");
     if (X == nullptr) return fail(SDB_ERR_ARG, "X is null");
@@ -169,9 +172,11 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     if (s != SDB_OK) return s;
     const sdb_params& p = prm;
     const int k = p.topK, m = p.topM, D = p.n_proj;
-    seedUsed = p.random_seed >= 0 ? p.random_seed
-                                  : (int)(unsigned)std::chrono::system_clock::now().time_since_epoch().count();
-    host_random(seedUsed);
+    if (!capture) {
+        seedUsed = p.random_seed >= 0 ? p.random_seed
+                                      : (int)(unsigned)std::chrono::system_clock::now().time_since_epoch().count();
+        host_random(seedUsed);
+    }
     cudaError_t ce = cudaSetDevice(device);
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
 
@@ -213,7 +218,8 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     const size_t maxHubs = std::min<size_t>((size_t)n, (size_t)L * m);
     ok &= ensure(hubIdx, sizeof(int32_t) * n) && ensure(kMask, sizeof(uint32_t) * maxHubs * maskWords);
     if (rff) ok &= ensure(E, sizeof(float) * (size_t)n * ker) && ensure(Rt, sizeof(float) * hostRt.size());
-    if (optics) ok &= ensure(dists, sizeof(float) * (size_t)n * 2 * k * m) && ensure(coreDist, sizeof(float) * n);
+    if (optics || sweep) ok &= ensure(dists, sizeof(float) * (size_t)n * 2 * k * m);
+    if (optics) ok &= ensure(coreDist, sizeof(float) * n);
     if (!ok) return SDB_ERR_NOMEM;
 
     cudaStream_t st = stream;
@@ -228,16 +234,20 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
     } while (0)
 
-    SDB_CK(cudaEventRecord(ev[0], st));
+    if (!capture) SDB_CK(cudaEventRecord(ev[0], st));
     const float* Xd = X;
     if (!xOnDevice) {
         SDB_CK(cudaMemcpyAsync(Xin.ptr, X, sizeof(float) * (size_t)n * d, cudaMemcpyHostToDevice, st));
         Xd = static_cast<const float*>(Xin.ptr);
     }
-    SDB_CK(cudaEventRecord(ev[1], st));
-    SDB_CK(cudaMemcpyAsync(signs.ptr, hostSigns.data(), sizeof(uint32_t) * hostSigns.size(), cudaMemcpyHostToDevice, st));
-    if (!hostCosh.empty())
-        SDB_CK(cudaMemcpyAsync(compCosh.ptr, hostCosh.data(), sizeof(double) * hostCosh.size(), cudaMemcpyHostToDevice, st));
+    if (!capture) SDB_CK(cudaEventRecord(ev[1], st));
+    if (!capture) {  // a captured sweep reuses the signs its sizing run uploaded
+        SDB_CK(cudaMemcpyAsync(signs.ptr, hostSigns.data(), sizeof(uint32_t) * hostSigns.size(),
+                               cudaMemcpyHostToDevice, st));
+        if (!hostCosh.empty())
+            SDB_CK(cudaMemcpyAsync(compCosh.ptr, hostCosh.data(), sizeof(double) * hostCosh.size(),
+                                   cudaMemcpyHostToDevice, st));
+    }
     SDB_CK(cudaMemsetAsync(errFlags.ptr, 0, sizeof(int32_t) * 8, st));
     SDB_CK(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long) * 8, st));
     unsigned long long* ctr = static_cast<unsigned long long*>(counters.ptr);
@@ -270,7 +280,8 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     pa.compCosh = static_cast<const double*>(compCosh.ptr);
     pa.ln4 = ln4;
     if (rff) {
-        SDB_CK(cudaMemcpyAsync(Rt.ptr, hostRt.data(), sizeof(float) * hostRt.size(), cudaMemcpyHostToDevice, st));
+        if (!capture)
+            SDB_CK(cudaMemcpyAsync(Rt.ptr, hostRt.data(), sizeof(float) * hostRt.size(), cudaMemcpyHostToDevice, st));
         L_(launch_pad_copy(Xd, n, d, f32(Xt), ld, st));
         L_(launch_rff(f32(Xt), ld, n, d, f32(Rt), ker / 2, f32(E), st));
         pa.X = f32(Xt);
@@ -280,7 +291,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     }
     L_(launch_project(pa, st));
     if (!ok) return fail(SDB_ERR_CUDA, std::string("projection launch failed: ") + cudaGetErrorString(cudaGetLastError()));
-    SDB_CK(cudaEventRecord(ev[2], st));
+    if (!capture) SDB_CK(cudaEventRecord(ev[2], st));
 
     // ---- stage 2: per-vector top-m -----------------------------------------
     TopMArgs ta{};
@@ -304,7 +315,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     L_(launch_topm_collect(ta, st));
     L_(launch_topm_select(ta, st));
     if (!ok) return fail(SDB_ERR_CUDA, std::string("top-m launch failed: ") + cudaGetErrorString(cudaGetLastError()));
-    SDB_CK(cudaEventRecord(ev[3], st));
+    if (!capture) SDB_CK(cudaEventRecord(ev[3], st));
 
     // ---- stage 3: inverted index, tiles, hub lists ---------------------------
     IndexArgs ia{};
@@ -341,7 +352,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     SDB_CK(cudaMemsetAsync(hubCount.ptr, 0, sizeof(int32_t) * n, st));
     L_(launch_hubs_scatter(ia, st));
     if (!ok) return fail(SDB_ERR_CUDA, std::string("index launch failed: ") + cudaGetErrorString(cudaGetLastError()));
-    SDB_CK(cudaEventRecord(ev[4], st));
+    if (!capture) SDB_CK(cudaEventRecord(ev[4], st));
 
     // ---- stage 4: distances + eps --------------------------------------------
     DistArgs da{};
@@ -363,14 +374,15 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     da.W = W;
     da.nct = nct;
     da.eps = eps;
+    if (sweep) da.eps = *std::max_element(sw->eps, sw->eps + sw->nEps);
     da.masks = static_cast<uint64_t*>(masks.ptr);
     da.inRaw = i32(inRaw);
-    da.dists = optics ? f32(dists) : nullptr;
+    da.dists = (optics || sweep) ? f32(dists) : nullptr;
     da.pairs = ctr + 3;
     da.topKmat = i32(topK);
     SDB_CK(cudaMemsetAsync(inRaw.ptr, 0, sizeof(int32_t) * n, st));
     bool screened = false;
-    if (p.precision == SDB_PREC_BF16 && p.distance == SDB_COSINE) {
+    if (p.precision == SDB_PREC_BF16 && p.distance == SDB_COSINE && !sweep) {
         // BF16 tensor-core screening + exact FP32 re-decision near eps
         const int ldb = (d + 63) / 64 * 64;
         const int64_t qcap = std::max<int64_t>(1 << 20, (int64_t)n * 2 * k * m / 8);
@@ -395,7 +407,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     }
     if (!screened) L_(launch_dist(da, st));
     if (!ok) return fail(SDB_ERR_CUDA, std::string("distance launch failed: ") + cudaGetErrorString(cudaGetLastError()));
-    SDB_CK(cudaEventRecord(ev[5], st));
+    if (!capture) SDB_CK(cudaEventRecord(ev[5], st));
 
     // ---- stage 5: neighbourhood sizes, core flags -----------------------------
     CoreArgs ca{};
@@ -423,10 +435,17 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     SDB_CK(cudaMemsetAsync(kMask.ptr, 0, sizeof(uint32_t) * maxHubs * maskWords, st));
     L_(launch_hub_masks(ca, i32(hubIdx), i64(rootFlag), static_cast<uint32_t*>(kMask.ptr), i64(scanTmp),
                         reinterpret_cast<int64_t*>(ctr + 5), st));
+    const int rounds = sweep ? sw->nEps : 1;
+    for (int ei = 0; ei < rounds; ++ei) {
+    if (sweep) {  // this eps: masks and reverse counts from the stored distances
+        da.eps = sw->eps[ei];
+        SDB_CK(cudaMemsetAsync(inRaw.ptr, 0, sizeof(int32_t) * n, st));
+        L_(launch_masks_from_dists(da, st));
+    }
     L_(launch_core_dedupe(ca, st));
     L_(launch_core_finish(ca, st));
     if (!ok) return fail(SDB_ERR_CUDA, std::string("core launch failed: ") + cudaGetErrorString(cudaGetLastError()));
-    SDB_CK(cudaEventRecord(ev[6], st));
+    if (!capture) SDB_CK(cudaEventRecord(ev[6], st));
 
     // ---- stage 6: clusters or sOPTICS ------------------------------------------
     if (!optics) {
@@ -451,12 +470,19 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         s = optics_stage(ca, launches);
         if (s != SDB_OK) return s;
     }
-    SDB_CK(cudaEventRecord(ev[7], st));
+    if (sweep) {
+        SDB_CK(cudaMemcpyAsync(sw->labelsDev + (size_t)ei * n, labels.ptr, sizeof(int32_t) * n,
+                               cudaMemcpyDeviceToDevice, st));
+        SDB_CK(cudaMemcpyAsync(sw->nclDev + ei, nClusters.ptr, sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+    }
+    }  // eps rounds
+    if (!capture) SDB_CK(cudaEventRecord(ev[7], st));
     SDB_CK(cudaMemcpyAsync(hostErr, errFlags.ptr, sizeof(int32_t) * 8, cudaMemcpyDeviceToHost, st));
     SDB_CK(cudaMemcpyAsync(hostCounters, counters.ptr, sizeof(unsigned long long) * 8, cudaMemcpyDeviceToHost, st));
+    launchCount = launches;
+    if (capture) return SDB_OK;  // flags are read by check_flags() after the graph has run
     SDB_CK(cudaEventRecord(ev[8], st));
     SDB_CK(cudaStreamSynchronize(st));
-    launchCount = launches;
 #undef SDB_CK
     for (int i = 0; i < 8; ++i) {
         float ms = 0.0f;
@@ -468,12 +494,8 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         cudaEventElapsedTime(&ms, ev[0], ev[8]);
         stageMs[8] = ms;
     }
-    if (hostErr[0]) return fail(SDB_ERR_NEGATIVE, "X is not non-negative (Chi2/JS need nonnegative data)");
-    if (hostErr[1])
-        return fail(SDB_ERR_ZERO_POINT, p.distance == SDB_COSINE ? "X has a point of zero norm (Cosine)"
-                                                                 : "X has a point of zero sum (Chi2/JS)");
-    if (hostErr[2]) return fail(SDB_ERR_ARG, "X has a non-finite value");
-    if (hostErr[3]) return fail(SDB_ERR_INTERNAL, "top-m selection found fewer candidates than topM");
+    s = check_flags();
+    if (s != SDB_OK) return s;
     if (optics) haveOptics = true;
     else haveLabels = true;
     haveFit = true;
@@ -486,6 +508,17 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         for (int i = 0; i < 9; ++i) std::printf("  %-14s %9.3f ms\n", names[i], stageMs[i]);
     }
     err.clear();
+    return SDB_OK;
+}
+
+// Error flags the kernels raised during the last (synchronised) fit.
+sdb_status sdb_engine::check_flags() {
+    if (hostErr[0]) return fail(SDB_ERR_NEGATIVE, "X is not non-negative (Chi2/JS need nonnegative data)");
+    if (hostErr[1])
+        return fail(SDB_ERR_ZERO_POINT, prm.distance == SDB_COSINE ? "X has a point of zero norm (Cosine)"
+                                                                   : "X has a point of zero sum (Chi2/JS)");
+    if (hostErr[2]) return fail(SDB_ERR_ARG, "X has a non-finite value");
+    if (hostErr[3]) return fail(SDB_ERR_INTERNAL, "top-m selection found fewer candidates than topM");
     return SDB_OK;
 }
 
@@ -578,6 +611,29 @@ sdb_status sdb_fit_soptics(sdb_engine* e, const float* X, float eps, int32_t min
 }
 sdb_status sdb_fit_soptics_device(sdb_engine* e, const float* X, float eps, int32_t minPts) {
     return e ? e->fit(X, true, eps, minPts, true) : SDB_ERR_ARG;
+}
+
+sdb_status sdb_fit_sdbscan_sweep(sdb_engine* e, const float* X, const float* eps, int32_t n_eps, int32_t minPts,
+                                 int32_t* labels, int32_t* n_clusters) {
+    if (!e) return SDB_ERR_ARG;
+    if (!eps || n_eps < 1 || !labels || !n_clusters) return e->fail(SDB_ERR_ARG, "eps list and outputs are required");
+    cudaSetDevice(e->device);
+    if (!e->ensure(e->sweepLabels, sizeof(int32_t) * (size_t)n_eps * e->n) ||
+        !e->ensure(e->sweepNcl, sizeof(int32_t) * n_eps))
+        return SDB_ERR_NOMEM;
+    SweepSpec sw;
+    sw.eps = eps;
+    sw.nEps = n_eps;
+    sw.labelsDev = static_cast<int32_t*>(e->sweepLabels.ptr);
+    sw.nclDev = static_cast<int32_t*>(e->sweepNcl.ptr);
+    sdb_status s = e->fit(X, false, eps[0], minPts, false, &sw);
+    if (s != SDB_OK) return s;
+    cudaError_t c = cudaMemcpyAsync(labels, sw.labelsDev, sizeof(int32_t) * (size_t)n_eps * e->n,
+                                    cudaMemcpyDeviceToHost, e->stream);
+    if (c == cudaSuccess)
+        c = cudaMemcpyAsync(n_clusters, sw.nclDev, sizeof(int32_t) * n_eps, cudaMemcpyDeviceToHost, e->stream);
+    if (c == cudaSuccess) c = cudaStreamSynchronize(e->stream);
+    return c == cudaSuccess ? SDB_OK : e->cuda_fail(c, "sweep download");
 }
 
 sdb_status sdb_get_labels(sdb_engine* e, int32_t* labels, int32_t* n_clusters) {

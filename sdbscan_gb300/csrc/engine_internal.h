@@ -14,6 +14,19 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+// Eps sweep of one fit (the reference's test_sDbscan pattern): the index and
+// the candidate distances are computed once, then core points and clusters
+// per eps value.  capture = enqueue only (no events, host syncs or pageable
+// uploads), for recording into a CUDA graph after a normal run has sized the
+// buffers and uploaded the random signs.
+struct SweepSpec {
+    const float* eps = nullptr;  // host, nEps values
+    int nEps = 0;
+    int32_t* labelsDev = nullptr;  // nEps x n device output
+    int32_t* nclDev = nullptr;     // nEps device output
+    bool capture = false;
+};
+
 struct sdb_engine {
     int n = 0, d = 0, device = 0;
     sdb_params prm{};
@@ -33,7 +46,7 @@ struct sdb_engine {
     DevBuf Xin, Xt, scale, P, topK, chunkMax, chunkMin, thr, cand, candCount, topM, listCount, listOff, listFill,
         members, tileOff, tileList, hubCount, hubOff, hubLists, masks, inRaw, aCount, degree, core, parent, border,
         rootFlag, labels, nClusters, scanTmp, errFlags, counters, E, Rt, signs, compCosh, dists, coreDist, nbOff,
-        nbIdx, nbDist, nbFill, hubIdx, kMask, firstMasks, Xb, queue;
+        nbIdx, nbDist, nbFill, hubIdx, kMask, firstMasks, Xb, queue, sweepLabels, sweepNcl;
 
     // results
     bool haveLabels = false, haveOptics = false, haveFit = false, lastOptics = false;
@@ -52,7 +65,9 @@ struct sdb_engine {
     std::vector<DevBuf*> all_bufs();
     sdb_status derive();
     void host_random(int seed);
-    sdb_status fit(const float* X, bool xOnDevice, float eps, int minPts, bool optics);
+    sdb_status fit(const float* X, bool xOnDevice, float eps, int minPts, bool optics,
+                   const SweepSpec* sw = nullptr);
+    sdb_status check_flags();
     sdb_status optics_stage(const sdb::CoreArgs& ca, int& launches);
 
     static float* f32(DevBuf& b) { return static_cast<float*>(b.ptr); }

@@ -227,7 +227,66 @@ template <int DIST> int launch_dist_t(const DistArgs& a, cudaStream_t st) {
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
+// eps masks and reverse counts from stored distances (eps sweeps: the
+// distances are computed once per dataset and thresholded per eps, the
+// pattern of the reference's test_sDbscan, src/sDbscan.cpp:1009-1038).
+// Same tiles as k_dist; one warp per member row, lanes over candidates.
+__global__ void k_masks_from_dists(DistArgs a) {
+    __shared__ int colCount[TN];
+    __shared__ int passTotal;
+    const int64_t t = blockIdx.x;
+    if (t >= *a.tileTotal) return;
+    const int l = a.tileList[t];
+    const int64_t ti = t - a.tileOff[l];
+    const int mt = (int)(ti / a.nct), ct = (int)(ti % a.nct);
+    const int64_t mbeg = a.listOff[l] + (int64_t)mt * TM, mend = a.listOff[l + 1];
+    const int r = l % a.nproj, side = l / a.nproj;
+    const int32_t* cand = a.topM + (size_t)r * 2 * a.m + side * a.m;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    for (int j = threadIdx.x; j < TN; j += blockDim.x) colCount[j] = 0;
+    if (threadIdx.x == 0) passTotal = 0;
+    __syncthreads();
+    int myPass = 0;
+    for (int row = warp; row < TM; row += warps) {
+        const int64_t q = mbeg + row;
+        if (q >= mend) break;
+        const int2 mb = a.members[q];
+        const int p = mb.x, slot = mb.y;
+        uint32_t half[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int col = h * 32 + lane;
+            const int c = ct * TN + col;
+            bool pass = false;
+            if (c < a.m) {
+                const int cp = __ldg(cand + c);
+                pass = cp != p && __ldg(a.dists + ((size_t)p * 2 * a.k + slot) * a.m + c) <= a.eps;
+                if (pass) {
+                    atomicAdd(&colCount[col], 1);
+                    ++myPass;
+                }
+            }
+            half[h] = __ballot_sync(0xffffffffu, pass);
+        }
+        if (lane == 0) a.masks[((size_t)p * 2 * a.k + slot) * a.W + ct] = ((uint64_t)half[1] << 32) | half[0];
+    }
+    const int wp = warp_sum(myPass);
+    if (lane == 0 && wp) atomicAdd(&passTotal, wp);
+    __syncthreads();
+    for (int j = threadIdx.x; j < TN; j += blockDim.x) {
+        const int c = ct * TN + j;
+        if (colCount[j]) atomicAdd(a.inRaw + cand[c], colCount[j]);
+    }
+    if (threadIdx.x == 0 && passTotal) atomicAdd(a.pairs, (unsigned long long)passTotal);
+}
+
 }  // namespace
+
+int launch_masks_from_dists(const DistArgs& a, cudaStream_t st) {
+    if (a.nTiles <= 0) return 0;
+    k_masks_from_dists<<<(unsigned)a.nTiles, 256, 0, st>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
 
 int dist_tile_rows() { return TM; }
 int dist_tile_cols() { return TN; }

@@ -15,7 +15,7 @@ import math
 import numpy as np
 
 __all__ = [
-    "cfg2_mnist_like_torch",
+    "cfg2_mnist_like_torch", "vmf_mixture_torch", "cfg5_batch_torch",
     "vmf_mixture", "cfg1_cosine", "cfg2_mnist_like", "cfg3_aniso_l2", "cfg4_dirichlet", "cfg5_batch",
     "CONFIGS",
 ]
@@ -166,3 +166,34 @@ def cfg2_mnist_like_torch(n: int = 1_000_000, d: int = 784, n_comp: int = 10, se
         blk[:, 0] += 1e-3
         X[s:e] = blk / blk.norm(dim=1, keepdim=True)
     return X, y
+
+
+def vmf_mixture_torch(n: int, d: int, n_clusters: int, sigma: float, noise_frac: float, seed: int,
+                      device: str = "cuda"):
+    """vmf_mixture's law drawn on the GPU with torch; (n, d) float32 tensor."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    centres = torch.randn(n_clusters, d, generator=g, device=device)
+    centres = centres / centres.norm(dim=1, keepdim=True)
+    y = torch.randint(0, n_clusters, (n,), generator=g, device=device)
+    noise = torch.rand(n, generator=g, device=device) < noise_frac
+    z = torch.randn(n, d, generator=g, device=device)
+    X = torch.where(noise[:, None], z, centres[y] + sigma * z)
+    X = X / X.norm(dim=1, keepdim=True)
+    return X.contiguous(), torch.where(noise, torch.full_like(y, -1), y)
+
+
+def cfg5_batch_torch(n_sets: int = 64, seed: int = 5007, n_lo: int = 2_000, n_hi: int = 200_000,
+                     device: str = "cuda"):
+    """cfg5_batch's sets (same sizes, dims and cluster counts, from the same
+    numpy seed) with the points drawn on the GPU."""
+    rng = np.random.default_rng(seed)
+    sets = []
+    for i in range(n_sets):
+        n = int(round(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi)))))
+        d = int(rng.choice([64, 128, 256]))
+        c = int(rng.integers(5, 41))
+        X, y = vmf_mixture_torch(n, d, c, 0.15 / math.sqrt(d), 0.05, seed * 100 + i, device=device)
+        sets.append((X, y))
+    return sets
