@@ -230,7 +230,9 @@ struct CoreArgs {
     const uint32_t* kMask;   // hubs x ceil(2D/32): bit l set when the hub meets list l (its top-k)
     uint64_t* firstMasks;    // n x 2k x W: the mask bits of each point's first occurrence of a candidate
 };
-int launch_core_dedupe(const CoreArgs& a, cudaStream_t st);
+int launch_slot_sigs(const int32_t* topM, int D, int m, const int64_t* hubOff, const int32_t* hubLists, void* sig,
+                     cudaStream_t st);
+int launch_core_dedupe(const CoreArgs& a, const void* sig, cudaStream_t st);
 // hubIdx from hubOff (a scan of hub flags into idxTmp) and the hubs' list masks.
 int launch_hub_masks(const CoreArgs& a, int32_t* hubIdx, int64_t* idxTmp, uint32_t* kMask, int64_t* scanTmp,
                      int64_t* nHubsDev, cudaStream_t st);

@@ -96,7 +96,7 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &listOff, &listFill, &members, &tileOff, &tileList, &hubCount, &hubOff, &hubLists, &masks, &inRaw,
             &aCount, &degree, &core, &parent, &border, &rootFlag, &labels, &nClusters, &scanTmp, &errFlags,
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
-            &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl};
+            &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig};
 }
 
 // ---------------------------------------------------------------------------
@@ -216,7 +216,8 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
           ensure(compCosh, sizeof(double) * std::max<size_t>(1, hostCosh.size()));
     const int maskWords = (L + 31) / 32;
     const size_t maxHubs = std::min<size_t>((size_t)n, (size_t)L * m);
-    ok &= ensure(hubIdx, sizeof(int32_t) * n) && ensure(kMask, sizeof(uint32_t) * maxHubs * maskWords);
+    ok &= ensure(hubIdx, sizeof(int32_t) * n) && ensure(kMask, sizeof(uint32_t) * maxHubs * maskWords) &&
+          ensure(sig, 16 * (size_t)L * m);
     if (rff) ok &= ensure(E, sizeof(float) * (size_t)n * ker) && ensure(Rt, sizeof(float) * hostRt.size());
     if (optics || sweep) ok &= ensure(dists, sizeof(float) * (size_t)n * 2 * k * m);
     if (optics) ok &= ensure(coreDist, sizeof(float) * n);
@@ -351,6 +352,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     L_(launch_scan_i64(i64(hubOff), i64(hubOff), (size_t)n + 1, i64(scanTmp), st));
     SDB_CK(cudaMemsetAsync(hubCount.ptr, 0, sizeof(int32_t) * n, st));
     L_(launch_hubs_scatter(ia, st));
+    L_(launch_slot_sigs(i32(topM), D, m, i64(hubOff), i32(hubLists), sig.ptr, st));
     if (!ok) return fail(SDB_ERR_CUDA, std::string("index launch failed: ") + cudaGetErrorString(cudaGetLastError()));
     if (!capture) SDB_CK(cudaEventRecord(ev[4], st));
 
@@ -442,7 +444,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         SDB_CK(cudaMemsetAsync(inRaw.ptr, 0, sizeof(int32_t) * n, st));
         L_(launch_masks_from_dists(da, st));
     }
-    L_(launch_core_dedupe(ca, st));
+    L_(launch_core_dedupe(ca, sig.ptr, st));
     L_(launch_core_finish(ca, st));
     if (!ok) return fail(SDB_ERR_CUDA, std::string("core launch failed: ") + cudaGetErrorString(cudaGetLastError()));
     if (!capture) SDB_CK(cudaEventRecord(ev[6], st));

@@ -5,8 +5,8 @@
 // its own candidates within eps (A) and every point that found it within eps
 // (B).  Here |A u B| = |A| + |B| - |A n B| is assembled without materialising
 // the lists:
-//  - |A(p)|: distinct passing candidates of p, from p's mask words, through a
-//    per-warp hash set in shared memory;
+//  - |A(p)|: distinct passing candidates of p, from p's mask words; a
+//    candidate met through several of p's lists is counted at its first list;
 //  - |B(i)|: the distance kernel added, per tile, how many members pass
 //    against candidate i (with multiplicity when a member meets i through
 //    several of its lists); here each point p removes its surplus (mult - 1)
@@ -21,10 +21,6 @@
 
 namespace sdb {
 namespace {
-
-constexpr int kEmpty = -1;
-
-__device__ __forceinline__ unsigned hash_pt(int p, unsigned mask) { return ((unsigned)p * 2654435761u) & mask; }
 
 // true iff hub point p is in one of point i's 2k candidate lists, i.e. one
 // of the top-m lists holding p is among the lists i meets through its top-k.
@@ -73,67 +69,90 @@ __global__ void k_hub_index(CoreArgs a, const int64_t* __restrict__ scanned, int
     }
 }
 
-// Per-warp working set in shared memory (see core_smem_words):
-//   keys[T], cnts[T]          open-addressing set of candidate ids (T = pow2 >= 2 * inserts)
-//   dsts[T]                   distance of each id (sOPTICS only)
-//   used[T]                   slots taken by the current point, in insertion order
-//   listMask[2D/32]           the lists holding the current point (hubs)
-struct WarpSet {
-    int* keys;
-    int* cnts;
-    float* dsts;
-    uint16_t* used;
-    uint32_t* listMask;
-    int* nUsed;
-};
+// Duplicates without hashing.  Point p meets candidate i once per list of p
+// that holds i, so with K(p) = p's 2k lists and L(i) = the top-m lists
+// holding i, i's multiplicity among p's candidates is |K(p) n L(i)|, and the
+// occurrence through list l is the first one iff no smaller list of
+// K(p) n L(i) exists.  sig[l][s] lists, for the point in slot s of list l, the
+// other lists holding it (up to three; cnt > 3 sends the test to the hub-list
+// CSR), and K(p) sits as a bit mask in shared memory while p is processed.
 
-__host__ __device__ inline int warp_set_words(int T, int maskWords, bool withDist) {
-    return 2 * T + T / 2 + maskWords + 1 + (withDist ? T : 0);
+__global__ void k_slot_sigs(const int32_t* __restrict__ topM, int D, int m, const int64_t* __restrict__ hubOff,
+                            const int32_t* __restrict__ hubLists, int4* __restrict__ sig) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= 2 * D * m) return;
+    const int l = q / m, s = q % m, r = l % D, side = l / D;
+    const int i = topM[(size_t)r * 2 * m + side * m + s];
+    int o[3] = {-1, -1, -1}, c = 0;
+    for (int64_t h = hubOff[i]; h < hubOff[i + 1]; ++h) {
+        const int lst = hubLists[h];
+        if (lst == l) continue;
+        if (c < 3) o[c] = lst;
+        ++c;
+    }
+    sig[q] = make_int4(o[0], o[1], o[2], c);
 }
 
-__device__ __forceinline__ WarpSet warp_set(int* sh, int w, int T, int maskWords, bool withDist) {
-    int* b = sh + (size_t)w * warp_set_words(T, maskWords, withDist);
-    WarpSet ws;
-    ws.keys = b;
-    ws.cnts = b + T;
-    ws.used = reinterpret_cast<uint16_t*>(b + 2 * T);
-    ws.listMask = reinterpret_cast<uint32_t*>(b + 2 * T + T / 2);
-    ws.nUsed = b + 2 * T + T / 2 + maskWords;
-    ws.dsts = withDist ? reinterpret_cast<float*>(b + 2 * T + T / 2 + maskWords + 1) : nullptr;
-    return ws;
+__device__ __forceinline__ bool has_list(const uint32_t* km, int lst) { return (km[lst >> 5] >> (lst & 31)) & 1u; }
+
+// Multiplicity and first-occurrence test of candidate i, met through list l.
+__device__ __forceinline__ void occurrence(const CoreArgs& a, const uint32_t* km, const int4* sig, int l, int s, int i,
+                                          int& mult, bool& first) {
+    const int4 g = __ldg(sig + (size_t)l * a.m + s);
+    mult = 1;
+    first = true;
+    if (g.w <= 3) {
+        if (g.w > 0 && has_list(km, g.x)) { ++mult; first &= g.x > l; }
+        if (g.w > 1 && has_list(km, g.y)) { ++mult; first &= g.y > l; }
+        if (g.w > 2 && has_list(km, g.z)) { ++mult; first &= g.z > l; }
+    } else {
+        for (int64_t h = a.hubOff[i]; h < a.hubOff[i + 1]; ++h) {
+            const int o = a.hubLists[h];
+            if (o != l && has_list(km, o)) {
+                ++mult;
+                first &= o > l;
+            }
+        }
+    }
 }
 
-// Inserts point p's candidates within eps (from its mask words) into the
-// warp's set; returns the number of distinct ids.  The 2k top-k ids and mask
-// words of p are fetched up front (two slots per lane), so the only
-// dependent loads left are the candidate ids themselves.
-__device__ int build_set(const CoreArgs& a, const WarpSet& ws, int p, unsigned tmask, uint64_t* firstOut) {
-    const unsigned l = lane_id();
+// Per-warp shared memory: K(p) mask and p's hub-list mask (2D bits each).
+__device__ __forceinline__ void set_k_mask(uint32_t* km, int l, bool on) {
+    if (on) atomicOr(km + (l >> 5), 1u << (l & 31));
+}
+
+// Visits the passing slots of point p; f(jj, l, s, i, first, mult) on lanes.
+// Writes p's first-occurrence mask words when firstOut is given.
+template <typename F>
+__device__ __forceinline__ int visit_point(const CoreArgs& a, uint32_t* km, const int4* sig, int p,
+                                           uint64_t* firstOut, F&& f) {
+    const unsigned lane = lane_id();
     const int slots = 2 * a.k;
-    int rA = 0, rB = 0;
-    uint64_t mA0 = 0, mA1 = 0, mB0 = 0, mB1 = 0;
     const unsigned long long* mk64 = reinterpret_cast<const unsigned long long*>(a.masks);
-    if ((int)l < slots) {
-        rA = __ldg(a.topK + (size_t)p * slots + l);
-        mA0 = __ldg(mk64 + ((size_t)p * slots + l) * a.W);
-        if (a.W > 1) mA1 = __ldg(mk64 + ((size_t)p * slots + l) * a.W + 1);
+    int rA = 0, rB = 0;
+    uint64_t mA0 = 0, mB0 = 0;
+    if ((int)lane < slots) {
+        rA = __ldg(a.topK + (size_t)p * slots + lane);
+        mA0 = __ldg(mk64 + ((size_t)p * slots + lane) * a.W);
     }
-    if ((int)l + 32 < slots) {
-        rB = __ldg(a.topK + (size_t)p * slots + l + 32);
-        mB0 = __ldg(mk64 + ((size_t)p * slots + l + 32) * a.W);
-        if (a.W > 1) mB1 = __ldg(mk64 + ((size_t)p * slots + l + 32) * a.W + 1);
+    if ((int)lane + 32 < slots) {
+        rB = __ldg(a.topK + (size_t)p * slots + lane + 32);
+        mB0 = __ldg(mk64 + ((size_t)p * slots + lane + 32) * a.W);
     }
-    if (l == 0) *ws.nUsed = 0;
+    const int lA = rA + ((int)lane >= a.k ? a.nproj : 0), lB = rB + ((int)lane + 32 >= a.k ? a.nproj : 0);
+    set_k_mask(km, lA, (int)lane < slots);
+    set_k_mask(km, lB, (int)lane + 32 < slots);
     __syncwarp();
+    int distinct = 0;
     for (int jj = 0; jj < slots; ++jj) {
         const int src = jj & 31;
-        const int r = __shfl_sync(0xffffffffu, jj < 32 ? rA : rB, src);
-        const int side = jj >= a.k;
+        const int l = __shfl_sync(0xffffffffu, jj < 32 ? lA : lB, src);
+        const int r = l % a.nproj, side = l / a.nproj;
         const int32_t* lst = a.topM + (size_t)r * 2 * a.m + side * a.m;
         for (int wd = 0; wd < a.W; ++wd) {
             uint64_t mk;
-            if (wd < 2) {
-                const uint64_t mine = jj < 32 ? (wd == 0 ? mA0 : mA1) : (wd == 0 ? mB0 : mB1);
+            if (wd == 0) {
+                const uint64_t mine = jj < 32 ? mA0 : mB0;
                 const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)mine, src);
                 const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(mine >> 32), src);
                 mk = ((uint64_t)hi << 32) | lo;
@@ -144,91 +163,106 @@ __device__ int build_set(const CoreArgs& a, const WarpSet& ws, int p, unsigned t
             if (mk) {
 #pragma unroll
                 for (int half = 0; half < 2; ++half) {
-                    const int bit = half * 32 + (int)l;
-                    bool isNew = false;
+                    const int bit = half * 32 + (int)lane;
+                    bool isFirst = false;
                     if ((mk >> bit) & 1ull) {
                         const int s = wd * 64 + bit;
                         const int i = __ldg(lst + s);
-                        unsigned h = hash_pt(i, tmask);
-                        while (true) {
-                            const int old = atomicCAS(&ws.keys[h], kEmpty, i);
-                            if (old == kEmpty) {
-                                ws.used[atomicAdd(ws.nUsed, 1)] = (uint16_t)h;
-                                atomicAdd(&ws.cnts[h], 1);
-                                if (ws.dsts) ws.dsts[h] = a.dists[((size_t)p * slots + jj) * a.m + s];
-                                isNew = true;
-                                break;
-                            }
-                            if (old == i) {
-                                atomicAdd(&ws.cnts[h], 1);
-                                break;
-                            }
-                            h = (h + 1) & tmask;
-                        }
+                        int mult;
+                        occurrence(a, km, sig, l, s, i, mult, isFirst);
+                        f(jj, l, s, i, isFirst, mult);
+                        distinct += isFirst ? 1 : 0;
                     }
-                    fresh[half] = __ballot_sync(0xffffffffu, isNew);
+                    fresh[half] = __ballot_sync(0xffffffffu, isFirst);
                 }
             }
-            if (firstOut && l == 0)
+            if (firstOut && lane == 0)
                 firstOut[((size_t)p * slots + jj) * a.W + wd] = ((uint64_t)fresh[1] << 32) | fresh[0];
         }
     }
     __syncwarp();
-    return *ws.nUsed;
+    if ((int)lane < slots) km[lA >> 5] = 0u;
+    if ((int)lane + 32 < slots) km[lB >> 5] = 0u;
+    __syncwarp();
+    return warp_sum(distinct);
 }
 
-// Marks, in the warp's list mask, the top-m lists holding hub point p.
-__device__ __forceinline__ void mark_lists(const CoreArgs& a, const WarpSet& ws, int64_t h0, int64_t h1,
+__device__ __forceinline__ void mark_lists(const CoreArgs& a, uint32_t* listMask, int64_t h0, int64_t h1,
                                            int maskWords) {
     const unsigned l = lane_id();
-    for (int t = (int)l; t < maskWords; t += 32) ws.listMask[t] = 0u;
+    for (int t = (int)l; t < maskWords; t += 32) listMask[t] = 0u;
     __syncwarp();
     for (int64_t h = h0 + l; h < h1; h += 32) {
         const int lst = a.hubLists[h];
-        atomicOr(&ws.listMask[lst >> 5], 1u << (lst & 31));
-    }
-    __syncwarp();
-}
-
-__device__ __forceinline__ void clear_set(const WarpSet& ws, int nd) {
-    for (int u = (int)lane_id(); u < nd; u += 32) {
-        const int h = ws.used[u];
-        ws.keys[h] = kEmpty;
-        ws.cnts[h] = 0;
+        atomicOr(&listMask[lst >> 5], 1u << (lst & 31));
     }
     __syncwarp();
 }
 
 // Persistent warps, each over points p = warp, warp + total, ...
-__global__ void k_core_dedupe(CoreArgs a, int T) {
-    extern __shared__ int sh[];
+__global__ void k_core_dedupe(CoreArgs a, const int4* __restrict__ sig) {
+    extern __shared__ uint32_t shm[];
     const int w = threadIdx.x >> 5;
-    const unsigned l = lane_id();
+    const unsigned lane = lane_id();
     const int maskWords = (2 * a.nproj + 31) / 32;
-    const WarpSet ws = warp_set(sh, w, T, maskWords, a.dists != nullptr);
-    const unsigned tmask = (unsigned)T - 1u;
-    for (int s = (int)l; s < T; s += 32) {
-        ws.keys[s] = kEmpty;
-        ws.cnts[s] = 0;
-    }
+    uint32_t* km = shm + (size_t)w * 2 * maskWords;
+    uint32_t* listMask = km + maskWords;
+    for (int t = (int)lane; t < maskWords; t += 32) km[t] = 0u;
     __syncwarp();
     const int gw = blockIdx.x * (blockDim.x >> 5) + w;
     const int nw = gridDim.x * (blockDim.x >> 5);
     for (int p = gw; p < a.n; p += nw) {
-        const int nd = build_set(a, ws, p, tmask, a.firstMasks);
         const int64_t h0 = a.hubOff[p], h1 = a.hubOff[p + 1];
         const bool hub = h1 > h0;
-        if (hub) mark_lists(a, ws, h0, h1, maskWords);
-        for (int u = (int)l; u < nd; u += 32) {
-            const int h = ws.used[u];
-            const int i = ws.keys[h];
-            int corr = ws.cnts[h] - 1;
-            if (hub && in_candidates_of(a, ws.listMask, a.hubLists + h0, (int)(h1 - h0), i)) corr += 1;
+        if (hub) mark_lists(a, listMask, h0, h1, maskWords);
+        const int nd = visit_point(a, km, sig, p, a.firstMasks, [&](int, int, int, int i, bool first, int mult) {
+            if (!first) return;
+            int corr = mult - 1;
+            if (hub && in_candidates_of(a, listMask, a.hubLists + h0, (int)(h1 - h0), i)) corr += 1;
             if (corr) atomicSub(a.inRaw + i, corr);
-        }
-        if (l == 0) a.aCount[p] = nd;
+        });
+        if (lane == 0) a.aCount[p] = nd;
+    }
+}
+
+// sOPTICS neighbour lists (src/sDbscan.cpp:1371-1372, :1404-1405, de-duplicated
+// at :1428-1431): for every point p, its distinct candidates within eps (own
+// entries, first |A(p)| slots of its row) and every point that found p within
+// eps without p finding it back (in entries, after them).  Row p starts at
+// nbOff[p] and holds degree[p] = |A(p)| + |B(p) \ A(p)| entries.
+__global__ void k_core_emit(CoreArgs a, const int4* __restrict__ sig, const int64_t* __restrict__ nbOff,
+                            int32_t* __restrict__ nbIdx, float* __restrict__ nbDist, int32_t* __restrict__ nbFill) {
+    extern __shared__ uint32_t shm[];
+    const int w = threadIdx.x >> 5;
+    const unsigned lane = lane_id();
+    const int maskWords = (2 * a.nproj + 31) / 32;
+    uint32_t* km = shm + (size_t)w * (2 * maskWords + 1);
+    uint32_t* listMask = km + maskWords;
+    int* cursor = reinterpret_cast<int*>(listMask + maskWords);  // next own-entry slot of the row
+    for (int t = (int)lane; t < maskWords; t += 32) km[t] = 0u;
+    __syncwarp();
+    const int gw = blockIdx.x * (blockDim.x >> 5) + w;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int p = gw; p < a.n; p += nw) {
+        const int64_t h0 = a.hubOff[p], h1 = a.hubOff[p + 1];
+        const bool hub = h1 > h0;
+        if (hub) mark_lists(a, listMask, h0, h1, maskWords);
+        if (lane == 0) *cursor = 0;
         __syncwarp();
-        clear_set(ws, nd);
+        const int64_t row = nbOff[p];
+        visit_point(a, km, sig, p, nullptr, [&](int jj, int, int s, int i, bool first, int) {
+            if (!first) return;
+            const float dd = a.dists[((size_t)p * 2 * a.k + jj) * a.m + s];
+            const int pos = atomicAdd(cursor, 1);
+            nbIdx[row + pos] = i;
+            nbDist[row + pos] = dd;
+            if (!(hub && in_candidates_of(a, listMask, a.hubLists + h0, (int)(h1 - h0), i))) {
+                const int q = atomicAdd(nbFill + i, 1);
+                const int64_t at = nbOff[i] + a.aCount[i] + q;
+                nbIdx[at] = p;
+                nbDist[at] = dd;
+            }
+        });
     }
 }
 
@@ -238,50 +272,6 @@ __global__ void k_core_finish(CoreArgs a) {
     const int deg = a.aCount[p] + a.inRaw[p];
     a.degree[p] = deg;
     a.core[p] = deg >= a.minPts - 1 ? 1 : 0;
-}
-
-// sOPTICS neighbour lists (src/sDbscan.cpp:1371-1372, :1404-1405, de-duplicated
-// at :1428-1431): for every point p, its distinct candidates within eps (own
-// entries, first |A(p)| slots of its row) and every point that found p within
-// eps without p finding it back (in entries, after them).  Row p starts at
-// nbOff[p] and holds degree[p] = |A(p)| + |B(p) \ A(p)| entries.
-__global__ void k_core_emit(CoreArgs a, int T, const int64_t* __restrict__ nbOff, int32_t* __restrict__ nbIdx,
-                            float* __restrict__ nbDist, int32_t* __restrict__ nbFill) {
-    extern __shared__ int sh[];
-    const int w = threadIdx.x >> 5;
-    const unsigned l = lane_id();
-    const int maskWords = (2 * a.nproj + 31) / 32;
-    const WarpSet ws = warp_set(sh, w, T, maskWords, true);
-    const unsigned tmask = (unsigned)T - 1u;
-    for (int s = (int)l; s < T; s += 32) {
-        ws.keys[s] = kEmpty;
-        ws.cnts[s] = 0;
-    }
-    __syncwarp();
-    const int gw = blockIdx.x * (blockDim.x >> 5) + w;
-    const int nw = gridDim.x * (blockDim.x >> 5);
-    for (int p = gw; p < a.n; p += nw) {
-        const int nd = build_set(a, ws, p, tmask, nullptr);
-        const int64_t h0 = a.hubOff[p], h1 = a.hubOff[p + 1];
-        const bool hub = h1 > h0;
-        if (hub) mark_lists(a, ws, h0, h1, maskWords);
-        const int64_t row = nbOff[p];
-        for (int u = (int)l; u < nd; u += 32) {
-            const int h = ws.used[u];
-            const int i = ws.keys[h];
-            const float dd = ws.dsts[h];
-            nbIdx[row + u] = i;
-            nbDist[row + u] = dd;
-            if (!(hub && in_candidates_of(a, ws.listMask, a.hubLists + h0, (int)(h1 - h0), i))) {
-                const int q = atomicAdd(nbFill + i, 1);
-                const int64_t at = nbOff[i] + a.aCount[i] + q;
-                nbIdx[at] = p;
-                nbDist[at] = dd;
-            }
-        }
-        __syncwarp();
-        clear_set(ws, nd);
-    }
 }
 
 // Core distance: the (minPts-1)-th smallest distance of a core point's row
@@ -330,32 +320,22 @@ __global__ void k_core_dist(CoreArgs a, const int64_t* __restrict__ nbOff, const
 
 }  // namespace
 
-// Table slots: a power of two above the most candidates a point can insert
-// (2km), so probing always ends; typical fill is well under half.
-int core_table_size(int k, int m) {
-    int t = 64;
-    while (t < 2 * k * m + 1) t <<= 1;
-    return t;
-}
-
-static size_t core_warp_bytes(const CoreArgs& a, int T, bool withDist) {
-    return sizeof(int) * (size_t)warp_set_words(T, (2 * a.nproj + 31) / 32, withDist);
-}
-
 static int core_grid(int n, int warps) {
     const int blocks = (n + warps - 1) / warps;
-    return std::min(blocks, 152 * 16);
+    return std::min(blocks, 152 * 8);
 }
 
-int launch_core_dedupe(const CoreArgs& a, cudaStream_t st) {
-    const int T = core_table_size(a.k, a.m);
-    const size_t perWarp = core_warp_bytes(a, T, a.dists != nullptr);
-    const int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (100 * 1024) / perWarp));
-    const size_t sm = perWarp * warps;
-    if (sm > 48 * 1024 &&
-        cudaFuncSetAttribute(k_core_dedupe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-        return -1;
-    k_core_dedupe<<<core_grid(a.n, warps), warps * 32, sm, st>>>(a, T);
+int launch_slot_sigs(const int32_t* topM, int D, int m, const int64_t* hubOff, const int32_t* hubLists, void* sig,
+                     cudaStream_t st) {
+    const int total = 2 * D * m;
+    k_slot_sigs<<<(total + 255) / 256, 256, 0, st>>>(topM, D, m, hubOff, hubLists, static_cast<int4*>(sig));
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int launch_core_dedupe(const CoreArgs& a, const void* sig, cudaStream_t st) {
+    const int warps = 8;
+    const size_t sm = sizeof(uint32_t) * 2 * ((2 * a.nproj + 31) / 32) * warps;
+    k_core_dedupe<<<core_grid(a.n, warps), warps * 32, sm, st>>>(a, static_cast<const int4*>(sig));
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
@@ -374,16 +354,12 @@ int launch_core_finish(const CoreArgs& a, cudaStream_t st) {
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
-int launch_core_emit(const CoreArgs& a, const int64_t* nbOff, int32_t* nbIdx, float* nbDist, int32_t* nbFill,
-                     cudaStream_t st) {
-    const int T = core_table_size(a.k, a.m);
-    const size_t perWarp = core_warp_bytes(a, T, true);
-    const int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (100 * 1024) / perWarp));
-    const size_t sm = perWarp * warps;
-    if (sm > 48 * 1024 &&
-        cudaFuncSetAttribute(k_core_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-        return -1;
-    k_core_emit<<<core_grid(a.n, warps), warps * 32, sm, st>>>(a, T, nbOff, nbIdx, nbDist, nbFill);
+int launch_core_emit(const CoreArgs& a, const void* sig, const int64_t* nbOff, int32_t* nbIdx, float* nbDist,
+                     int32_t* nbFill, cudaStream_t st) {
+    const int warps = 8;
+    const size_t sm = sizeof(uint32_t) * (2 * ((2 * a.nproj + 31) / 32) + 1) * warps;
+    k_core_emit<<<core_grid(a.n, warps), warps * 32, sm, st>>>(a, static_cast<const int4*>(sig), nbOff, nbIdx,
+                                                               nbDist, nbFill);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 

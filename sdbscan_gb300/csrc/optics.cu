@@ -18,8 +18,8 @@
 #include "engine_internal.h"
 
 namespace sdb {
-int launch_core_emit(const CoreArgs& a, const int64_t* nbOff, int32_t* nbIdx, float* nbDist, int32_t* nbFill,
-                     cudaStream_t st);
+int launch_core_emit(const CoreArgs& a, const void* sig, const int64_t* nbOff, int32_t* nbIdx, float* nbDist,
+                     int32_t* nbFill, cudaStream_t st);
 int launch_core_dist(const CoreArgs& a, const int64_t* nbOff, const float* nbDist, cudaStream_t st);
 int launch_i32_to_i64(const int32_t* in, int64_t* out, int n, cudaStream_t st);
 }  // namespace sdb
@@ -88,7 +88,7 @@ sdb_status sdb_engine::optics_stage(const CoreArgs& ca, int& launches) {
         return SDB_ERR_NOMEM;
     e = cudaMemsetAsync(nbFill.ptr, 0, sizeof(int32_t) * n, st);
     if (e != cudaSuccess) return cuda_fail(e, "memset");
-    r = launch_core_emit(ca, i64(nbOff), i32(nbIdx), f32(nbDist), i32(nbFill), st);
+    r = launch_core_emit(ca, sig.ptr, i64(nbOff), i32(nbIdx), f32(nbDist), i32(nbFill), st);
     if (r < 0) return fail(SDB_ERR_CUDA, "neighbour list launch failed");
     launches += r;
     r = launch_core_dist(ca, i64(nbOff), f32(nbDist), st);
