@@ -95,31 +95,42 @@ __device__ __forceinline__ uint64_t warp_sort_desc(uint64_t x) {
     return x;
 }
 
-// Top-(k+1) of the warp's nproj keys (key[j] for element l + 32 j; invalid
-// elements hold key 0 and never win against a valid element since valid keys
-// are > 0 except -NaN).  Writes the k winners in descending order to out[0..k)
-// and returns whether the k-th and (k+1)-th values tie.  `e` ties break toward
-// the smaller vector index.
-template <int NJ>
-__device__ bool warp_topk(const float (&v)[NJ], bool far, int nproj, int k, int32_t* out, uint64_t* sbuf) {
+// 32-bit warp bitonic sort, one key per lane, descending in lane order.
+__device__ __forceinline__ uint32_t warp_sort_desc_u32(uint32_t x) {
     const unsigned l = lane_id();
-    auto keyj = [&](int j) -> uint32_t {
-        const int e = (int)l + 32 * j;
-        return e < nproj ? key_of(far ? -v[j] : v[j]) : 0u;
-    };
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            const uint32_t o = __shfl_xor_sync(0xffffffffu, x, stride);
+            const bool keep_max = ((l & size) == 0) == ((l & stride) == 0);
+            x = keep_max ? max(o, x) : min(o, x);
+        }
+    }
+    return x;
+}
+
+// Top-(k+1) of the warp's keys (key[j] for element l + 32 j, 0 for elements
+// past nproj; every real key is > 0).  Writes the k winners in descending
+// order to out[0..k) and returns whether the k-th and (k+1)-th values tie.
+// Ties between equal values break toward the smaller vector index.
+//   Fast path: T = the (k+1)-th largest lane maximum is attained by k+1
+//   different elements, so every winner has key >= T; the (usually few)
+//   candidates >= T are compacted and sorted in one warp sort.
+//   Fallback (more than 32 candidates, e.g. many equal values): repeated
+//   warp argmax.
+template <int NJ>
+__device__ bool warp_topk(const uint32_t (&key)[NJ], int nproj, int k, int32_t* out, uint64_t* sbuf) {
+    const unsigned l = lane_id();
     const int want = k + 1 <= nproj ? k + 1 : k;
-    // Fast path: threshold from the lane maxima.
     if (want <= 32) {
         uint32_t lm = 0;
 #pragma unroll
-        for (int j = 0; j < NJ; ++j) lm = max(lm, keyj(j));
-        const uint64_t lmk = ((uint64_t)lm << 32) | (uint64_t)l;
-        const uint64_t sorted = warp_sort_desc(lmk);
-        const uint32_t T = (uint32_t)(__shfl_sync(0xffffffffu, sorted, want - 1) >> 32);
-        // candidates: key >= T (at least `want` of them)
+        for (int j = 0; j < NJ; ++j) lm = max(lm, key[j]);
+        const uint32_t T = __shfl_sync(0xffffffffu, warp_sort_desc_u32(lm), want - 1);
         int cnt = 0;
 #pragma unroll
-        for (int j = 0; j < NJ; ++j) cnt += (keyj(j) >= T && (l + 32 * j) < (unsigned)nproj) ? 1 : 0;
+        for (int j = 0; j < NJ; ++j) cnt += key[j] >= T ? 1 : 0;
         int incl = cnt;
 #pragma unroll
         for (int s = 1; s < 32; s <<= 1) {
@@ -130,11 +141,9 @@ __device__ bool warp_topk(const float (&v)[NJ], bool far, int nproj, int k, int3
         if (total <= 32) {
             int pos = incl - cnt;
 #pragma unroll
-            for (int j = 0; j < NJ; ++j) {
-                const int e = (int)l + 32 * j;
-                const uint32_t kj = keyj(j);
-                if (kj >= T && e < nproj) sbuf[pos++] = ((uint64_t)kj << 32) | (uint64_t)(0xffffffffu - (uint32_t)e);
-            }
+            for (int j = 0; j < NJ; ++j)
+                if (key[j] >= T)
+                    sbuf[pos++] = ((uint64_t)key[j] << 32) | (uint64_t)(0xffffffffu - (uint32_t)(l + 32 * j));
             __syncwarp();
             const uint64_t mine = (int)l < total ? sbuf[l] : 0ull;
             __syncwarp();
@@ -145,27 +154,20 @@ __device__ bool warp_topk(const float (&v)[NJ], bool far, int nproj, int k, int3
             return want > k && (uint32_t)(a >> 32) == (uint32_t)(b >> 32);
         }
     }
-    // General path: repeated warp argmax.
-    uint32_t taken[(NJ + 31) / 32];
-#pragma unroll
-    for (int w = 0; w < (NJ + 31) / 32; ++w) taken[w] = 0;
+    uint64_t taken = 0;  // bit j: element l + 32 j already selected
     uint32_t prev = 0, last = 0;
     for (int it = 0; it < want; ++it) {
         uint64_t best = 0;
 #pragma unroll
         for (int j = 0; j < NJ; ++j) {
-            const int e = (int)l + 32 * j;
-            if (e < nproj && !((taken[j >> 5] >> (j & 31)) & 1u)) {
-                const uint64_t pk = ((uint64_t)keyj(j) << 32) | (uint64_t)(0xffffffffu - (uint32_t)e);
+            if (key[j] && !((taken >> j) & 1ull)) {
+                const uint64_t pk = ((uint64_t)key[j] << 32) | (uint64_t)(0xffffffffu - (uint32_t)(l + 32 * j));
                 best = pk > best ? pk : best;
             }
         }
         best = warp_max_u64(best);
         const int e = (int)(0xffffffffu - (uint32_t)best);
-        if ((e & 31) == (int)l) {
-            const int j = e >> 5;
-            taken[j >> 5] |= 1u << (j & 31);
-        }
+        if ((e & 31) == (int)l) taken |= 1ull << (e >> 5);
         if (it < k) {
             if (l == 0) out[it] = e;
             prev = (uint32_t)(best >> 32);
@@ -343,10 +345,18 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
                 ext[e] = __hmax2(ext[e], b);
             }
         }
+        // top-k on order-preserving keys; the far side's keys are the
+        // complements (the order of -v), so one key array serves both sides
+        uint32_t key[NJ];
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) key[j] = ((int)l + 32 * j) < a.nproj ? key_of(v[j]) : 0u;
         int32_t* tk = a.topK + (size_t)p * 2 * a.k;
 #pragma unroll 1
-        for (int side = 0; side < 2; ++side)
-            localTies += warp_topk<NJ>(v, side == 1, a.nproj, a.k, tk + side * a.k, sbuf) ? 1 : 0;
+        for (int side = 0; side < 2; ++side) {
+            localTies += warp_topk<NJ>(key, a.nproj, a.k, tk + side * a.k, sbuf) ? 1 : 0;
+#pragma unroll
+            for (int j = 0; j < NJ; ++j) key[j] = key[j] ? ~key[j] : 0u;
+        }
         __syncwarp();
     }
     if (l == 0 && localTies) atomicAdd(a.ties, (unsigned long long)localTies);
