@@ -391,7 +391,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * ldb) || !ensure(queue, sizeof(uint64_t) * (size_t)qcap))
             return SDB_ERR_NOMEM;
         L_(launch_to_bf16(f32(Xt), ld, n, Xb.ptr, ldb, st));
-        const int grid = (int)std::min<int64_t>(maxTiles, 152 * 2);
+        const int grid = (int)std::min<int64_t>(maxTiles, 152 * 3);
         L_(launch_dist_tc(da, Xb.ptr, ldb, static_cast<uint64_t*>(queue.ptr), qcap, ctr + 4,
                           i32(errFlags) + 4, grid, st));
         L_(launch_recheck(da, static_cast<const uint64_t*>(queue.ptr), ctr + 4, qcap, st));

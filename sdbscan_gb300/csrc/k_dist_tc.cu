@@ -6,7 +6,8 @@
 // rows and the products accumulate in FP32 in tensor memory:
 //   - operands are staged by cp.async into shared memory in the 128-byte
 //     swizzled K-major layout the MMA reads (8-row x 128-byte atoms, 16-byte
-//     chunk c of row r stored at chunk c ^ (r & 7)), 4 stages of 64 dimensions;
+//     chunk c of row r stored at chunk c ^ (r & 7)), 3 stages of 64 dimensions
+//     (73 KB, so three CTAs share an SM);
 //   - one thread issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=64,
 //     K=16) into a 128 x 64 FP32 accumulator in TMEM, and tcgen05.commit
 //     arrives on the stage's mbarrier when the MMAs have read it;
@@ -31,7 +32,7 @@ namespace sdb {
 namespace {
 
 constexpr int TM = 128, TN = 64, TKB = 64;  // rows, candidate columns, bf16 per stage row (128 B)
-constexpr int STAGES = 4, NT = 128;
+constexpr int STAGES = 3, NT = 128;
 constexpr int A_BYTES = TM * 128, B_BYTES = TN * 128, STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr float kMargin = 0.0125f;
 constexpr uint32_t kTmemCols = 64;
@@ -110,7 +111,7 @@ __device__ __forceinline__ uint32_t sw128(int r, int c) {
     return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
 }
 
-__global__ void __launch_bounds__(NT, 1) k_dist_tc(DistArgs a, const __nv_bfloat16* __restrict__ Xb, int ldb,
+__global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat16* __restrict__ Xb, int ldb,
                                                   uint64_t* __restrict__ queue, int64_t qcap,
                                                   unsigned long long* __restrict__ qcount, int32_t* __restrict__ err,
                                                   float* __restrict__ dbgAcc) {
