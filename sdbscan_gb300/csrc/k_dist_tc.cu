@@ -16,11 +16,11 @@
 // Decision rule.  For unit vectors x, y and their BF16 roundings x', y'
 // (relative error <= 2^-8 each), |x'.y' - x.y| <= (2^-7 + 2^-16) * sum|x_i y_i|
 // <= 0.00783; FP32 accumulation of 784 exact products adds < 2^-10, and the
-// FP32 reference's own rounding < 5e-5.  A pair whose screened distance is
-// farther than kMargin = 0.0125 from eps is therefore on the same side of eps
-// as the reference's FP32 distance; every other pair goes to a queue and is
-// recomputed by k_recheck with the plain path's exact sequential FP32 dot.
-// The resulting masks are identical to the plain FP32 path's.
+// FP32 reference's own rounding < 5e-5, 0.00886 in all.  A pair whose screened
+// distance is farther than kMargin = 0.009 from eps is therefore on the same
+// side of eps as the reference's FP32 distance; every other pair goes to a
+// queue and is recomputed by k_recheck with the plain path's exact sequential
+// FP32 dot.  The resulting masks are identical to the plain FP32 path's.
 //
 // Every wait on an mbarrier is bounded; on timeout the CTA records an error,
 // stops issuing work, drains its own copies, frees its TMEM and returns.
@@ -34,7 +34,7 @@ namespace {
 constexpr int TM = 128, TN = 64, TKB = 64;  // rows, candidate columns, bf16 per stage row (128 B)
 constexpr int STAGES = 3, NT = 128;
 constexpr int A_BYTES = TM * 128, B_BYTES = TN * 128, STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr float kMargin = 0.0125f;
+constexpr float kMargin = 0.009f;
 constexpr uint32_t kTmemCols = 64;
 constexpr long long kWaitLimit = 1LL << 22;  // bounded spins on an mbarrier
 
@@ -290,32 +290,65 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
 
 // Exact FP32 re-decision of the queued pairs: the plain path's sequential
 // fmaf dot over ascending dimensions, so the decision equals k_dist's.
-__global__ void k_recheck(DistArgs a, const uint64_t* __restrict__ queue, const unsigned long long* __restrict__ qcount,
-                          int64_t qcap) {
+// Exact re-decision of the queued pairs.  A warp takes 32 queue entries, one
+// per lane.  Both rows of every pair are staged through shared memory 32
+// dimensions at a time with coalesced 128-byte row loads (the next chunk is
+// loaded into registers while the current one is consumed), and each lane runs
+// its own pair's sequential fmaf chain out of shared memory in ascending
+// dimension order: the plain path's arithmetic, so the same bits.  Dimensions
+// past d are the zero padding of Xt, and fmaf(0, 0, s) = s.
+constexpr int RC_WARPS = 4;
+
+__global__ void __launch_bounds__(RC_WARPS * 32) k_recheck(DistArgs a, const uint64_t* __restrict__ queue,
+                                                           const unsigned long long* __restrict__ qcount,
+                                                           int64_t qcap) {
+    __shared__ float tile[RC_WARPS][64][33];  // rows 0..31: the pairs' points, 32..63: their candidates
+    __shared__ const float* rows[RC_WARPS][64];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t nq = (int64_t)min((unsigned long long)qcap, *qcount);
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nq; e += (int64_t)gridDim.x * blockDim.x) {
-        const uint64_t v = queue[e];
-        const int p = (int)(v >> 32), slot = (int)((v >> 16) & 0xFFFF), col = (int)(v & 0xFFFF);
-        const int r = __ldg(a.topKmat + (size_t)p * 2 * a.k + slot);
-        const int side = slot >= a.k;
-        const int q = __ldg(a.topM + (size_t)r * 2 * a.m + side * a.m + col);
-        const float4* x = reinterpret_cast<const float4*>(a.Xt + (size_t)p * a.ld);
-        const float4* y = reinterpret_cast<const float4*>(a.Xt + (size_t)q * a.ld);
-        float s = 0.0f;
-        for (int i = 0; i < a.ld / 4; ++i) {
-            const float4 xa = __ldg(x + i), ya = __ldg(y + i);
-            s = __fmaf_rn(xa.x, ya.x, s);
-            s = __fmaf_rn(xa.y, ya.y, s);
-            s = __fmaf_rn(xa.z, ya.z, s);
-            s = __fmaf_rn(xa.w, ya.w, s);
+    const int64_t warpsTotal = (int64_t)gridDim.x * RC_WARPS;
+    for (int64_t base = ((int64_t)blockIdx.x * RC_WARPS + w) * 32; base < nq; base += warpsTotal * 32) {
+        const int64_t e = base + lane;
+        const bool valid = e < nq;
+        int p = 0, q = 0, slot = 0, col = 0;
+        if (valid) {
+            const uint64_t v = queue[e];
+            p = (int)(v >> 32);
+            slot = (int)((v >> 16) & 0xFFFF);
+            col = (int)(v & 0xFFFF);
+            const int r = __ldg(a.topKmat + (size_t)p * 2 * a.k + slot);
+            const int side = slot >= a.k;
+            q = __ldg(a.topM + (size_t)r * 2 * a.m + side * a.m + col);
         }
-        const float dist = __fsub_rn(1.0f, s);
-        if (dist <= a.eps) {
+        rows[w][lane] = a.Xt + (size_t)p * a.ld;
+        rows[w][32 + lane] = a.Xt + (size_t)q * a.ld;
+        __syncwarp();
+        float stage[64];
+#pragma unroll
+        for (int r = 0; r < 64; ++r) stage[r] = lane < a.ld ? __ldg(rows[w][r] + lane) : 0.0f;
+        float s = 0.0f;
+        for (int c = 0; c < a.ld; c += 32) {
+#pragma unroll
+            for (int r = 0; r < 64; ++r) tile[w][r][lane] = stage[r];
+            __syncwarp();
+            const int cn = c + 32 + lane;
+            if (c + 32 < a.ld) {
+#pragma unroll
+                for (int r = 0; r < 64; ++r) stage[r] = cn < a.ld ? __ldg(rows[w][r] + cn) : 0.0f;
+            }
+#pragma unroll
+            for (int t = 0; t < 32; ++t) s = __fmaf_rn(tile[w][lane][t], tile[w][32 + lane][t], s);
+            __syncwarp();
+        }
+        const bool pass = valid && __fsub_rn(1.0f, s) <= a.eps;
+        if (pass) {
             atomicOr(reinterpret_cast<unsigned long long*>(a.masks) + ((size_t)p * 2 * a.k + slot) * a.W + col / 64,
                      1ull << (col % 64));
             atomicAdd(a.inRaw + q, 1);
-            atomicAdd(a.pairs, 1ull);
         }
+        const unsigned pm = __ballot_sync(0xffffffffu, pass);
+        if (lane == 0 && pm) atomicAdd(a.pairs, (unsigned long long)__popc(pm));
+        __syncwarp();
     }
 }
 
@@ -353,7 +386,7 @@ int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, uint64_t* queue, 
 
 int launch_recheck(const DistArgs& a, const uint64_t* queue, const unsigned long long* qcount, int64_t qcap,
                    cudaStream_t st) {
-    k_recheck<<<152 * 16, 256, 0, st>>>(a, queue, qcount, qcap);
+    k_recheck<<<152 * 8, RC_WARPS * 32, 0, st>>>(a, queue, qcount, qcap);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
