@@ -34,6 +34,21 @@ WORKLOADS = {
             eps=0.15, minPts=20, seed=1007),
 }
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # nominal FP32 CUDA-core peak at max SM clock
+# DRAM bytes (read + write) of one k_dist<Cosine> launch on the 1M x 784
+# workload, from a one-pass ncu capture of
+# `python -m sdbscan_gb300.profile_fit 1000000 0` (profiles/k_dist_fp32_cfg2.md):
+# 64.44 GB read + 0.646 GB written.
+K_DIST_TRAFFIC_1M = 64.44e9 + 0.646e9
+
+
+def _peaks():
+    """Measured HBM copy GB/s and cuBLAS BF16 TFLOP/s of this GPU pool."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            m = json.load(f)
+        return m["hbm_gbs"], m["bf16_tflops_sustained"], "measured"
+    except Exception:
+        return 6800.0, 1700.0, "fallback"
 
 
 def _dist_env():
@@ -151,32 +166,104 @@ def run_reference(args, cfg):
     return 0
 
 
-def run_batched(args, local):
+def run_batched(args, local, cpu=True):
     """Config 5: 64 vMF mixtures (n log-uniform 2K..200K, d in {64,128,256}),
-    an 8-value eps sweep each (0.05 .. 0.40), minPts 20, D 1024, k 5, m 50,
-    as one CUDA graph.  Rate = sum(n) * 8 / graph time."""
+    an 8-value eps sweep each (0.05 .. 0.40), minPts 20, D 1024, k 5, m 50.
+
+    Three GPU forms of the same 512 clusterings:
+      - batched BF16+recheck: one CUDA graph of all sets' sweeps, BF16-screened distances;
+      - batched plain: the same graph with plain FP32 distances;
+      - plain fits: 512 separate fit_sDbscan calls (one per set and eps).
+    Rate = sum(n) * 8 / time.  The labels of all three forms are compared."""
+    import numpy as np
     import torch
     from sdbscan_gb300 import capi, datasets
     sets = datasets.cfg5_batch_torch(64, seed=5007, device=f"cuda:{local}")
     torch.cuda.synchronize()
     eps_list = [0.05 * (i + 1) for i in range(8)]
     ptrs = [(X.data_ptr(), X.shape[0], X.shape[1]) for X, _ in sets]
-    t0 = time.perf_counter()
-    b = capi.Batch(ptrs, eps_list, 20, device=local, n_proj=1024, topK=5, topM=50, distance="Cosine",
-                   random_seed=42)
-    setup_s = time.perf_counter() - t0
-    for _ in range(args.warmup):
-        b.run()
-    times = [b.run() for _ in range(args.steps)]
     total_n = sum(X.shape[0] for X, _ in sets)
-    ms = sum(times) / len(times)
-    ncl = [b.labels(i, 3)[1] for i in range(4)]
-    out = {"workload": "cfg5_64sets_x8eps", "value": total_n * len(eps_list) / (ms / 1e3),
-           "unit": "point-clusterings/s", "ms_per_batch": ms, "sets": len(sets), "points": total_n,
-           "eps": [round(e, 2) for e in eps_list], "launches_per_batch": 1, "graph_lanes": b.lanes(),
-           "setup_s": setup_s, "n_clusters_eps0.20_first4": ncl}
-    b.close()
+    params = dict(n_proj=1024, topK=5, topM=50, distance="Cosine", random_seed=42)
+
+    def graph(precision):
+        t0 = time.perf_counter()
+        b = capi.Batch(ptrs, eps_list, 20, device=local, precision=precision, **params)
+        setup_s = time.perf_counter() - t0
+        for _ in range(max(3, args.warmup)):
+            b.run()
+        times = [b.run() for _ in range(args.steps)]
+        labels = [[b.labels(i, j) for j in range(len(eps_list))] for i in range(len(sets))]
+        lanes = b.lanes()
+        b.close()
+        return sum(times) / len(times), setup_s, lanes, labels
+
+    bms, bsetup, blanes, blabels = graph(capi.PREC_BF16)
+    pms, psetup, planes, plabels = graph(capi.PREC_FP32)
+    bf16_identical = all(np.array_equal(blabels[i][j][0], plabels[i][j][0]) and blabels[i][j][1] == plabels[i][j][1]
+                         for i in range(len(sets)) for j in range(len(eps_list)))
+
+    # plain GPU form: one fit_sDbscan per (set, eps), device-resident input
+    engines = []
+    for X, _ in sets:
+        e = capi.Engine(X.shape[0], X.shape[1], device=local)
+        e.set_params(**params)
+        engines.append(e)
+    fits_identical = True
+    for i, ((X, _), e) in enumerate(zip(sets, engines)):  # warm-up pass, checks the labels
+        for j, eps in enumerate(eps_list):
+            e.fit_sdbscan_device(X.data_ptr(), eps, 20)
+            lab, ncl = e.labels()
+            fits_identical &= bool(np.array_equal(lab, plabels[i][j][0])) and ncl == plabels[i][j][1]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for (X, _), e in zip(sets, engines):
+        for eps in eps_list:
+            e.fit_sdbscan_device(X.data_ptr(), eps, 20)
+    torch.cuda.synchronize()
+    fits_s = time.perf_counter() - t0
+    for e in engines:
+        e.close()
+    rate = lambda sec: total_n * len(eps_list) / sec
+    out = {"workload": "cfg5_64sets_x8eps", "value": rate(bms / 1e3), "unit": "point-clusterings/s",
+           "form": "BF16+recheck, one CUDA graph", "ms_per_batch": bms, "sets": len(sets), "points": total_n,
+           "eps": [round(e, 2) for e in eps_list], "launches_per_batch": 1, "graph_lanes": blanes,
+           "setup_s": bsetup, "labels_identical_to_plain": bf16_identical,
+           "plain_graph": {"value": rate(pms / 1e3), "ms_per_batch": pms, "graph_lanes": planes, "setup_s": psetup},
+           "plain_fits": {"value": rate(fits_s), "ms_per_batch": fits_s * 1e3, "fits": len(sets) * len(eps_list),
+                          "labels_identical_to_graph": fits_identical,
+                          "form": "512 separate fit_sDbscan calls on device-resident data"},
+           "n_clusters_eps0.20_first4": [plabels[i][3][1] for i in range(4)]}
+    if cpu:
+        out["cpu_baseline"] = _cpu_batched(sets, eps_list, params)
     return out
+
+
+def _cpu_batched(sets, eps_list, params, n_sets=6):
+    """The oracle on the smallest n_sets datasets of the batch, all host
+    threads: separate fit_sDbscan calls per eps, and the reference's own
+    index-once sweep (test_sDbscan).  Rates in point-clusterings/s."""
+    from oracle.oracle import Port, build_port
+    build_port()
+    port = Port()
+    threads = os.cpu_count() or 1
+    order = sorted(range(len(sets)), key=lambda i: sets[i][0].shape[0])[:n_sets]
+    Xs = [sets[i][0].cpu().numpy() for i in order]
+    kw = dict(dist=params["distance"], n_proj=params["n_proj"], topK=params["topK"], topM=params["topM"],
+              seed=params["random_seed"], threads=threads)
+    pts = sum(X.shape[0] for X in Xs) * len(eps_list)
+    t0 = time.perf_counter()
+    for X in Xs:
+        for eps in eps_list:
+            port.fit_sdbscan(X, eps, 20, **kw)
+    fits_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for X in Xs:
+        port.fit_sdbscan_sweep(X, eps_list, 20, **kw)
+    sweep_s = time.perf_counter() - t0
+    return {"value": pts / sweep_s, "unit": "point-clusterings/s", "cores": threads, "kind": "port",
+            "form": "index-once eps sweep (test_sDbscan pattern)", "separate_fits_value": pts / fits_s,
+            "sample": f"the {n_sets} smallest datasets ({sum(X.shape[0] for X in Xs)} points) x 8 eps "
+                      f"(oracle/ restatement, OpenMP, {threads} threads; sweep {sweep_s:.1f} s, fits {fits_s:.1f} s)"}
 
 
 def run_ours(args, cfg):
@@ -248,7 +335,16 @@ def run_ours(args, cfg):
         blabels, bncl = eng.labels()
         bc = eng.counters()
         from tests._metrics import adjusted_rand_score
+        flops = 2.0 * (2 * cfg["topK"] * cfg["topM"]) * d * n
+        stage_s = bstages["distances"] / args.steps / 1e3
+        _, bf16_peak, src = _peaks()
+        broof = {"bound": "tensor", "kernel": "distance stage: k_to_bf16 + k_dist_tc + k_recheck",
+                 "achieved": flops / stage_s / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
+                 "frac": flops / stage_s / 1e12 / bf16_peak, "traffic": None,
+                 "peak_source": f"{src} bf16_tflops_sustained (timed inside the fit)",
+                 "flops_per_launch": flops, "stage_ms": stage_s * 1e3}
         bf16 = {"value": ws * n * args.steps / (bms / 1e3), "unit": "points/s", "ms_per_step": bms / args.steps,
+                "roofline": broof,
                 "ari_vs_plain": adjusted_rand_score(labels, blabels), "labels_identical": bool(np.array_equal(labels, blabels)),
                 "rechecked_pairs": bc["rechecked"], "fallbacks": bc["fallbacks"],
                 "stage_ms": {k_: v_ / args.steps for k_, v_ in bstages.items()}}
@@ -272,17 +368,26 @@ def run_ours(args, cfg):
     e2e_value = ws * n * args.steps / e2e_s
     assert np.array_equal(lab_e2e, labels), "host-input and device-input fits disagree"
 
-    batched = None if args.no_batched else run_batched(args, local)
+    batched = None if args.no_batched else run_batched(args, local, cpu=ws == 1 and not args.no_cpu)
     if rank != 0:
         return 0
     # dominant kernel: the distance stage (one k_dist launch per fit)
     dist_ms = stage_sum["distances"] / args.steps
     flops = 2.0 * (2 * cfg["topK"] * cfg["topM"]) * d * n
     achieved = flops / (dist_ms / 1e3) / 1e12
+    hbm_peak, _, src = _peaks()
+    traffic = K_DIST_TRAFFIC_1M if cfg["workload"].startswith("cfg2") else None
+    alg_bytes = n * d * 4 + 2 * cfg["n_proj"] * cfg["topM"] * d * 4  # rows of X + candidate rows, once each
     roofline = {"bound": "fp32", "kernel": "k_dist<Cosine>", "achieved": achieved, "peak": FP32_PEAK_TFLOPS,
-                "unit": "TFLOP/s", "frac": achieved / FP32_PEAK_TFLOPS, "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / FP32_PEAK_TFLOPS, "traffic": traffic,
+                "bound_note": "exact FP32 SIMT grouped GEMM (sequential fmaf per pair): bounded by the FP32 FMA "
+                              "pipe, not by HBM or the tensor cores; the BF16 leg carries the tensor roofline",
                 "peak_source": "nominal FP32 CUDA-core peak (152 SMs x 128 lanes x 2 flop x 2.07 GHz); "
                                "MEASURED_PEAKS.json has no FP32 figure",
+                "traffic_source": "ncu dram__bytes_read+write of one k_dist launch on this workload",
+                "hbm_view": {"algorithmic_bytes": alg_bytes, "achieved_gbs": alg_bytes / (dist_ms / 1e3) / 1e9,
+                             "measured_traffic_gbs": traffic / (dist_ms / 1e3) / 1e9 if traffic else None,
+                             "peak_gbs": hbm_peak, "peak_source": src},
                 "flops_per_launch": flops, "kernel_ms": dist_ms}
     stages = {k_: v_ / args.steps for k_, v_ in stage_sum.items()}
     cpu = None

@@ -76,6 +76,7 @@ class Port:
         L.orc_form_optics.restype = _i64
         L.orc_fit_sdbscan.restype = _i
         L.orc_fit_soptics.restype = _i
+        L.orc_fit_sdbscan_sweep.restype = _i
         L.orc_distance.restype = _f
 
     # RNG -------------------------------------------------------------------
@@ -185,6 +186,26 @@ class Port:
         if ncl < 0:
             raise ValueError(f"transform rejected the input (code {-ncl})")
         return labels, ncl, core, times
+
+    def fit_sdbscan_sweep(self, X, eps_list, minPts, *, dist="Cosine", n_proj=1024, topK=10, topM=50, ker=1024,
+                          sigma=1.0, L=0.4, seed=42, threads=-1):
+        """The reference's index-once sweep restated (test_sDbscan, src/sDbscan.cpp:980-1039)."""
+        X = np.ascontiguousarray(X, np.float32)
+        n, d = X.shape
+        ker = d if dist == "Cosine" else ker
+        fd = fht_dim(n_proj, ker)
+        bits = self.hd3_bits(3 * fd, seed)
+        R = self._R(dist, ker, d, sigma, seed)
+        eps = np.ascontiguousarray(eps_list, np.float32)
+        labels = np.zeros((len(eps), n), np.int32)
+        ncl = np.zeros(len(eps), np.int32)
+        times = np.zeros(5, np.float64)
+        r = self.L.orc_fit_sdbscan_sweep(_p(X), _i(n), _i(d), _i(DIST_CODES[dist]), _i(n_proj), _i(topK), _i(topM),
+                                         _i(ker), _f(L), _p(R), _p(bits), _i(fd), _p(eps), _i(len(eps)),
+                                         _i(minPts), _i(threads), _p(labels), _p(ncl), _p(times))
+        if r < 0:
+            raise ValueError(f"transform rejected the input (code {-r})")
+        return labels, ncl, times
 
     def fit_soptics(self, X, eps, minPts, *, dist="Cosine", n_proj=1024, topK=10, topM=50, ker=1024,
                     sigma=1.0, L=0.4, seed=42, threads=-1, tie_mode=1):

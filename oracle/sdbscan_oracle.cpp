@@ -534,6 +534,44 @@ int orc_fit_sdbscan(const float* X, int n, int d, int code, int nproj, int k, in
     return ncl;
 }
 
+// The reference's index-once eps sweep (test_sDbscan, src/sDbscan.cpp:980-1039):
+// transform and index once, then for each eps find the core points and form
+// the clusters.  labels: nEps x n; ncl: nEps.  times as orc_fit_sdbscan, with
+// core and cluster summed over the eps values.
+int orc_fit_sdbscan_sweep(const float* X, int n, int d, int code, int nproj, int k, int m, int ker, float L,
+                          const float* R, const uint8_t* bits, int fhtDim, const float* eps, int nEps, int minPts,
+                          int threads, int32_t* labels, int32_t* ncl, double* times) {
+    if (threads > 0) omp_set_num_threads(threads);
+    Timer tm, all;
+    std::vector<float> Xc(X, X + (size_t)n * d);
+    int err = orc_transform(Xc.data(), n, d, code);
+    if (err) return -err;
+    times[0] = tm.lap();
+    std::vector<float> P((size_t)n * nproj);
+    std::vector<int> topK((size_t)n * 2 * k), topM((size_t)nproj * 2 * m);
+    orc_project(Xc.data(), n, d, code, ker, L, R, bits, fhtDim, nproj, P.data());
+    orc_topk(P.data(), n, nproj, k, topK.data());
+    orc_topm(P.data(), n, nproj, m, topM.data());
+    std::vector<float>().swap(P);
+    times[1] = tm.lap();
+    times[2] = times[3] = 0.0;
+    std::vector<int32_t> deg(n);
+    std::vector<uint8_t> core(n);
+    for (int e = 0; e < nEps; ++e) {
+        orc_find_core(Xc.data(), n, d, code, topK.data(), k, topM.data(), m, eps[e], minPts, 0, 0, core.data(),
+                      deg.data());
+        times[2] += tm.lap();
+        std::vector<int64_t> off(n + 1);
+        std::vector<int32_t> idx(orc_neighbors_total(n));
+        orc_neighbors_export(n, off.data(), idx.data(), nullptr);
+        ncl[e] = orc_form_cluster(n, core.data(), off.data(), idx.data(), labels + (size_t)e * n);
+        orc_graph_free();
+        times[3] += tm.lap();
+    }
+    times[4] = all.lap();
+    return 0;
+}
+
 int orc_fit_soptics(const float* X, int n, int d, int code, int nproj, int k, int m, int ker, float L,
                     const float* R, const uint8_t* bits, int fhtDim, float eps, int minPts, int threads,
                     int tie_mode, int32_t* ordering, float* reach, uint8_t* core, float* coreDist, double* times) {

@@ -202,10 +202,15 @@ struct DistArgs {
     float* dists;         // n x 2k x m (optional)
     unsigned long long* pairs;  // pass counter
     const int32_t* topKmat;     // n x 2k (the re-decision kernel maps slots back to lists)
+    const int32_t* gate;        // optional: k_dist runs only if *gate != 0 (screening failed)
+    int nSweep;                 // BF16 sweep: eps values whose margins are re-decided exactly
+    float sweepEps[16];
 };
+constexpr int kMaxScreenedSweep = 16;
 int launch_dist(const DistArgs& a, cudaStream_t st);
 int launch_masks_from_dists(const DistArgs& a, cudaStream_t st);
 int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream_t st);
+int launch_screen_reset(const DistArgs& a, cudaStream_t st);
 int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, uint64_t* queue, int64_t qcap,
                    unsigned long long* qcount, int32_t* err, int grid, cudaStream_t st,
                    float* dbgAcc = nullptr);

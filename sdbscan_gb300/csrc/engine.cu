@@ -383,9 +383,17 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     da.pairs = ctr + 3;
     da.topKmat = i32(topK);
     SDB_CK(cudaMemsetAsync(inRaw.ptr, 0, sizeof(int32_t) * n, st));
-    bool screened = false;
-    if (p.precision == SDB_PREC_BF16 && p.distance == SDB_COSINE && !sweep) {
-        // BF16 tensor-core screening + exact FP32 re-decision near eps
+    // BF16 tensor-core screening + exact FP32 re-decision near eps (Cosine
+    // sDBSCAN fits and eps sweeps of up to kMaxScreenedSweep values).  The
+    // plain kernel is launched after it in every case and runs only if the
+    // screening raised its flag (queue overflow or a timed-out wait), so the
+    // stage needs no host synchronisation and can be captured in a graph.
+    if (p.precision == SDB_PREC_BF16 && p.distance == SDB_COSINE && !optics &&
+        (!sweep || sw->nEps <= kMaxScreenedSweep)) {
+        if (sweep) {
+            da.nSweep = sw->nEps;
+            for (int e = 0; e < sw->nEps; ++e) da.sweepEps[e] = sw->eps[e];
+        }
         const int ldb = (d + 63) / 64 * 64;
         const int64_t qcap = std::max<int64_t>(1 << 20, (int64_t)n * 2 * k * m / 8);
         if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * ldb) || !ensure(queue, sizeof(uint64_t) * (size_t)qcap))
@@ -395,19 +403,12 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         L_(launch_dist_tc(da, Xb.ptr, ldb, static_cast<uint64_t*>(queue.ptr), qcap, ctr + 4,
                           i32(errFlags) + 4, grid, st));
         L_(launch_recheck(da, static_cast<const uint64_t*>(queue.ptr), ctr + 4, qcap, st));
+        da.gate = i32(errFlags) + 4;
+        L_(launch_screen_reset(da, st));
         if (!ok) return fail(SDB_ERR_CUDA, std::string("tensor-core distance launch failed: ") +
                                                cudaGetErrorString(cudaGetLastError()));
-        int32_t tcErr = 0;
-        SDB_CK(cudaMemcpyAsync(&tcErr, i32(errFlags) + 4, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-        SDB_CK(cudaStreamSynchronize(st));
-        screened = tcErr == 0;
-        if (!screened) {  // queue overflow or a timed-out wait: redo this stage on the plain path
-            SDB_CK(cudaMemsetAsync(inRaw.ptr, 0, sizeof(int32_t) * n, st));
-            SDB_CK(cudaMemsetAsync(ctr + 3, 0, sizeof(unsigned long long), st));
-            fallbacks += 1;
-        }
     }
-    if (!screened) L_(launch_dist(da, st));
+    L_(launch_dist(da, st));
     if (!ok) return fail(SDB_ERR_CUDA, std::string("distance launch failed: ") + cudaGetErrorString(cudaGetLastError()));
     if (!capture) SDB_CK(cudaEventRecord(ev[5], st));
 
@@ -515,6 +516,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
 
 // Error flags the kernels raised during the last (synchronised) fit.
 sdb_status sdb_engine::check_flags() {
+    if (hostErr[4]) fallbacks += 1;  // the screened stage was redone on the plain path
     if (hostErr[0]) return fail(SDB_ERR_NEGATIVE, "X is not non-negative (Chi2/JS need nonnegative data)");
     if (hostErr[1])
         return fail(SDB_ERR_ZERO_POINT, prm.distance == SDB_COSINE ? "X has a point of zero norm (Cosine)"

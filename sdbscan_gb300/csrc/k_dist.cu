@@ -63,6 +63,7 @@ template <int DIST> __device__ __forceinline__ float finish(float acc) {
 
 template <int DIST>
 __global__ void __launch_bounds__(NT, 2) k_dist(DistArgs a) {
+    if (a.gate != nullptr && __ldg(a.gate) == 0) return;  // the BF16 screening succeeded
     extern __shared__ __align__(16) float sm[];
     float* As = sm;                                   // STAGES x TM x LDS
     float* Bs = As + STAGES * TM * LDS;               // STAGES x TN x LDS

@@ -111,6 +111,10 @@ __device__ __forceinline__ uint32_t sw128(int r, int c) {
     return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
 }
 
+// SWEEP: store the screened distance of every pair and queue the pairs near
+// any of the sweep's eps values (masks follow per eps from the distances);
+// otherwise decide against eps and write the masks.
+template <bool SWEEP>
 __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat16* __restrict__ Xb, int ldb,
                                                   uint64_t* __restrict__ queue, int64_t qcap,
                                                   unsigned long long* __restrict__ qcount, int32_t* __restrict__ err,
@@ -228,7 +232,7 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
         const int p = rowPoint[row];
         uint64_t bits = 0;
         int nPass = 0;
-#pragma unroll
+#pragma unroll 1
         for (int c16 = 0; c16 < TN / 16; ++c16) {
             float v[16];
             tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c16 * 16), v);
@@ -241,10 +245,16 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
                 const int col = c16 * 16 + j;
                 const int q = colPoint[col];
                 bool pass = false, unsure = false;
-                if (p >= 0 && q >= 0 && p != q) {
+                if (p >= 0 && q >= 0) {
                     const float dist = 1.0f - v[j];
-                    pass = dist <= a.eps - kMargin;
-                    unsure = !pass && dist <= a.eps + kMargin;
+                    if constexpr (SWEEP) {  // keep the screened distance, re-decide near any eps
+                        a.dists[((size_t)p * 2 * a.k + rowSlot[row]) * a.m + ct * TN + col] = dist;
+                        if (p != q)
+                            for (int e = 0; e < a.nSweep; ++e) unsure |= fabsf(dist - a.sweepEps[e]) <= kMargin;
+                    } else if (p != q) {
+                        pass = dist <= a.eps - kMargin;
+                        unsure = !pass && dist <= a.eps + kMargin;
+                    }
                 }
                 const unsigned um = __ballot_sync(0xffffffffu, unsure);
                 if (um) {
@@ -269,7 +279,7 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
                 if (lane == 0 && b) atomicAdd(&colCount[col], __popc(b));
             }
         }
-        if (p >= 0) a.masks[((size_t)p * 2 * a.k + rowSlot[row]) * a.W + ct] = bits;
+        if (!SWEEP && p >= 0) a.masks[((size_t)p * 2 * a.k + rowSlot[row]) * a.W + ct] = bits;
         const int wp = warp_sum(nPass);
         if (lane == 0 && wp) atomicAdd(a.pairs, (unsigned long long)wp);
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -340,7 +350,13 @@ __global__ void __launch_bounds__(RC_WARPS * 32) k_recheck(DistArgs a, const uin
             for (int t = 0; t < 32; ++t) s = __fmaf_rn(tile[w][lane][t], tile[w][32 + lane][t], s);
             __syncwarp();
         }
-        const bool pass = valid && __fsub_rn(1.0f, s) <= a.eps;
+        const float dist = __fsub_rn(1.0f, s);
+        if (a.dists != nullptr) {  // eps sweep: store the exact distance; masks follow per eps
+            if (valid) a.dists[((size_t)p * 2 * a.k + slot) * a.m + col] = dist;
+            __syncwarp();
+            continue;
+        }
+        const bool pass = valid && dist <= a.eps;
         if (pass) {
             atomicOr(reinterpret_cast<unsigned long long*>(a.masks) + ((size_t)p * 2 * a.k + slot) * a.W + col / 64,
                      1ull << (col % 64));
@@ -350,6 +366,14 @@ __global__ void __launch_bounds__(RC_WARPS * 32) k_recheck(DistArgs a, const uin
         if (lane == 0 && pm) atomicAdd(a.pairs, (unsigned long long)__popc(pm));
         __syncwarp();
     }
+}
+
+// When screening failed (queue overflow or a timed-out wait) the plain path
+// redoes the stage: clear what the screening counted.
+__global__ void k_screen_reset(DistArgs a) {
+    if (__ldg(a.gate) == 0) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) a.inRaw[i] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.pairs = 0;
 }
 
 // Xt (FP32, row stride ld) -> Xb (BF16, row stride ldb, zero padded).
@@ -378,9 +402,15 @@ int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream
 int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, uint64_t* queue, int64_t qcap,
                    unsigned long long* qcount, int32_t* err, int grid, cudaStream_t st, float* dbgAcc) {
     const size_t sm = (size_t)STAGES * STAGE_BYTES + 1024;
-    if (cudaFuncSetAttribute(k_dist_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+    auto kern = a.dists != nullptr ? k_dist_tc<true> : k_dist_tc<false>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return -1;
-    k_dist_tc<<<grid, NT, sm, st>>>(a, static_cast<const __nv_bfloat16*>(Xb), ldb, queue, qcap, qcount, err, dbgAcc);
+    kern<<<grid, NT, sm, st>>>(a, static_cast<const __nv_bfloat16*>(Xb), ldb, queue, qcap, qcount, err, dbgAcc);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int launch_screen_reset(const DistArgs& a, cudaStream_t st) {
+    k_screen_reset<<<152 * 4, 256, 0, st>>>(a);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 

@@ -260,15 +260,20 @@ def test_bf16_screening_equals_plain(gen, n, d, k, m, eps, minPts):
     assert l16[1] == l32[1]
 
 
-def test_eps_sweep_equals_separate_fits():
+@pytest.mark.parametrize("precision", [0, 1])
+def test_eps_sweep_equals_separate_fits(precision):
     """test_sDbscan's pattern (index and distances once, then per eps) gives
-    the labels of separate fit_sDbscan calls at each eps."""
+    the labels of separate plain fit_sDbscan calls at each eps, also when the
+    sweep's distances are BF16-screened (exact re-decision near every eps)."""
     from sdbscan_gb300 import capi, datasets
     X, _ = datasets.cfg2_mnist_like(8000, 196, seed=81)
     eps_list = [0.15, 0.2, 0.25, 0.3]
     eng = capi.Engine(*X.shape)
-    eng.set_params(n_proj=512, topK=8, topM=40, distance="Cosine", random_seed=19)
+    eng.set_params(n_proj=512, topK=8, topM=40, distance="Cosine", random_seed=19, precision=precision)
     labels, ncl = eng.fit_sdbscan_sweep(X, eps_list, 20)
+    if precision:
+        assert eng.counters()["rechecked"] > 0 and eng.counters()["fallbacks"] == 0
+    eng.set_params(n_proj=512, topK=8, topM=40, distance="Cosine", random_seed=19)
     for i, e in enumerate(eps_list):
         eng.fit_sdbscan(X, e, 20)
         l1, n1 = eng.labels()
@@ -276,14 +281,17 @@ def test_eps_sweep_equals_separate_fits():
         assert ncl[i] == n1
 
 
-def test_batch_graph_equals_sweeps():
-    """The CUDA-graph batch gives, for every set and eps, the sweep's labels."""
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_graph_equals_sweeps(precision):
+    """The CUDA-graph batch gives, for every set and eps, the plain sweep's
+    labels, with plain or BF16-screened distances."""
     import torch
     from sdbscan_gb300 import capi, datasets
     sets = datasets.cfg5_batch_torch(n_sets=5, seed=91, n_lo=2000, n_hi=12000)
     eps_list = [0.05, 0.1, 0.2, 0.3]
     ptrs = [(X.data_ptr(), X.shape[0], X.shape[1]) for X, _ in sets]
-    b = capi.Batch(ptrs, eps_list, 20, n_proj=1024, topK=5, topM=50, distance="Cosine", random_seed=23)
+    b = capi.Batch(ptrs, eps_list, 20, n_proj=1024, topK=5, topM=50, distance="Cosine", random_seed=23,
+                   precision=precision)
     b.run()
     b.run()
     for i, (X, _) in enumerate(sets):

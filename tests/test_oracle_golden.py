@@ -90,3 +90,16 @@ def test_transform_rejects_like_reference(port):
     Xz = X.copy()
     Xz[5] = 0
     assert port.transform(Xz, "JS")[1] == 2
+
+
+def test_oracle_sweep_equals_separate_fits(port):
+    """The index-once eps sweep (test_sDbscan, src/sDbscan.cpp:980-1039) gives
+    each eps the labels of a separate fit_sDbscan."""
+    from sdbscan_gb300 import datasets
+    X, _ = datasets.cfg2_mnist_like(3000, 64, seed=3)
+    eps = [0.15, 0.25, 0.35]
+    labels, ncl, _ = port.fit_sdbscan_sweep(X, eps, 20, n_proj=256, topK=5, topM=30, seed=4)
+    for i, e in enumerate(eps):
+        l1, n1, _, _ = port.fit_sdbscan(X, e, 20, n_proj=256, topK=5, topM=30, seed=4)
+        np.testing.assert_array_equal(labels[i], l1)
+        assert ncl[i] == n1
