@@ -248,6 +248,14 @@ struct ClusterArgs {
     const uint64_t* masks;   // first-occurrence masks: each distinct candidate once per point
     const int32_t* topK;
     const int32_t* topM;
+    // the distance stage's tiles (list l, 128 member rows, 64 candidate columns)
+    const int2* members;
+    const int64_t* listOff;
+    const int32_t* tileList;
+    const int64_t* tileOff;
+    const int64_t* tileTotal;  // device: actual number of tiles
+    int64_t nTiles;            // launch grid (an upper bound)
+    int TM, nct, nproj;
     const uint8_t* core;
     int32_t* parent;
     int32_t* border;

@@ -460,6 +460,15 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         ka.masks = static_cast<const uint64_t*>(firstMasks.ptr);
         ka.topK = i32(topK);
         ka.topM = i32(topM);
+        ka.members = static_cast<const int2*>(members.ptr);
+        ka.listOff = i64(listOff);
+        ka.tileList = i32(tileList);
+        ka.tileOff = i64(tileOff);
+        ka.tileTotal = i64(tileOff) + L;
+        ka.nTiles = maxTiles;
+        ka.TM = TMr;
+        ka.nct = nct;
+        ka.nproj = D;
         ka.core = static_cast<const uint8_t*>(core.ptr);
         ka.parent = i32(parent);
         ka.border = i32(border);

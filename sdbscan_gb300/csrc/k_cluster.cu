@@ -53,23 +53,66 @@ __global__ void k_init(int32_t* parent, int32_t* border, int n) {
     border[p] = INT_MAX;
 }
 
-template <typename F>
-__device__ __forceinline__ void for_passing(const ClusterArgs& a, int p, F&& f) {
-    for_each_passing(a.topK, a.topM, a.masks, a.k, a.m, a.W, p, f);
+// A tile of the distance stage: list l's member rows [mbeg, mend) against its
+// candidate columns [64 ct, 64 ct + 64) (mask word ct).
+struct Tile {
+    int64_t mbeg, mend;
+    int ct;
+    const int32_t* cand;
+};
+
+__device__ __forceinline__ bool tile_of(const ClusterArgs& a, int64_t t, Tile& tl) {
+    if (t >= *a.tileTotal) return false;
+    const int l = a.tileList[t];
+    const int64_t ti = t - a.tileOff[l];
+    const int mt = (int)(ti / a.nct);
+    tl.ct = (int)(ti % a.nct);
+    tl.mbeg = a.listOff[l] + (int64_t)mt * a.TM;
+    tl.mend = min(tl.mbeg + a.TM, a.listOff[l + 1]);
+    const int r = l % a.nproj, side = l / a.nproj;
+    tl.cand = a.topM + (size_t)r * 2 * a.m + side * a.m;
+    return true;
 }
 
-__global__ void k_union(ClusterArgs a) {
-    const int warps = blockDim.x >> 5;
-    const int p = blockIdx.x * warps + (threadIdx.x >> 5);
-    if (p >= a.n || !a.core[p]) return;
+// Union over the core-core edges of one tile.  The roots of the tile's core
+// candidates are found once and cached in shared memory; a member row then
+// compares its own root with the cached roots of its passing candidates and
+// unites only where they differ.  A cached value is always an ancestor of its
+// candidate (parents only move up), so equality proves the same set; a stale
+// value only costs a redundant unite.
+__global__ void __launch_bounds__(128) k_union_tiles(ClusterArgs a) {
+    __shared__ int croot[64];
+    Tile tl;
+    if (!tile_of(a, blockIdx.x, tl)) return;
+    volatile int* vroot = croot;
+    if (threadIdx.x < 64) {
+        const int c = tl.ct * 64 + threadIdx.x;
+        int root = -1;
+        if (c < a.m) {
+            const int q = __ldg(tl.cand + c);
+            if (a.core[q]) root = find_root(a.parent, q);
+        }
+        croot[threadIdx.x] = root;
+    }
+    __syncthreads();
+    const int64_t row = tl.mbeg + threadIdx.x;
+    if (row >= tl.mend) return;
+    const int2 mb = __ldg(a.members + row);
+    const int p = mb.x;
+    if (!a.core[p]) return;
+    uint64_t bits = __ldg(reinterpret_cast<const unsigned long long*>(a.masks) +
+                          ((size_t)p * 2 * a.k + mb.y) * a.W + tl.ct);
+    if (!bits) return;
     int rp = find_root(a.parent, p);
-    for_passing(a, p, [&](int i) {
-        if (!a.core[i]) return;
-        const int pi = load_parent(a.parent, i);
-        if (pi == rp || load_parent(a.parent, pi) == rp) return;  // already joined (common case)
-        unite(a.parent, rp, i);
+    while (bits) {
+        const int j = __ffsll((long long)bits) - 1;
+        bits &= bits - 1;
+        const int cr = vroot[j];
+        if (cr < 0 || cr == rp) continue;
+        unite(a.parent, rp, cr);
         rp = find_root(a.parent, rp);
-    });
+        vroot[j] = rp;
+    }
 }
 
 __global__ void k_compress(ClusterArgs a) {
@@ -78,24 +121,49 @@ __global__ void k_compress(ClusterArgs a) {
     if (a.core[p]) a.parent[p] = find_root(a.parent, p);
 }
 
-__global__ void k_border(ClusterArgs a) {
-    const int warps = blockDim.x >> 5;
-    const int p = blockIdx.x * warps + (threadIdx.x >> 5);
-    if (p >= a.n) return;
-    if (a.core[p]) {
-        const int rp = a.parent[p];
-        for_passing(a, p, [&](int i) {
-            if (!a.core[i]) atomicMin(a.border + i, rp);
-        });
-    } else {
-        int best = INT_MAX;
-        for_passing(a, p, [&](int i) {
-            if (a.core[i]) best = min(best, __ldcg(a.parent + i));
-        });
-#pragma unroll
-        for (int m = 16; m >= 1; m >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, m));
-        if (lane_id() == 0 && best != INT_MAX) atomicMin(a.border + p, best);
+// Border labels of one tile (parents are roots after k_compress).  A non-core
+// member takes the smallest root among its passing core candidates; a non-core
+// candidate takes the smallest root among the core members passing with it,
+// reduced in shared memory first so each candidate sees one global atomic.
+__global__ void __launch_bounds__(128) k_border_tiles(ClusterArgs a) {
+    __shared__ int croot[64], cbest[64], cpt[64];
+    Tile tl;
+    if (!tile_of(a, blockIdx.x, tl)) return;
+    if (threadIdx.x < 64) {
+        const int c = tl.ct * 64 + threadIdx.x;
+        const int q = c < a.m ? __ldg(tl.cand + c) : -1;
+        cpt[threadIdx.x] = q;
+        croot[threadIdx.x] = (q >= 0 && a.core[q]) ? __ldcg(a.parent + q) : INT_MAX;
+        cbest[threadIdx.x] = INT_MAX;
     }
+    __syncthreads();
+    const int64_t row = tl.mbeg + threadIdx.x;
+    if (row < tl.mend) {
+        const int2 mb = __ldg(a.members + row);
+        const int p = mb.x;
+        uint64_t bits = __ldg(reinterpret_cast<const unsigned long long*>(a.masks) +
+                              ((size_t)p * 2 * a.k + mb.y) * a.W + tl.ct);
+        if (bits) {
+            if (a.core[p]) {
+                const int rp = __ldcg(a.parent + p);
+                while (bits) {
+                    const int j = __ffsll((long long)bits) - 1;
+                    bits &= bits - 1;
+                    if (croot[j] == INT_MAX) atomicMin(&cbest[j], rp);
+                }
+            } else {
+                int best = INT_MAX;
+                while (bits) {
+                    const int j = __ffsll((long long)bits) - 1;
+                    bits &= bits - 1;
+                    best = min(best, croot[j]);
+                }
+                if (best != INT_MAX) atomicMin(a.border + p, best);
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 64 && cbest[threadIdx.x] != INT_MAX) atomicMin(a.border + cpt[threadIdx.x], cbest[threadIdx.x]);
 }
 
 __global__ void k_root_flags(ClusterArgs a) {
@@ -124,12 +192,11 @@ int launch_cluster(const ClusterArgs& a, cudaStream_t st) {
     const int g = (a.n + 255) / 256;
     k_init<<<g, 256, 0, st>>>(a.parent, a.border, a.n);
     ++launches;
-    const int wg = (a.n + 7) / 8;
-    k_union<<<wg, 256, 0, st>>>(a);
+    k_union_tiles<<<(unsigned)a.nTiles, 128, 0, st>>>(a);
     ++launches;
     k_compress<<<g, 256, 0, st>>>(a);
     ++launches;
-    k_border<<<wg, 256, 0, st>>>(a);
+    k_border_tiles<<<(unsigned)a.nTiles, 128, 0, st>>>(a);
     ++launches;
     k_root_flags<<<(a.n + 1 + 255) / 256, 256, 0, st>>>(a);
     ++launches;

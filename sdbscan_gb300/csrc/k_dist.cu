@@ -22,7 +22,13 @@
 namespace sdb {
 namespace {
 
-constexpr int TM = 128, TN = 64, TK = 32, LDS = TK + 4, STAGES = 3, NT = 256;
+// Tile rows, dimensions per stage, smem row stride, stages.  The candidate
+// columns per tile are TX * CN (TX column groups of CN columns, 16 row groups
+// of 8 rows): <16, 4> gives 64 columns on 256 threads (any m, one 64-bit mask
+// word per tile) and <10, 5> exactly 50 columns on 160 threads (m in 41..50,
+// no padded columns).
+constexpr int TM = 128, TK = 32, LDS = TK + 4, STAGES = 3;
+constexpr int TN = 64;  // the tile grid's candidate columns (and mask bits) per tile
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -61,17 +67,18 @@ template <int DIST> __device__ __forceinline__ float finish(float acc) {
     return __fsub_rn(1.0f, __fmul_rn(acc, 0.5f));                    // == (float)(1.0 - t/2.0), exact
 }
 
-template <int DIST>
-__global__ void __launch_bounds__(NT, 2) k_dist(DistArgs a) {
+template <int DIST, int TX, int CN>
+__global__ void __launch_bounds__(16 * TX, 2) k_dist(DistArgs a) {
+    constexpr int NT = 16 * TX, TNK = TX * CN;  // threads, candidate columns this kernel computes
     if (a.gate != nullptr && __ldg(a.gate) == 0) return;  // the BF16 screening succeeded
     extern __shared__ __align__(16) float sm[];
     float* As = sm;                                   // STAGES x TM x LDS
-    float* Bs = As + STAGES * TM * LDS;               // STAGES x TN x LDS
-    int* rowPoint = reinterpret_cast<int*>(Bs + STAGES * TN * LDS);
+    float* Bs = As + STAGES * TM * LDS;               // STAGES x TNK x LDS
+    int* rowPoint = reinterpret_cast<int*>(Bs + STAGES * TNK * LDS);
     int* rowSlot = rowPoint + TM;
     int* colPoint = rowSlot + TM;
-    unsigned* smask = reinterpret_cast<unsigned*>(colPoint + TN);  // TM x 2
-    int* colCount = reinterpret_cast<int*>(smask + 2 * TM);          // TN
+    unsigned* smask = reinterpret_cast<unsigned*>(colPoint + TNK);  // TM x 2
+    int* colCount = reinterpret_cast<int*>(smask + 2 * TM);           // TNK
     __shared__ int passTotal;
 
     const int tid = threadIdx.x;
@@ -98,7 +105,7 @@ __global__ void __launch_bounds__(NT, 2) k_dist(DistArgs a) {
         smask[2 * i] = 0;
         smask[2 * i + 1] = 0;
     }
-    for (int j = tid; j < TN; j += NT) {
+    for (int j = tid; j < TNK; j += NT) {
         const int c = ct * TN + j;
         colPoint[j] = c < a.m ? cand[c] : -1;
         colCount[j] = 0;
@@ -109,11 +116,10 @@ __global__ void __launch_bounds__(NT, 2) k_dist(DistArgs a) {
     const int nk = (a.d + TK - 1) / TK;
     auto load_stage = [&](int stage, int kc) {
         float* as = As + stage * TM * LDS;
-        float* bs = Bs + stage * TN * LDS;
+        float* bs = Bs + stage * TNK * LDS;
         const int k0 = kc * TK;
 #pragma unroll
-        for (int it = 0; it < (TM * TK / 4) / NT; ++it) {  // 4 per thread
-            const int idx = tid + it * NT;
+        for (int idx = tid; idx < TM * TK / 4; idx += NT) {
             const int row = idx >> 3, c4 = idx & 7;
             const int p = rowPoint[row];
             const int col = k0 + c4 * 4;
@@ -122,8 +128,7 @@ __global__ void __launch_bounds__(NT, 2) k_dist(DistArgs a) {
             cp_async16(as + row * LDS + c4 * 4, src, ok);
         }
 #pragma unroll
-        for (int it = 0; it < (TN * TK / 4) / NT; ++it) {  // 2 per thread
-            const int idx = tid + it * NT;
+        for (int idx = tid; idx < TNK * TK / 4; idx += NT) {
             const int row = idx >> 3, c4 = idx & 7;
             const int p = colPoint[row];
             const int col = k0 + c4 * 4;
@@ -133,13 +138,13 @@ __global__ void __launch_bounds__(NT, 2) k_dist(DistArgs a) {
         }
     };
 
-    float acc[8][4];
+    float acc[8][CN];
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+        for (int j = 0; j < CN; ++j) acc[i][j] = 0.0f;
 
-    const int ty = tid >> 4, tx = tid & 15;
+    const int ty = tid / TX, tx = tid % TX;
 #pragma unroll
     for (int s = 0; s < STAGES - 1; ++s) {
         if (s < nk) load_stage(s, s);
@@ -152,18 +157,18 @@ __global__ void __launch_bounds__(NT, 2) k_dist(DistArgs a) {
         if (nxt < nk) load_stage(nxt % STAGES, nxt);
         cp_async_commit();
         const float* as = As + (kc % STAGES) * TM * LDS;
-        const float* bs = Bs + (kc % STAGES) * TN * LDS;
+        const float* bs = Bs + (kc % STAGES) * TNK * LDS;
 #pragma unroll
         for (int kk = 0; kk < TK; kk += 4) {
-            float4 av[8], bv[4];
+            float4 av[8], bv[CN];
 #pragma unroll
             for (int i = 0; i < 8; ++i) av[i] = *reinterpret_cast<const float4*>(as + (ty + 16 * i) * LDS + kk);
 #pragma unroll
-            for (int j = 0; j < 4; ++j) bv[j] = *reinterpret_cast<const float4*>(bs + (tx + 16 * j) * LDS + kk);
+            for (int j = 0; j < CN; ++j) bv[j] = *reinterpret_cast<const float4*>(bs + (tx + TX * j) * LDS + kk);
 #pragma unroll
             for (int i = 0; i < 8; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
+                for (int j = 0; j < CN; ++j) {
                     float c = acc[i][j];
                     c = acc_step<DIST>(c, av[i].x, bv[j].x);
                     c = acc_step<DIST>(c, av[i].y, bv[j].y);
@@ -177,15 +182,17 @@ __global__ void __launch_bounds__(NT, 2) k_dist(DistArgs a) {
 
     // epilogue
     int myPass = 0;
-    int colPass[4] = {0, 0, 0, 0};
+    int colPass[CN];
+#pragma unroll
+    for (int j = 0; j < CN; ++j) colPass[j] = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const int row = ty + 16 * i;
         const int p = rowPoint[row];
         unsigned lo = 0, hi = 0;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int col = tx + 16 * j;
+        for (int j = 0; j < CN; ++j) {
+            const int col = tx + TX * j;
             const int q = colPoint[col];
             const float dist = finish<DIST>(acc[i][j]);
             const bool pass = p >= 0 && q >= 0 && p != q && dist <= a.eps;
@@ -202,8 +209,8 @@ __global__ void __launch_bounds__(NT, 2) k_dist(DistArgs a) {
         if (hi) atomicOr(&smask[2 * row + 1], hi);
     }
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
-        if (colPass[j]) atomicAdd(&colCount[tx + 16 * j], colPass[j]);
+    for (int j = 0; j < CN; ++j)
+        if (colPass[j]) atomicAdd(&colCount[tx + TX * j], colPass[j]);
     const int wp = warp_sum(myPass);
     if ((tid & 31) == 0 && wp) atomicAdd(&passTotal, wp);
     __syncthreads();
@@ -214,18 +221,25 @@ __global__ void __launch_bounds__(NT, 2) k_dist(DistArgs a) {
             a.masks[((size_t)p * 2 * a.k + rowSlot[row]) * a.W + ct] = w;
         }
     }
-    for (int j = tid; j < TN; j += NT)
+    for (int j = tid; j < TNK; j += NT)
         if (colCount[j]) atomicAdd(a.inRaw + colPoint[j], colCount[j]);
     if (tid == 0 && passTotal) atomicAdd(a.pairs, (unsigned long long)passTotal);
 }
 
-template <int DIST> int launch_dist_t(const DistArgs& a, cudaStream_t st) {
-    const size_t sm = sizeof(float) * (STAGES * (TM + TN) * LDS) + sizeof(int) * (3 * TM + 2 * TN + 2 * TM);
-    if (cudaFuncSetAttribute(k_dist<DIST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+template <int DIST, int TX, int CN> int launch_dist_v(const DistArgs& a, cudaStream_t st) {
+    constexpr int TNK = TX * CN;
+    const size_t sm = sizeof(float) * (STAGES * (TM + TNK) * LDS) + sizeof(int) * (3 * TM + 2 * TNK + 2 * TM);
+    if (cudaFuncSetAttribute(k_dist<DIST, TX, CN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+        cudaSuccess)
         return -1;
     if (a.nTiles <= 0) return 0;
-    k_dist<DIST><<<(unsigned)a.nTiles, NT, sm, st>>>(a);
+    k_dist<DIST, TX, CN><<<(unsigned)a.nTiles, 16 * TX, sm, st>>>(a);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+template <int DIST> int launch_dist_t(const DistArgs& a, cudaStream_t st) {
+    if (a.m > 40 && a.m <= 50) return launch_dist_v<DIST, 10, 5>(a, st);  // exact 50-column tiles
+    return launch_dist_v<DIST, 16, 4>(a, st);
 }
 
 // eps masks and reverse counts from stored distances (eps sweeps: the
