@@ -184,7 +184,10 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     const int nct = (m + TNc - 1) / TNc;
     const int W = (m + 63) / 64;
     const int L = 2 * D;
-    const int chunk = std::max(8, (n + std::max(1024, 4 * m) - 1) / std::max(1024, 4 * m));
+    // projection blocks = top-m threshold chunks: one full wave of 4 blocks per
+    // SM, and at least 4m chunks so the chunk maxima bound the m-th value
+    const int chunksWanted = std::max(152 * 4, 4 * m);
+    const int chunk = std::max(8, (n + chunksWanted - 1) / chunksWanted);
     const int G = (n + chunk - 1) / chunk;
     int cap = 256;
     while (cap < 8 * m) cap <<= 1;

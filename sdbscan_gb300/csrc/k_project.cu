@@ -22,6 +22,15 @@
 namespace sdb {
 namespace {
 
+__device__ __forceinline__ void cp_async16(float* dst, const float* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src));
+}
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src));
+}
+
 // One thread per point: Cosine norm (sequential fmaf of squares) or Chi2/JS
 // column sum (sequential adds), plus the reference's input checks
 // (src/Utilities.h:308-324) and a finiteness check.  The CTA's 256 rows are
@@ -193,6 +202,23 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
     float* rowbuf = base + w * rowLen;                                // per-warp copy of the row (Chi2/JS)
     // per-warp running (max v, max -v) per vector, bf16x2 rounded toward -inf
     __nv_bfloat162* ext = reinterpret_cast<__nv_bfloat162*>(base + warps * rowLen) + (size_t)w * a.nproj;
+    // per-warp double buffer of input rows: the next point's row is fetched
+    // with cp.async while the current one is transformed
+    const int xs = (a.d + 3) & ~3;
+    float* xbuf = base + warps * rowLen + warps * a.nproj + (size_t)w * 2 * xs;
+    const bool vec16 = (a.ldx & 3) == 0 && (reinterpret_cast<uintptr_t>(a.X) & 15) == 0;
+    auto fetch = [&](int pp, int b) {
+        if (pp < min(a.n, (int)(blockIdx.x + 1) * a.chunk)) {
+            const float* src = a.X + (size_t)pp * a.ldx;
+            float* dst = xbuf + b * xs;
+            if (vec16) {
+                for (int c = (int)l; c < a.d / 4; c += 32) cp_async16(dst + 4 * c, src + 4 * c);
+            } else {
+                for (int e = (int)l; e < a.d; e += 32) cp_async4(dst + e, src + e);
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::);
+    };
     for (int i = threadIdx.x; i < nsw; i += blockDim.x) sw[i] = a.signs[i];
     __syncthreads();
     // Lane l's sign bits for its elements e = l + 32 j, one 32-bit mask per
@@ -216,9 +242,14 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
     const int p0 = blockIdx.x * a.chunk;
     const int p1 = min(a.n, p0 + a.chunk);
     int localTies = 0;
-    for (int p = p0 + w; p < p1; p += warps) {
-        const float* x = a.X + (size_t)p * a.ldx;
+    int buf = 0;
+    fetch(p0 + w, 0);
+    for (int p = p0 + w; p < p1; p += warps, buf ^= 1) {
+        fetch(p + warps, buf ^ 1);
         const float sc = scale[p];
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        __syncwarp();
+        const float* x = xbuf + buf * xs;  // this point's input row, in shared memory
         // transformed row -> Xt (zero padded to ld)
         float v[NJ];
         if (EMB == 0) {
@@ -227,20 +258,20 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
             for (int j = 0; j < NJ; ++j) {
                 const int e = (int)l + 32 * j;
                 float t = 0.0f;
-                if (e < a.d) t = a.do_transform ? __fdiv_rn(__ldg(x + e), sc) : __ldg(x + e);
+                if (e < a.d) t = a.do_transform ? __fdiv_rn(x[e], sc) : x[e];
                 if (e < a.ld) a.Xt[(size_t)p * a.ld + e] = t;
                 v[j] = t;
             }
             for (int e = (int)l + 32 * NJ; e < a.ld; e += 32) {
                 float t = 0.0f;
-                if (e < a.d) t = a.do_transform ? __fdiv_rn(__ldg(x + e), sc) : __ldg(x + e);
+                if (e < a.d) t = a.do_transform ? __fdiv_rn(x[e], sc) : x[e];
                 a.Xt[(size_t)p * a.ld + e] = t;
             }
         }
         for (int i = (int)l; EMB != 0 && i < a.ld; i += 32) {
             float t = 0.0f;
             if (i < a.d) {
-                t = __ldg(x + i);
+                t = x[i];
                 if (a.do_transform && EMB != 1) t = __fdiv_rn(t, sc);
             }
             a.Xt[(size_t)p * a.ld + i] = t;
@@ -359,6 +390,7 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
         }
         __syncwarp();
     }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     if (l == 0 && localTies) atomicAdd(a.ties, (unsigned long long)localTies);
     // chunk extremes: reduce the warps' rows
     __syncthreads();
@@ -377,7 +409,9 @@ int launch_project_nje(const ProjectArgs& a, const float* scale, cudaStream_t st
     const int G = (a.n + a.chunk - 1) / a.chunk;
     const int nsw = (3 * a.fhtDim + 31) / 32;
     const int rowLen = EMB == 2 ? ((a.d + 3) & ~3) + a.fhtDim : 0;
-    size_t sm = sizeof(float) * (warps * 64 + ((nsw + 3) & ~3) + (size_t)warps * rowLen + (size_t)warps * a.nproj);
+    const size_t xs = (size_t)((a.d + 3) & ~3);
+    size_t sm = sizeof(float) * (warps * 64 + ((nsw + 3) & ~3) + (size_t)warps * rowLen + (size_t)warps * a.nproj +
+                                 (size_t)warps * 2 * xs);
     if (sm > 227 * 1024) return -1;
     if (sm > 48 * 1024) {
         if (cudaFuncSetAttribute(k_project<NJ, EMB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
