@@ -122,6 +122,7 @@ struct ProjectArgs {
     float* chunkMax;     // G x nproj
     float* chunkMin;     // G x nproj
     int chunk;           // points per chunk (G = ceil(n / chunk))
+    int chunkBase, chunkEnd;  // chunks this launch covers (chunkEnd 0: all G)
     int32_t* err;        // device flags: [0] negative input, [1] zero point
     unsigned long long* ties;  // top-k boundary tie counter
     int do_transform;    // 1: apply transformData; 0: X already transformed

@@ -184,9 +184,10 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     const int nct = (m + TNc - 1) / TNc;
     const int W = (m + 63) / 64;
     const int L = 2 * D;
-    // projection blocks = top-m threshold chunks: one full wave of 4 blocks per
-    // SM, and at least 4m chunks so the chunk maxima bound the m-th value
-    const int chunksWanted = std::max(152 * 4, 4 * m);
+    // top-m threshold chunks: a full wave of projection blocks (4 per SM) for
+    // each upload segment, and at least 4m chunks so the chunk maxima bound
+    // the m-th value
+    const int chunksWanted = std::max(152 * 4 * kUploadSegs, 4 * m);
     const int chunk = std::max(8, (n + chunksWanted - 1) / chunksWanted);
     const int G = (n + chunk - 1) / chunk;
     int cap = 256;
@@ -240,9 +241,13 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
 
     if (!capture) SDB_CK(cudaEventRecord(ev[0], st));
     const float* Xd = X;
+    // host input without an embedding GEMM: the upload runs in segments on the
+    // copy stream and overlaps stage 1 (the "upload" stage time then reads 0)
+    const bool overlapUpload = !xOnDevice && !rff && !capture;
     if (!xOnDevice) {
-        SDB_CK(cudaMemcpyAsync(Xin.ptr, X, sizeof(float) * (size_t)n * d, cudaMemcpyHostToDevice, st));
         Xd = static_cast<const float*>(Xin.ptr);
+        if (!overlapUpload)
+            SDB_CK(cudaMemcpyAsync(Xin.ptr, X, sizeof(float) * (size_t)n * d, cudaMemcpyHostToDevice, st));
     }
     if (!capture) SDB_CK(cudaEventRecord(ev[1], st));
     if (!capture) {  // a captured sweep reuses the signs its sizing run uploaded
@@ -293,7 +298,25 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         pa.E = f32(E);
         pa.do_transform = 0;
     }
-    L_(launch_project(pa, st));
+    if (overlapUpload) {
+        const int segs = std::min(kUploadSegs, G);
+        SDB_CK(cudaEventRecord(segEv[kUploadSegs], st));  // Xin is free once the stream got here
+        SDB_CK(cudaStreamWaitEvent(copyStream, segEv[kUploadSegs], 0));
+        for (int sgi = 0; sgi < segs; ++sgi) {
+            const int cb = (int)((int64_t)G * sgi / segs), ce = (int)((int64_t)G * (sgi + 1) / segs);
+            const size_t pb = (size_t)cb * chunk, pe = std::min<size_t>((size_t)n, (size_t)ce * chunk);
+            SDB_CK(cudaMemcpyAsync(static_cast<float*>(Xin.ptr) + pb * d, X + pb * d, sizeof(float) * (pe - pb) * d,
+                                   cudaMemcpyHostToDevice, copyStream));
+            SDB_CK(cudaEventRecord(segEv[sgi], copyStream));
+            SDB_CK(cudaStreamWaitEvent(st, segEv[sgi], 0));
+            pa.chunkBase = cb;
+            pa.chunkEnd = ce;
+            L_(launch_project(pa, st));
+        }
+        pa.chunkBase = pa.chunkEnd = 0;
+    } else {
+        L_(launch_project(pa, st));
+    }
     if (!ok) return fail(SDB_ERR_CUDA, std::string("projection launch failed: ") + cudaGetErrorString(cudaGetLastError()));
     if (!capture) SDB_CK(cudaEventRecord(ev[2], st));
 
@@ -576,18 +599,24 @@ sdb_status sdb_engine_create(int32_t n_points, int32_t n_features, int32_t devic
     e->d = n_features;
     e->device = device;
     sdb_params_default(&e->prm);
-    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
-        delete e;
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&e->copyStream, cudaStreamNonBlocking) != cudaSuccess) {
+        sdb_engine_destroy(e);
         return SDB_ERR_CUDA;
     }
+    for (int i = 0; i <= sdb_engine::kUploadSegs; ++i)
+        if (cudaEventCreateWithFlags(&e->segEv[i], cudaEventDisableTiming) != cudaSuccess) {
+            sdb_engine_destroy(e);
+            return SDB_ERR_CUDA;
+        }
     for (int i = 0; i < 9; ++i)
         if (cudaEventCreate(&e->ev[i]) != cudaSuccess) {
-            delete e;
+            sdb_engine_destroy(e);
             return SDB_ERR_CUDA;
         }
     if (cudaMallocHost(&e->hostErr, sizeof(int32_t) * 8) != cudaSuccess ||
         cudaMallocHost(&e->hostCounters, sizeof(unsigned long long) * 8) != cudaSuccess) {
-        delete e;
+        sdb_engine_destroy(e);
         return SDB_ERR_CUDA;
     }
     *out = e;
@@ -598,9 +627,13 @@ void sdb_engine_destroy(sdb_engine* e) {
     if (!e) return;
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->copyStream) cudaStreamSynchronize(e->copyStream);
     e->free_all();
     for (int i = 0; i < 9; ++i)
         if (e->ev[i]) cudaEventDestroy(e->ev[i]);
+    for (int i = 0; i <= sdb_engine::kUploadSegs; ++i)
+        if (e->segEv[i]) cudaEventDestroy(e->segEv[i]);
+    if (e->copyStream) cudaStreamDestroy(e->copyStream);
     if (e->hostErr) cudaFreeHost(e->hostErr);
     if (e->hostCounters) cudaFreeHost(e->hostCounters);
     if (e->stream) cudaStreamDestroy(e->stream);

@@ -33,6 +33,11 @@ struct sdb_engine {
     bool paramsSet = false;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[9] = {};
+    // host input is uploaded in segments on a second stream, each segment's
+    // projection starting as soon as its rows have landed
+    static constexpr int kUploadSegs = 8;
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t segEv[kUploadSegs + 1] = {};
     std::string err;
 
     // derived from the parameters

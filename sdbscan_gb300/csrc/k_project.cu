@@ -19,8 +19,14 @@
 
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 namespace sdb {
 namespace {
+
+// Projection blocks per launch: one full wave of 4 blocks per SM; the blocks
+// walk the launch's chunks grid-stride.
+constexpr int kProjectBlocks = 152 * 4;
 
 __device__ __forceinline__ void cp_async16(float* dst, const float* src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
@@ -39,10 +45,11 @@ __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
 // without bank conflicts); each thread then runs its point's sequential chain.
 constexpr int kCsPoints = 256, kCsDims = 32;
 
-__global__ void __launch_bounds__(kCsPoints) k_colstats(const float* __restrict__ X, int ldx, int n, int d, int dist,
-                                                        float* __restrict__ scale, int32_t* __restrict__ err) {
+// Points [pBase, pEnd).
+__global__ void __launch_bounds__(kCsPoints) k_colstats(const float* __restrict__ X, int ldx, int pBase, int n, int d,
+                                                        int dist, float* __restrict__ scale, int32_t* __restrict__ err) {
     __shared__ float tile[kCsDims][kCsPoints + 1];
-    const int p0 = blockIdx.x * kCsPoints;
+    const int p0 = pBase + blockIdx.x * kCsPoints;
     const int p = p0 + threadIdx.x;
     float s = 0.0f;
     bool neg = false, nonfinite = false;
@@ -202,13 +209,15 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
     float* rowbuf = base + w * rowLen;                                // per-warp copy of the row (Chi2/JS)
     // per-warp running (max v, max -v) per vector, bf16x2 rounded toward -inf
     __nv_bfloat162* ext = reinterpret_cast<__nv_bfloat162*>(base + warps * rowLen) + (size_t)w * a.nproj;
+    const int gEnd = a.chunkEnd > 0 ? a.chunkEnd : (a.n + a.chunk - 1) / a.chunk;
+    int g = a.chunkBase + blockIdx.x;  // the block's current chunk of points
     // per-warp double buffer of input rows: the next point's row is fetched
     // with cp.async while the current one is transformed
     const int xs = (a.d + 3) & ~3;
     float* xbuf = base + warps * rowLen + warps * a.nproj + (size_t)w * 2 * xs;
     const bool vec16 = (a.ldx & 3) == 0 && (reinterpret_cast<uintptr_t>(a.X) & 15) == 0;
     auto fetch = [&](int pp, int b) {
-        if (pp < min(a.n, (int)(blockIdx.x + 1) * a.chunk)) {
+        if (pp < min(a.n, (g + 1) * a.chunk)) {
             const float* src = a.X + (size_t)pp * a.ldx;
             float* dst = xbuf + b * xs;
             if (vec16) {
@@ -234,14 +243,16 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
         laneSigns[r] = msk;
     }
 
+    int localTies = 0;
+    // the block's chunks, grid-stride
+    for (; g < gEnd; g += gridDim.x) {
     // Per vector: (max v, max -v) over the warp's points, as bf16 rounded
     // toward -inf.  A rounded-down maximum is still a lower bound on a value
     // attained by a point of the chunk, which is all the top-m threshold needs.
     for (int e = (int)l; e < a.nproj; e += 32) ext[e] = __floats2bfloat162_rn(-INFINITY, -INFINITY);
     __syncwarp();
-    const int p0 = blockIdx.x * a.chunk;
+    const int p0 = g * a.chunk;
     const int p1 = min(a.n, p0 + a.chunk);
-    int localTies = 0;
     int buf = 0;
     fetch(p0 + w, 0);
     for (int p = p0 + w; p < p1; p += warps, buf ^= 1) {
@@ -391,22 +402,26 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
         __syncwarp();
     }
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    if (l == 0 && localTies) atomicAdd(a.ties, (unsigned long long)localTies);
     // chunk extremes: reduce the warps' rows
     __syncthreads();
     const __nv_bfloat162* ext0 = reinterpret_cast<const __nv_bfloat162*>(base + warps * rowLen);
     for (int e = threadIdx.x; e < a.nproj; e += blockDim.x) {
         __nv_bfloat162 m2 = ext0[e];
         for (int ww = 1; ww < warps; ++ww) m2 = __hmax2(m2, ext0[(size_t)ww * a.nproj + e]);
-        a.chunkMax[(size_t)blockIdx.x * a.nproj + e] = __bfloat162float(m2.x);
-        a.chunkMin[(size_t)blockIdx.x * a.nproj + e] = -__bfloat162float(m2.y);
+        a.chunkMax[(size_t)g * a.nproj + e] = __bfloat162float(m2.x);
+        a.chunkMin[(size_t)g * a.nproj + e] = -__bfloat162float(m2.y);
     }
+    __syncthreads();  // the warps' extremes are re-initialised for the next chunk
+    }  // chunks
+    if (l == 0 && localTies) atomicAdd(a.ties, (unsigned long long)localTies);
 }
 
 template <int NJ, int EMB>
 int launch_project_nje(const ProjectArgs& a, const float* scale, cudaStream_t st) {
     const int warps = 4;
-    const int G = (a.n + a.chunk - 1) / a.chunk;
+    const int G = (a.chunkEnd > 0 ? a.chunkEnd : (a.n + a.chunk - 1) / a.chunk) - a.chunkBase;
+    if (G <= 0) return 0;
+    const int grid = std::min(G, kProjectBlocks);
     const int nsw = (3 * a.fhtDim + 31) / 32;
     const int rowLen = EMB == 2 ? ((a.d + 3) & ~3) + a.fhtDim : 0;
     const size_t xs = (size_t)((a.d + 3) & ~3);
@@ -418,7 +433,7 @@ int launch_project_nje(const ProjectArgs& a, const float* scale, cudaStream_t st
             cudaSuccess)
             return -1;
     }
-    k_project<NJ, EMB><<<G, warps * 32, sm, st>>>(a, scale);
+    k_project<NJ, EMB><<<grid, warps * 32, sm, st>>>(a, scale);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
@@ -433,7 +448,11 @@ int launch_project_nj(const ProjectArgs& a, const float* scale, cudaStream_t st)
 
 int launch_project(const ProjectArgs& a, cudaStream_t st) {
     float* scale = a.scale;
-    k_colstats<<<(a.n + kCsPoints - 1) / kCsPoints, kCsPoints, 0, st>>>(a.X, a.ldx, a.n, a.d, a.dist, scale, a.err);
+    const int G = (a.n + a.chunk - 1) / a.chunk;
+    const int pb = a.chunkBase * a.chunk, pe = std::min(a.n, (a.chunkEnd > 0 ? a.chunkEnd : G) * a.chunk);
+    if (pe > pb)
+        k_colstats<<<(pe - pb + kCsPoints - 1) / kCsPoints, kCsPoints, 0, st>>>(a.X, a.ldx, pb, pe, a.d, a.dist,
+                                                                               scale, a.err);
     if (cudaPeekAtLastError() != cudaSuccess) return -1;
     int r;
     switch (a.fhtDim) {

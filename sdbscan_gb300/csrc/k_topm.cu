@@ -47,25 +47,52 @@ __host__ __device__ inline int pow2_ceil(int x) {
     return p;
 }
 
-// One CTA per list (r, side): T = m-th largest key among the G chunk extremes.
+// One CTA per list (r, side): T = m-th largest key among the G chunk extremes
+// (0 when G < m), by a 4-pass 8-bit radix select over the keys staged in
+// shared memory.
 __global__ void k_thresholds(TopMArgs a) {
-    extern __shared__ uint64_t sk[];
+    extern __shared__ uint32_t keys[];
+    __shared__ uint32_t hist[256];
+    __shared__ uint32_t selPrefix, selMask, selRank;
     const int list = blockIdx.x;
     const int r = list % a.nproj, side = list / a.nproj;
-    const int len = pow2_ceil(a.G);
-    for (int g = threadIdx.x; g < len; g += blockDim.x) {
-        uint64_t v = 0;
-        if (g < a.G) {
-            const float x = side == 0 ? a.chunkMax[(size_t)g * a.nproj + r] : -a.chunkMin[(size_t)g * a.nproj + r];
-            v = (uint64_t)key_of(x) << 32;
-        }
-        sk[g] = v;
+    for (int g = threadIdx.x; g < a.G; g += blockDim.x) {
+        const float x = side == 0 ? a.chunkMax[(size_t)g * a.nproj + r] : -a.chunkMin[(size_t)g * a.nproj + r];
+        keys[g] = key_of(x);
     }
-    block_sort_desc(sk, len);
     if (threadIdx.x == 0) {
-        const uint32_t T = a.G >= a.m ? (uint32_t)(sk[a.m - 1] >> 32) : 0u;
-        (side == 0 ? a.thrMax : a.thrMin)[r] = __uint_as_float(T);  // stored as raw key bits
+        selPrefix = 0;
+        selMask = 0;
+        selRank = (uint32_t)a.m;  // rank (1-based, from the top) still to find inside the prefix
     }
+    if (a.G < a.m) {
+        if (threadIdx.x == 0) (side == 0 ? a.thrMax : a.thrMin)[r] = __uint_as_float(0u);
+        return;
+    }
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+        __syncthreads();
+        const uint32_t pre = selPrefix, msk = selMask;
+        for (int g = threadIdx.x; g < a.G; g += blockDim.x) {
+            const uint32_t k = keys[g];
+            if ((k & msk) == pre) atomicAdd(&hist[(k >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t cum = 0, rank = selRank;
+            for (int b = 255; b >= 0; --b) {
+                if (cum + hist[b] >= rank) {
+                    selRank = rank - cum;
+                    selPrefix = pre | ((uint32_t)b << shift);
+                    selMask = msk | (255u << shift);
+                    break;
+                }
+                cum += hist[b];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) (side == 0 ? a.thrMax : a.thrMin)[r] = __uint_as_float(selPrefix);  // raw key bits
 }
 
 // One thread per 4 consecutive projections of a point.
@@ -231,8 +258,7 @@ __global__ void k_fallback(TopMArgs a) {
 }  // namespace
 
 int launch_topm_thresholds(const TopMArgs& a, cudaStream_t st) {
-    const int len = pow2_ceil(a.G);
-    const size_t sm = sizeof(uint64_t) * len;
+    const size_t sm = sizeof(uint32_t) * (size_t)a.G;
     if (sm > 48 * 1024 &&
         cudaFuncSetAttribute(k_thresholds, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return -1;
