@@ -133,7 +133,12 @@ struct ProjectArgs {
 int launch_project(const ProjectArgs& a, cudaStream_t st);
 
 // Random Fourier features for L1/L2: E[p] = [cos(R x_p), sin(R x_p)].
-int launch_rff(const float* Xt, int ld, int n, int d, const float* R, int h, float* E, cudaStream_t st);
+// gate (optional): run only if *gate != 0 (the tensor-core embedding failed).
+int launch_rff(const float* Xt, int ld, int n, int d, const float* R, int h, float* E, cudaStream_t st,
+               const int32_t* gate = nullptr);
+// BF16 mode: the same embedding on the tensor cores from BF16 copies of the
+// points (n x ldb) and of R (h x ldb); err set on a timed-out wait.
+int launch_rff_tc(const void* Xb, const void* Rb, int n, int h, int ldb, float* E, int32_t* err, cudaStream_t st);
 
 struct TopMArgs {
     const float* P;

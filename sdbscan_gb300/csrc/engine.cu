@@ -96,7 +96,7 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &listOff, &listFill, &members, &tileOff, &tileList, &hubCount, &hubOff, &hubLists, &masks, &inRaw,
             &aCount, &degree, &core, &parent, &border, &rootFlag, &labels, &nClusters, &scanTmp, &errFlags,
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
-            &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig};
+            &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig, &Rb};
 }
 
 // ---------------------------------------------------------------------------
@@ -292,7 +292,20 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         if (!capture)
             SDB_CK(cudaMemcpyAsync(Rt.ptr, hostRt.data(), sizeof(float) * hostRt.size(), cudaMemcpyHostToDevice, st));
         L_(launch_pad_copy(Xd, n, d, f32(Xt), ld, st));
-        L_(launch_rff(f32(Xt), ld, n, d, f32(Rt), ker / 2, f32(E), st));
+        const int h = ker / 2;
+        int tcr = -1;
+        if (p.precision == SDB_PREC_BF16) {
+            // the embedding GEMM on the tensor cores from BF16 copies of X and R;
+            // the FP32 kernel after it runs only if the tensor-core one failed
+            const int ldb = (d + 63) / 64 * 64;
+            if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * ldb) || !ensure(Rb, sizeof(uint16_t) * (size_t)h * ldb))
+                return SDB_ERR_NOMEM;
+            L_(launch_to_bf16(f32(Xt), ld, n, Xb.ptr, ldb, st));
+            L_(launch_to_bf16(f32(Rt), ld, h, Rb.ptr, ldb, st));
+            tcr = launch_rff_tc(Xb.ptr, Rb.ptr, n, h, ldb, f32(E), i32(errFlags) + 5, st);
+            if (tcr > 0) launches += tcr;
+        }
+        L_(launch_rff(f32(Xt), ld, n, d, f32(Rt), h, f32(E), st, tcr > 0 ? i32(errFlags) + 5 : nullptr));
         pa.X = f32(Xt);
         pa.ldx = ld;
         pa.E = f32(E);
@@ -552,6 +565,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
 // Error flags the kernels raised during the last (synchronised) fit.
 sdb_status sdb_engine::check_flags() {
     if (hostErr[4]) fallbacks += 1;  // the screened stage was redone on the plain path
+    if (hostErr[5]) fallbacks += 1;  // the tensor-core embedding was redone in FP32
     if (hostErr[0]) return fail(SDB_ERR_NEGATIVE, "X is not non-negative (Chi2/JS need nonnegative data)");
     if (hostErr[1])
         return fail(SDB_ERR_ZERO_POINT, prm.distance == SDB_COSINE ? "X has a point of zero norm (Cosine)"

@@ -16,7 +16,9 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool va
 }
 
 __global__ void __launch_bounds__(NT, 2)
-    k_rff(const float* __restrict__ X, int ld, int n, int d, const float* __restrict__ Rt, int h, float* __restrict__ E) {
+    k_rff(const float* __restrict__ X, int ld, int n, int d, const float* __restrict__ Rt, int h, float* __restrict__ E,
+          const int32_t* __restrict__ gate) {
+    if (gate != nullptr && __ldg(gate) == 0) return;  // the tensor-core embedding succeeded
     extern __shared__ __align__(16) float sm[];
     float* As = sm;
     float* Bs = As + STAGES * TM * LDS;
@@ -100,11 +102,12 @@ __global__ void __launch_bounds__(NT, 2)
 
 }  // namespace
 
-int launch_rff(const float* Xt, int ld, int n, int d, const float* Rt, int h, float* E, cudaStream_t st) {
+int launch_rff(const float* Xt, int ld, int n, int d, const float* Rt, int h, float* E, cudaStream_t st,
+               const int32_t* gate) {
     const size_t sm = sizeof(float) * STAGES * (TM + TN) * LDS;
     if (cudaFuncSetAttribute(k_rff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) return -1;
     dim3 grid((n + TM - 1) / TM, (h + TN - 1) / TN);
-    k_rff<<<grid, NT, sm, st>>>(Xt, ld, n, d, Rt, h, E);
+    k_rff<<<grid, NT, sm, st>>>(Xt, ld, n, d, Rt, h, E, gate);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 

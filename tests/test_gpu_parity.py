@@ -305,3 +305,32 @@ def test_batch_graph_equals_sweeps(precision):
     assert b.lanes() >= 1
     b.close()
     torch.cuda.synchronize()
+
+
+def test_bf16_rff_embedding_on_tensor_cores():
+    """BF16 mode for L2: the random-Fourier embedding GEMM runs on the tcgen05
+    tensor cores (BF16 operands, FP32 accumulation).  Against the plain FP32
+    embedding: projections within 2e-3 of each point's projection norm (BF16
+    rounding of X and R perturbs v = R x by ~2^-8 relative, and cos/sin and
+    the orthogonal rotation keep that scale), labels at ARI >= 0.99, and the
+    tensor-core kernel did not fall back."""
+    import torch
+    from sdbscan_gb300 import capi, datasets
+    from tests._metrics import adjusted_rand_score
+    X, _ = datasets.cfg3_aniso_l2(20000, 64, n_comp=10, seed=33)
+    Xt = torch.from_numpy(X).cuda()
+    dist = lambda a, b: (a.pow(2).sum(1)[:, None] + b.pow(2).sum(1)[None, :] - 2 * a @ b.T).clamp_min(0).sqrt()
+    sigma = float(dist(Xt[:2000], Xt[:2000])[torch.triu_indices(2000, 2000, 1).unbind()].median())
+    eps = float(torch.sort(dist(Xt[:500], Xt), dim=1).values[:, 30].median())  # median 30-NN distance
+    out = {}
+    for prec in (0, 1):
+        eng = capi.Engine(*X.shape)
+        eng.set_params(n_proj=1024, topK=10, topM=100, distance="L2", ker_n_features=1024, ker_sigma=sigma,
+                       random_seed=5, precision=prec)
+        eng.fit_sdbscan(X, eps, 30)
+        out[prec] = (eng.labels()[0], eng.projections(), eng.counters())
+    assert out[1][2]["fallbacks"] == 0
+    P0, P1 = out[0][1], out[1][1]
+    rel = np.abs(P1 - P0) / np.linalg.norm(P0, axis=1, keepdims=True)
+    assert rel.max() < 2e-3, rel.max()
+    assert adjusted_rand_score(out[0][0], out[1][0]) >= 0.99
