@@ -29,10 +29,26 @@ sys.path.insert(0, ROOT)
 METRIC = "points/sec fit_sDbscan: plain FP32 vs BF16+recheck & batched, at ARI≥0.99"
 WORKLOADS = {
     2: dict(workload="cfg2_cosine_1Mx784", n=1_000_000, d=784, distance="Cosine", n_proj=1024, topK=10, topM=50,
-            eps=0.25, minPts=50, seed=2007),
+            eps=0.25, minPts=50, seed=2007, fit="sdbscan"),
     1: dict(workload="cfg1_cosine_50Kx128", n=50_000, d=128, distance="Cosine", n_proj=1024, topK=5, topM=50,
-            eps=0.15, minPts=20, seed=1007),
+            eps=0.15, minPts=20, seed=1007, fit="sdbscan"),
+    # L2 through the random-Fourier embedding (ker 1024, sigma = median pairwise
+    # distance of the first 10K points).  The literal data puts every point
+    # farther than eps = 0.3 from all others, so the data is scaled by 0.0148:
+    # the median 30-NN distance of the unscaled 1M set is 20.23 and
+    # 0.3 / 20.23 = 0.0148 (scaling X and sigma together leaves the embedding's
+    # law unchanged).
+    3: dict(workload="cfg3_l2_rff_1Mx256_scaled", n=1_000_000, d=256, distance="L2", n_proj=1024, topK=10,
+            topM=100, eps=0.3, minPts=30, seed=3007, fit="sdbscan", ker_n_features=1024, scale=0.3 / 20.234),
+    # k, m, eps and minPts are not given for this config: k = 10, m = 50 (the
+    # Python defaults), minPts = 50, and eps = 0.17, the median 50-NN Chi2
+    # distance of 100 sampled points (about 60% of the points get reached).
+    4: dict(workload="cfg4_chi2_soptics_500Kx512", n=500_000, d=512, distance="Chi2", n_proj=1024, topK=10,
+            topM=50, eps=0.17, minPts=50, seed=4007, fit="soptics", ker_n_features=1024),
 }
+# flops per dimension of one candidate distance (multiply-add = 2; L2 sub + fma;
+# Chi2 mul, add, div, add)
+DIST_FLOPS = {"Cosine": 2, "L2": 3, "L1": 3, "Chi2": 4, "JS": 8}
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # nominal FP32 CUDA-core peak at max SM clock
 # DRAM bytes (read + write) of one k_dist<Cosine> launch on the 1M x 784
 # workload, from a one-pass ncu capture of
@@ -58,15 +74,42 @@ def _dist_env():
     return ws, rank, local
 
 
+def _host_data(cfg, n):
+    """The workload's law, n points, as a numpy (n, d) float32 array."""
+    from sdbscan_gb300 import datasets
+    w = cfg["workload"]
+    if w.startswith("cfg2"):
+        return datasets.cfg2_mnist_like(n, cfg["d"], seed=cfg["seed"])[0]
+    if w.startswith("cfg3"):
+        return datasets.cfg3_aniso_l2(n, cfg["d"], seed=cfg["seed"], scale=cfg["scale"])[0]
+    if w.startswith("cfg4"):
+        return datasets.cfg4_dirichlet(n, cfg["d"], seed=cfg["seed"])[0]
+    return datasets.cfg1_cosine(n, cfg["d"], seed=cfg["seed"])[0]
+
+
 def _make_data(cfg, device):
     import torch
     from sdbscan_gb300 import datasets
     if cfg["workload"].startswith("cfg2"):
         X, _ = datasets.cfg2_mnist_like_torch(cfg["n"], cfg["d"], seed=cfg["seed"], device=device)
     else:
-        Xn, _ = datasets.cfg1_cosine(cfg["n"], cfg["d"], seed=cfg["seed"])
-        X = torch.from_numpy(Xn).to(device)
+        X = torch.from_numpy(_host_data(cfg, cfg["n"])).to(device)
     return X.contiguous()
+
+
+def _kernel_params(cfg, X=None):
+    """ker_n_features / ker_sigma for the embedded distances; sigma is the
+    median pairwise distance of the first 10K points (L1/L2)."""
+    out = {}
+    if "ker_n_features" in cfg:
+        out["ker_n_features"] = cfg["ker_n_features"]
+    if cfg["distance"] in ("L1", "L2") and X is not None:
+        import torch
+        a = torch.as_tensor(X[:10000]).float().cuda() if not torch.is_tensor(X) else X[:10000].float()
+        d2 = (a.pow(2).sum(1)[:, None] + a.pow(2).sum(1)[None, :] - 2 * a @ a.T).clamp_min(0).sqrt()
+        iu = torch.triu_indices(a.shape[0], a.shape[0], 1, device=a.device)
+        out["ker_sigma"] = float(d2[iu[0], iu[1]].median())
+    return out
 
 
 class ClockSampler:
@@ -115,18 +158,35 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-def _cpu_sample_rate(Xh, cfg, n_sample):
+def _cpu_sample_rate(Xh, cfg, n_sample, kp=None):
     """The oracle (CPU restatement of the reference) on the first n_sample
     points, all host threads.  Returns (points/s, threads, seconds)."""
     from oracle.oracle import Port, build_port
     build_port()
     port = Port()
     threads = os.cpu_count() or 1
+    kp = kp or {}
+    kw = dict(dist=cfg["distance"], n_proj=cfg["n_proj"], topK=cfg["topK"], topM=cfg["topM"], seed=42,
+              threads=threads)
+    if "ker_n_features" in kp:
+        kw["ker"] = kp["ker_n_features"]
+    if "ker_sigma" in kp:
+        kw["sigma"] = kp["ker_sigma"]
+    fit = port.fit_soptics if cfg["fit"] == "soptics" else port.fit_sdbscan
     t0 = time.perf_counter()
-    port.fit_sdbscan(Xh[:n_sample], cfg["eps"], cfg["minPts"], dist=cfg["distance"], n_proj=cfg["n_proj"],
-                     topK=cfg["topK"], topM=cfg["topM"], seed=42, threads=threads)
+    fit(Xh[:n_sample], cfg["eps"], cfg["minPts"], **kw)
     dt = time.perf_counter() - t0
     return n_sample / dt, threads, dt
+
+
+def _np_median_pair(a):
+    """Median pairwise L2 distance of the rows of a (numpy, CPU)."""
+    import numpy as np
+    a = a.astype(np.float64)
+    sq = (a * a).sum(1)
+    d2 = np.maximum(sq[:, None] + sq[None, :] - 2.0 * a @ a.T, 0.0)
+    iu = np.triu_indices(a.shape[0], 1)
+    return float(np.median(np.sqrt(d2[iu])))
 
 
 def run_reference(args, cfg):
@@ -137,14 +197,13 @@ def run_reference(args, cfg):
         return 0
     import numpy as np
     from sdbscan_gb300 import datasets
-    n_sample = args.cpu_sample
-    if cfg["workload"].startswith("cfg2"):
-        Xh, _ = datasets.cfg2_mnist_like(n_sample, cfg["d"], seed=cfg["seed"])
-    else:
-        Xh, _ = datasets.cfg1_cosine(n_sample, cfg["d"], seed=cfg["seed"])
+    n_sample = min(args.cpu_sample, cfg["n"])
+    Xh = _host_data(cfg, n_sample)
+    kp = _kernel_params(cfg, Xh) if cfg["distance"] not in ("L1", "L2") else {
+        "ker_n_features": cfg["ker_n_features"], "ker_sigma": _np_median_pair(Xh[:2000])}
     rates = []
     for i in range(args.warmup + args.steps):
-        r, threads, dt = _cpu_sample_rate(Xh, cfg, n_sample)
+        r, threads, dt = _cpu_sample_rate(Xh, cfg, n_sample, kp)
         if i >= args.warmup:
             rates.append((r, dt))
     total_pts = n_sample * args.steps
@@ -154,11 +213,12 @@ def run_reference(args, cfg):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (config-2 law, numpy, seed 2007)",
+        "data": f"synthetic ({cfg['workload']} law, numpy, seed {cfg['seed']})",
         "config": {"workload": cfg["workload"], "n": cfg["n"], "d": cfg["d"], "n_proj": cfg["n_proj"],
                    "topK": cfg["topK"], "topM": cfg["topM"], "eps": cfg["eps"], "minPts": cfg["minPts"]},
         "cpu_baseline": {"value": value, "unit": "points/s", "cores": threads, "kind": "port",
-                         "sample": f"full fit_sDbscan on {n_sample} points of the workload's law per step "
+                         "sample": f"full fit_{'sOptics' if cfg['fit'] == 'soptics' else 'sDbscan'} on {n_sample} "
+                                   f"points of the workload's law per step "
                                    f"(oracle/ restatement, OpenMP, {threads} threads)"},
         "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -279,9 +339,21 @@ def run_ours(args, cfg):
     n, d = cfg["n"], cfg["d"]
     X = _make_data(cfg, f"cuda:{local}")
     torch.cuda.synchronize()
+    kp = _kernel_params(cfg, X)
+    optics = cfg["fit"] == "soptics"
     eng = capi.Engine(n, d, device=local)
-    eng.set_params(n_proj=cfg["n_proj"], topK=cfg["topK"], topM=cfg["topM"], distance=cfg["distance"],
-                   random_seed=42)
+
+    def params(precision=capi.PREC_FP32):
+        eng.set_params(n_proj=cfg["n_proj"], topK=cfg["topK"], topM=cfg["topM"], distance=cfg["distance"],
+                       random_seed=42, precision=precision, **kp)
+
+    def fit_dev():
+        (eng.fit_soptics_device if optics else eng.fit_sdbscan_device)(X.data_ptr(), cfg["eps"], cfg["minPts"])
+
+    def result():
+        return eng.optics() if optics else eng.labels()
+
+    params()
     stream = torch.cuda.ExternalStream(eng.stream(), device=f"cuda:{local}")
 
     def barrier():
@@ -290,7 +362,7 @@ def run_ours(args, cfg):
             torch.distributed.barrier()
 
     for _ in range(args.warmup):
-        eng.fit_sdbscan_device(X.data_ptr(), cfg["eps"], cfg["minPts"])
+        fit_dev()
     barrier()
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
@@ -299,7 +371,7 @@ def run_ours(args, cfg):
     with ClockSampler(local) as clk:
         start.record(stream)
         for _ in range(args.steps):
-            eng.fit_sdbscan_device(X.data_ptr(), cfg["eps"], cfg["minPts"])
+            fit_dev()
             for k_, v_ in eng.stage_ms().items():
                 stage_sum[k_] = stage_sum.get(k_, 0.0) + v_
             launches += eng.counters()["launches"]
@@ -312,21 +384,23 @@ def run_ours(args, cfg):
         ms = float(t.item())
     value = ws * n * args.steps / (ms / 1e3)
     counters = eng.counters()
-    labels, ncl = eng.labels()
+    res = result()
+    labels = None if optics else res[0]
 
-    # the BF16 screening mode on the same data: same eps decisions, tensor cores
+    # BF16 mode on the same data: Cosine distances screened on the tensor cores
+    # with exact re-decision (identical labels); L1/L2 embedding GEMM on the
+    # tensor cores (labels compared by ARI)
     bf16 = None
-    if not args.no_bf16:
-        eng.set_params(n_proj=cfg["n_proj"], topK=cfg["topK"], topM=cfg["topM"], distance=cfg["distance"],
-                       random_seed=42, precision=capi.PREC_BF16)
+    if not args.no_bf16 and not optics and cfg["distance"] in ("Cosine", "L1", "L2"):
+        params(capi.PREC_BF16)
         for _ in range(args.warmup):
-            eng.fit_sdbscan_device(X.data_ptr(), cfg["eps"], cfg["minPts"])
+            fit_dev()
         barrier()
         sb, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         bstages = {}
         sb.record(stream)
         for _ in range(args.steps):
-            eng.fit_sdbscan_device(X.data_ptr(), cfg["eps"], cfg["minPts"])
+            fit_dev()
             for k_, v_ in eng.stage_ms().items():
                 bstages[k_] = bstages.get(k_, 0.0) + v_
         eb.record(stream)
@@ -335,10 +409,16 @@ def run_ours(args, cfg):
         blabels, bncl = eng.labels()
         bc = eng.counters()
         from tests._metrics import adjusted_rand_score
-        flops = 2.0 * (2 * cfg["topK"] * cfg["topM"]) * d * n
-        stage_s = bstages["distances"] / args.steps / 1e3
         _, bf16_peak, src = _peaks()
-        broof = {"bound": "tensor", "kernel": "distance stage: k_to_bf16 + k_dist_tc + k_recheck",
+        if cfg["distance"] == "Cosine":
+            flops = 2.0 * (2 * cfg["topK"] * cfg["topM"]) * d * n
+            stage_s = bstages["distances"] / args.steps / 1e3
+            kern = "distance stage: k_to_bf16 + k_dist_tc + k_recheck"
+        else:
+            flops = 2.0 * n * d * (kp["ker_n_features"] // 2)
+            stage_s = bstages["project"] / args.steps / 1e3
+            kern = "projection stage incl. the embedding GEMM k_rff_tc (upper bound on its time)"
+        broof = {"bound": "tensor", "kernel": kern,
                  "achieved": flops / stage_s / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
                  "frac": flops / stage_s / 1e12 / bf16_peak, "traffic": None,
                  "peak_source": f"{src} bf16_tflops_sustained (timed inside the fit)",
@@ -348,37 +428,43 @@ def run_ours(args, cfg):
                 "ari_vs_plain": adjusted_rand_score(labels, blabels), "labels_identical": bool(np.array_equal(labels, blabels)),
                 "rechecked_pairs": bc["rechecked"], "fallbacks": bc["fallbacks"],
                 "stage_ms": {k_: v_ / args.steps for k_, v_ in bstages.items()}}
-        eng.set_params(n_proj=cfg["n_proj"], topK=cfg["topK"], topM=cfg["topM"], distance=cfg["distance"],
-                       random_seed=42)
+        params()
 
     # end to end through the public call: pinned host input, labels back
     Xh_t = torch.empty((n, d), dtype=torch.float32, pin_memory=True)
     Xh_t.copy_(X)
     Xh = Xh_t.numpy()
+    fit_host = eng.fit_soptics if optics else eng.fit_sdbscan
     for _ in range(min(args.warmup, 2)):
-        eng.fit_sdbscan(Xh, cfg["eps"], cfg["minPts"])
-        eng.labels()
+        fit_host(Xh, cfg["eps"], cfg["minPts"])
+        result()
     barrier()
     t0 = time.perf_counter()
+    e2e_stages = {}
     for _ in range(args.steps):
-        eng.fit_sdbscan(Xh, cfg["eps"], cfg["minPts"])
-        lab_e2e, _ = eng.labels()
+        fit_host(Xh, cfg["eps"], cfg["minPts"])
+        res_e2e = result()
+        for k_, v_ in eng.stage_ms().items():
+            e2e_stages[k_] = e2e_stages.get(k_, 0.0) + v_ / args.steps
     barrier()
     e2e_s = time.perf_counter() - t0
     e2e_value = ws * n * args.steps / e2e_s
-    assert np.array_equal(lab_e2e, labels), "host-input and device-input fits disagree"
+    assert all(np.array_equal(a, b) for a, b in zip(res_e2e[:1], res[:1])), "host-input and device-input fits disagree"
+    d2h = n * 8 if optics else n * 4 + 4
 
-    batched = None if args.no_batched else run_batched(args, local, cpu=ws == 1 and not args.no_cpu)
+    batched = None
+    if not args.no_batched and cfg["workload"].startswith("cfg2"):
+        batched = run_batched(args, local, cpu=ws == 1 and not args.no_cpu)
     if rank != 0:
         return 0
     # dominant kernel: the distance stage (one k_dist launch per fit)
     dist_ms = stage_sum["distances"] / args.steps
-    flops = 2.0 * (2 * cfg["topK"] * cfg["topM"]) * d * n
+    flops = float(DIST_FLOPS[cfg["distance"]]) * (2 * cfg["topK"] * cfg["topM"]) * d * n
     achieved = flops / (dist_ms / 1e3) / 1e12
     hbm_peak, _, src = _peaks()
     traffic = K_DIST_TRAFFIC_1M if cfg["workload"].startswith("cfg2") else None
     alg_bytes = n * d * 4 + 2 * cfg["n_proj"] * cfg["topM"] * d * 4  # rows of X + candidate rows, once each
-    roofline = {"bound": "fp32", "kernel": "k_dist<Cosine>", "achieved": achieved, "peak": FP32_PEAK_TFLOPS,
+    roofline = {"bound": "fp32", "kernel": f"k_dist<{cfg['distance']}>", "achieved": achieved, "peak": FP32_PEAK_TFLOPS,
                 "unit": "TFLOP/s", "frac": achieved / FP32_PEAK_TFLOPS, "traffic": traffic,
                 "bound_note": "exact FP32 SIMT grouped GEMM (sequential fmaf per pair): bounded by the FP32 FMA "
                               "pipe, not by HBM or the tensor cores; the BF16 leg carries the tensor roofline",
@@ -392,31 +478,39 @@ def run_ours(args, cfg):
     stages = {k_: v_ / args.steps for k_, v_ in stage_sum.items()}
     cpu = None
     if ws == 1 and not args.no_cpu:
-        Xs = Xh[: args.cpu_sample].copy()
-        rate, threads, dt = _cpu_sample_rate(Xs, cfg, args.cpu_sample)
+        ns = min(args.cpu_sample, n)
+        Xs = Xh[:ns].copy()
+        rate, threads, dt = _cpu_sample_rate(Xs, cfg, ns, kp)
         cpu = {"value": rate, "unit": "points/s", "cores": threads, "kind": "port",
-               "sample": f"full fit_sDbscan on the first {args.cpu_sample} points of the same matrix "
-                         f"(oracle/ restatement, OpenMP, {threads} threads, {dt:.1f} s)"}
+               "sample": f"full fit_{'sOptics' if optics else 'sDbscan'} on the first {ns} points of the same "
+                         f"matrix (oracle/ restatement, OpenMP, {threads} threads, {dt:.1f} s)"}
     line = {
         "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (config-2 law: Bernoulli(0.2) x U(0.3,1) prototypes, 10% redraw, L2-normalised; "
-                "drawn on device, seed 2007)",
-        "config": {"workload": cfg["workload"], "n": n, "d": d, "n_proj": cfg["n_proj"], "topK": cfg["topK"],
+        "data": ("synthetic (config-2 law: Bernoulli(0.2) x U(0.3,1) prototypes, 10% redraw, L2-normalised; "
+                 "drawn on device, seed 2007)") if cfg["workload"].startswith("cfg2") else
+                f"synthetic ({cfg['workload']} law, numpy, seed {cfg['seed']})",
+        "config": {"workload": cfg["workload"], "n": n, "d": d, "distance": cfg["distance"],
+                   "fit": "fit_sOptics" if optics else "fit_sDbscan", "n_proj": cfg["n_proj"], "topK": cfg["topK"],
                    "topM": cfg["topM"], "eps": cfg["eps"], "minPts": cfg["minPts"], "precision": "fp32",
-                   "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2 (3.1 GB per step)"},
+                   **kp, "parallelism": f"replicas x{ws}",
+                   "l2": f"inputs larger than L2 ({n * d * 4 / 1e9:.2f} GB per step)" if n * d * 4 > 129e6 else
+                         "inputs smaller than L2: L2 flushed between steps is not done; small workload"},
         "clocks": clk.summary(),
         "e2e": {"value": e2e_value, "unit": "points/s", "h2d_bytes_per_step": n * d * 4,
-                "d2h_bytes_per_step": n * 4 + 4},
+                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / args.steps,
+                "stage_ms": e2e_stages},
         "gpu_launches": launches,
         "roofline": roofline,
         "cpu_baseline": cpu,
         "stage_ms": stages,
         "bf16_screening": bf16,
         "batched": batched,
-        "result": {"n_clusters": ncl, "noise": int((labels < 0).sum()), "topk_ties": counters["topk_ties"],
-                   "topm_ties": counters["topm_ties"], "pairs_within_eps": counters["pairs"]},
+        "result": ({"reachable": int((res[1] >= 0).sum()), "max_reachability": float(res[1].max())} if optics else
+                   {"n_clusters": res[1], "noise": int((labels < 0).sum())}) |
+                  {"topk_ties": counters["topk_ties"], "topm_ties": counters["topm_ties"],
+                   "pairs_within_eps": counters["pairs"]},
     }
     print(json.dumps(line))
     if ws > 1:

@@ -136,8 +136,9 @@ int launch_project(const ProjectArgs& a, cudaStream_t st);
 // gate (optional): run only if *gate != 0 (the tensor-core embedding failed).
 int launch_rff(const float* Xt, int ld, int n, int d, const float* R, int h, float* E, cudaStream_t st,
                const int32_t* gate = nullptr);
-// BF16 mode: the same embedding on the tensor cores from BF16 copies of the
-// points (n x ldb) and of R (h x ldb); err set on a timed-out wait.
+// BF16 mode: the same embedding on the tensor cores from split-BF16 copies
+// ([hi | lo] per row) of the points (n x 2 ldb) and of R (h x 2 ldb); err set
+// on a timed-out wait.
 int launch_rff_tc(const void* Xb, const void* Rb, int n, int h, int ldb, float* E, int32_t* err, cudaStream_t st);
 
 struct TopMArgs {
@@ -216,6 +217,7 @@ constexpr int kMaxScreenedSweep = 16;
 int launch_dist(const DistArgs& a, cudaStream_t st);
 int launch_masks_from_dists(const DistArgs& a, cudaStream_t st);
 int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream_t st);
+int launch_to_bf16_split(const float* Xt, int ld, int n, void* Xs, int ldb, cudaStream_t st);
 int launch_screen_reset(const DistArgs& a, cudaStream_t st);
 int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, uint64_t* queue, int64_t qcap,
                    unsigned long long* qcount, int32_t* err, int grid, cudaStream_t st,

@@ -295,13 +295,14 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         const int h = ker / 2;
         int tcr = -1;
         if (p.precision == SDB_PREC_BF16) {
-            // the embedding GEMM on the tensor cores from BF16 copies of X and R;
-            // the FP32 kernel after it runs only if the tensor-core one failed
+            // the embedding GEMM on the tensor cores from split-BF16 copies of X
+            // and R; the FP32 kernel after it runs only if the tensor-core one failed
             const int ldb = (d + 63) / 64 * 64;
-            if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * ldb) || !ensure(Rb, sizeof(uint16_t) * (size_t)h * ldb))
+            if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * 2 * ldb) ||
+                !ensure(Rb, sizeof(uint16_t) * (size_t)h * 2 * ldb))
                 return SDB_ERR_NOMEM;
-            L_(launch_to_bf16(f32(Xt), ld, n, Xb.ptr, ldb, st));
-            L_(launch_to_bf16(f32(Rt), ld, h, Rb.ptr, ldb, st));
+            L_(launch_to_bf16_split(f32(Xt), ld, n, Xb.ptr, ldb, st));
+            L_(launch_to_bf16_split(f32(Rt), ld, h, Rb.ptr, ldb, st));
             tcr = launch_rff_tc(Xb.ptr, Rb.ptr, n, h, ldb, f32(E), i32(errFlags) + 5, st);
             if (tcr > 0) launches += tcr;
         }

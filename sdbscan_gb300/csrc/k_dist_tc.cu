@@ -342,7 +342,32 @@ __global__ void k_to_bf16(const float* __restrict__ Xt, int ld, int n, __nv_bflo
     *reinterpret_cast<uint4*>(Xb + (size_t)p * ldb + c0) = *reinterpret_cast<const uint4*>(out);
 }
 
+// Xt (FP32, row stride ld) -> [hi | lo] BF16 halves per row (row stride
+// 2 ldb): hi = bf16(x), lo = bf16(x - hi), both zero past ld.
+__global__ void k_to_bf16_split(const float* __restrict__ Xt, int ld, int n, __nv_bfloat16* __restrict__ Xs, int ldb) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t per = (size_t)ldb / 8;
+    if (q >= (size_t)n * per) return;
+    const int p = (int)(q / per), c0 = (int)(q % per) * 8;
+    __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int c = c0 + i;
+        const float x = c < ld ? Xt[(size_t)p * ld + c] : 0.0f;
+        hi[i] = __float2bfloat16_rn(x);
+        lo[i] = __float2bfloat16_rn(x - __bfloat162float(hi[i]));
+    }
+    *reinterpret_cast<uint4*>(Xs + (size_t)p * 2 * ldb + c0) = *reinterpret_cast<const uint4*>(hi);
+    *reinterpret_cast<uint4*>(Xs + (size_t)p * 2 * ldb + ldb + c0) = *reinterpret_cast<const uint4*>(lo);
+}
+
 }  // namespace
+
+int launch_to_bf16_split(const float* Xt, int ld, int n, void* Xs, int ldb, cudaStream_t st) {
+    const size_t total = (size_t)n * (ldb / 8);
+    k_to_bf16_split<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(Xt, ld, n, static_cast<__nv_bfloat16*>(Xs), ldb);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
 
 int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream_t st) {
     const size_t total = (size_t)n * (ldb / 8);

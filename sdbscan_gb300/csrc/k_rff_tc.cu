@@ -3,6 +3,13 @@
 //   V = X R^T   (X: n x d points, R: h x d, h = ker / 2),   E = [cos V, sin V],
 // with BF16 operands loaded by TMA and FP32 accumulation in tensor memory.
 //
+// Split BF16: each FP32 operand x is stored as hi = bf16(x), lo = bf16(x - hi)
+// (x - hi is exact in FP32) and the accumulator takes hi.hi + hi.lo + lo.hi:
+// three passes over K into the same tensor memory.  Each product then errs by
+// at most ~3 * 2^-16 of |x||y| (the dropped lo.lo and the rounding of the lo
+// parts) instead of 2^-7 for one BF16 pass, which keeps the cos / sin
+// features within ~1e-4 of FP32 and the candidate lists of the plain path.
+//
 // Tile: 128 points x 256 rows of R, K in chunks of 64 (one 128-byte swizzle
 // atom per row, the layout TMA's 128B swizzle writes and the MMA's smem
 // descriptor reads); 97 KB of smem, so two CTAs share an SM and one's
@@ -64,17 +71,20 @@ __global__ void __launch_bounds__(NT, 2) k_rff_tc(const __grid_constant__ CUtens
     int failed = 0;
     if (tid == 0) {
         int issued[STAGES] = {}, landed[STAGES] = {};  // loads issued into / waited on per stage
+        // chunk kc of pass kc / nk: pass 0 hi(X).hi(R), 1 hi(X).lo(R), 2 lo(X).hi(R)
+        // (each matrix holds [hi | lo], nk chunks apiece)
         auto load = [&](int kc) {
-            const int s = kc % STAGES;
+            const int s = kc % STAGES, pass = kc / nk, kk = kc % nk;
             const uint32_t sA = base + s * STAGE_BYTES, sB = sA + A_BYTES, bar = tc::smem_u32(&fullBar[s]);
             tc::mbar_expect_tx(bar, STAGE_BYTES);
-            tc::tma_load_2d(sA, &tmX, kc * BK, m0, bar);
-            tc::tma_load_2d(sB, &tmR, kc * BK, n0, bar);
+            tc::tma_load_2d(sA, &tmX, (pass == 2 ? nk + kk : kk) * BK, m0, bar);
+            tc::tma_load_2d(sB, &tmR, (pass == 1 ? nk + kk : kk) * BK, n0, bar);
             ++issued[s];
         };
-        for (int kc = 0; kc < nk && kc < STAGES; ++kc) load(kc);
+        const int nkAll = 3 * nk;
+        for (int kc = 0; kc < nkAll && kc < STAGES; ++kc) load(kc);
         int committed = 0;
-        for (int kc = 0; kc < nk; ++kc) {
+        for (int kc = 0; kc < nkAll; ++kc) {
             const int s = kc % STAGES;
             if (!tc::mbar_wait(tc::smem_u32(&fullBar[s]), (uint32_t)(landed[s] & 1))) {
                 failed = 1;
@@ -90,7 +100,7 @@ __global__ void __launch_bounds__(NT, 2) k_rff_tc(const __grid_constant__ CUtens
             tc::mma_commit(tc::smem_u32(&freeBar[s]));
             ++committed;
             const int nxt = kc + STAGES;
-            if (nxt < nk) {  // stage s is refilled once the MMAs above have read it
+            if (nxt < nkAll) {  // stage s is refilled once the MMAs above have read it
                 if (!tc::mbar_wait(tc::smem_u32(&freeBar[s]), (uint32_t)((kc / STAGES) & 1))) {
                     failed = 1;
                     break;
@@ -178,12 +188,13 @@ bool encode_bf16(CUtensorMap* m, const void* ptr, int rows, int ldb, int boxRows
 
 }  // namespace
 
-// Xb: n x ldb BF16 points, Rb: h x ldb BF16 rows of R (ldb a multiple of 64,
-// both 16-byte aligned, zero padded past d); E: n x 2h FP32.
-int launch_rff_tc(const void* Xb, const void* Rb, int n, int h, int ldb, float* E, int32_t* err, cudaStream_t st) {
-    if (ldb % BK != 0 || (reinterpret_cast<uintptr_t>(Xb) & 15) || (reinterpret_cast<uintptr_t>(Rb) & 15)) return -1;
+// Xs: n x 2 ldb BF16 points ([hi | lo] per row), Rs: h x 2 ldb BF16 rows of R
+// likewise (ldb a multiple of 64, zero padded past d, 16-byte aligned);
+// E: n x 2h FP32.
+int launch_rff_tc(const void* Xs, const void* Rs, int n, int h, int ldb, float* E, int32_t* err, cudaStream_t st) {
+    if (ldb % BK != 0 || (reinterpret_cast<uintptr_t>(Xs) & 15) || (reinterpret_cast<uintptr_t>(Rs) & 15)) return -1;
     CUtensorMap tmX, tmR;
-    if (!encode_bf16(&tmX, Xb, n, ldb, BM) || !encode_bf16(&tmR, Rb, h, ldb, BN)) return -1;
+    if (!encode_bf16(&tmX, Xs, n, 2 * ldb, BM) || !encode_bf16(&tmR, Rs, h, 2 * ldb, BN)) return -1;
     const size_t sm = (size_t)STAGES * STAGE_BYTES + 1024;
     if (cudaFuncSetAttribute(k_rff_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return -1;
