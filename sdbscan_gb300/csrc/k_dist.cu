@@ -27,7 +27,7 @@ namespace {
 // of 8 rows): <16, 4> gives 64 columns on 256 threads (any m, one 64-bit mask
 // word per tile) and <10, 5> exactly 50 columns on 160 threads (m in 41..50,
 // no padded columns).
-constexpr int TM = 128, TK = 32, LDS = TK + 4, STAGES = 3;
+constexpr int TM = 128, TK = 32, LDS = TK + 4, STAGES = 2;
 constexpr int TN = 64;  // the tile grid's candidate columns (and mask bits) per tile
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
@@ -68,7 +68,7 @@ template <int DIST> __device__ __forceinline__ float finish(float acc) {
 }
 
 template <int DIST, int TX, int CN>
-__global__ void __launch_bounds__(16 * TX, 2) k_dist(DistArgs a) {
+__global__ void __launch_bounds__(16 * TX, TX == 10 ? 3 : 2) k_dist(DistArgs a) {
     constexpr int NT = 16 * TX, TNK = TX * CN;  // threads, candidate columns this kernel computes
     if (a.gate != nullptr && __ldg(a.gate) == 0) return;  // the BF16 screening succeeded
     extern __shared__ __align__(16) float sm[];
