@@ -108,8 +108,7 @@ sdb_status sdb_batch_create(int32_t n_sets, const int32_t* n_points, const int32
         delete b;
         return SDB_ERR_CUDA;
     }
-    sdb_params q = *p;
-    q.precision = SDB_PREC_FP32;  // sweeps threshold stored FP32 distances
+    sdb_params q = *p;  // BF16 precision screens each set's distances (exact re-decision near every eps)
     if (q.random_seed < 0) q.random_seed = 42;
     b->labels.resize(n_sets);
     b->ncl.resize(n_sets);
