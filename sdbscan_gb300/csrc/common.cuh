@@ -204,6 +204,7 @@ struct DistArgs {
     int nproj, m, k, W;   // W = 64-bit mask words per (point, slot)
     int nct;              // candidate tiles per list
     float eps;
+    float epsLo;          // eps sweeps: k_masks_from_dists keeps epsLo < d <= eps
     uint64_t* masks;      // n x 2k x W
     int32_t* inRaw;       // n
     float* dists;         // n x 2k x m (optional)
@@ -242,6 +243,12 @@ struct CoreArgs {
     const int32_t* hubIdx;   // n: dense index of hub points, -1 for others
     const uint32_t* kMask;   // hubs x ceil(2D/32): bit l set when the hub meets list l (its top-k)
     uint64_t* firstMasks;    // n x 2k x W: the mask bits of each point's first occurrence of a candidate
+    // eps sweeps, processed in ascending eps: the masks hold only the pairs new
+    // at this eps (previous eps < d <= eps); degrees accumulate, core flags only
+    // grow, firstMasks accumulate and newMasks receive this round's bits
+    int accumulate, round;
+    uint64_t* newMasks;      // n x 2k x W (accumulate only)
+    int32_t* coreEps;        // n: round at which the point became core, -1 before (accumulate only)
 };
 int launch_slot_sigs(const int32_t* topM, int D, int m, const int64_t* hubOff, const int32_t* hubLists, void* sig,
                      cudaStream_t st);
@@ -264,6 +271,11 @@ struct ClusterArgs {
     const int64_t* tileTotal;  // device: actual number of tiles
     int64_t nTiles;            // launch grid (an upper bound)
     int TM, nct, nproj;
+    // eps sweeps: the union-find carries over from the previous (smaller) eps,
+    // and only rows with a new edge or a newly core endpoint are united
+    int carry, round;
+    const uint64_t* newMasks;  // this round's first-occurrence bits
+    const int32_t* coreEps;    // round at which each point became core
     const uint8_t* core;
     int32_t* parent;
     int32_t* border;

@@ -96,7 +96,7 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &listOff, &listFill, &members, &tileOff, &tileList, &hubCount, &hubOff, &hubLists, &masks, &inRaw,
             &aCount, &degree, &core, &parent, &border, &rootFlag, &labels, &nClusters, &scanTmp, &errFlags,
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
-            &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig, &Rb};
+            &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig, &Rb, &newMasks, &coreEps};
 }
 
 // ---------------------------------------------------------------------------
@@ -479,9 +479,29 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     L_(launch_hub_masks(ca, i32(hubIdx), i64(rootFlag), static_cast<uint32_t*>(kMask.ptr), i64(scanTmp),
                         reinterpret_cast<int64_t*>(ctr + 5), st));
     const int rounds = sweep ? sw->nEps : 1;
+    // an eps sweep runs in ascending eps: each round adds the pairs with
+    // previous eps < d <= eps to the degrees, the first-occurrence masks and
+    // the union-find of the round before (neighbourhoods only grow with eps)
+    std::vector<int> ord(rounds, 0);
+    if (sweep) {
+        for (int i = 0; i < rounds; ++i) ord[i] = i;
+        std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return sw->eps[x] < sw->eps[y]; });
+        if (!ensure(newMasks, sizeof(uint64_t) * (size_t)n * 2 * k * W) || !ensure(coreEps, sizeof(int32_t) * n))
+            return SDB_ERR_NOMEM;
+        SDB_CK(cudaMemsetAsync(degree.ptr, 0, sizeof(int32_t) * n, st));
+        SDB_CK(cudaMemsetAsync(core.ptr, 0, n, st));
+        SDB_CK(cudaMemsetAsync(coreEps.ptr, 0xFF, sizeof(int32_t) * n, st));
+        SDB_CK(cudaMemsetAsync(firstMasks.ptr, 0, sizeof(uint64_t) * (size_t)n * 2 * k * W, st));
+        ca.accumulate = 1;
+        ca.newMasks = static_cast<uint64_t*>(newMasks.ptr);
+        ca.coreEps = i32(coreEps);
+    }
     for (int ei = 0; ei < rounds; ++ei) {
-    if (sweep) {  // this eps: masks and reverse counts from the stored distances
-        da.eps = sw->eps[ei];
+    const int eo = ord[ei];  // the eps value (and output slot) of this round
+    if (sweep) {  // this eps: new pairs' masks and reverse counts from the stored distances
+        da.eps = sw->eps[eo];
+        da.epsLo = ei > 0 ? sw->eps[ord[ei - 1]] : -INFINITY;
+        ca.round = ei;
         SDB_CK(cudaMemsetAsync(inRaw.ptr, 0, sizeof(int32_t) * n, st));
         L_(launch_masks_from_dists(da, st));
     }
@@ -516,6 +536,12 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         ka.scanTmp = i64(scanTmp);
         ka.labels = i32(labels);
         ka.nClusters = i32(nClusters);
+        if (sweep) {
+            ka.carry = 1;
+            ka.round = ei;
+            ka.newMasks = static_cast<const uint64_t*>(newMasks.ptr);
+            ka.coreEps = i32(coreEps);
+        }
         L_(launch_cluster(ka, st));
         if (!ok) return fail(SDB_ERR_CUDA, std::string("cluster launch failed: ") + cudaGetErrorString(cudaGetLastError()));
     } else {
@@ -523,9 +549,9 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         if (s != SDB_OK) return s;
     }
     if (sweep) {
-        SDB_CK(cudaMemcpyAsync(sw->labelsDev + (size_t)ei * n, labels.ptr, sizeof(int32_t) * n,
+        SDB_CK(cudaMemcpyAsync(sw->labelsDev + (size_t)eo * n, labels.ptr, sizeof(int32_t) * n,
                                cudaMemcpyDeviceToDevice, st));
-        SDB_CK(cudaMemcpyAsync(sw->nclDev + ei, nClusters.ptr, sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+        SDB_CK(cudaMemcpyAsync(sw->nclDev + eo, nClusters.ptr, sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
     }
     }  // eps rounds
     if (!capture) SDB_CK(cudaEventRecord(ev[7], st));

@@ -51,7 +51,8 @@ struct sdb_engine {
     DevBuf Xin, Xt, scale, P, topK, chunkMax, chunkMin, thr, cand, candCount, topM, listCount, listOff, listFill,
         members, tileOff, tileList, hubCount, hubOff, hubLists, masks, inRaw, aCount, degree, core, parent, border,
         rootFlag, labels, nClusters, scanTmp, errFlags, counters, E, Rt, signs, compCosh, dists, coreDist, nbOff,
-        nbIdx, nbDist, nbFill, hubIdx, kMask, firstMasks, Xb, queue, sweepLabels, sweepNcl, sig, Rb;
+        nbIdx, nbDist, nbFill, hubIdx, kMask, firstMasks, Xb, queue, sweepLabels, sweepNcl, sig, Rb, newMasks,
+        coreEps;
 
     // results
     bool haveLabels = false, haveOptics = false, haveFit = false, lastOptics = false;

@@ -46,10 +46,10 @@ __device__ void unite(int32_t* parent, int a, int b) {
     }
 }
 
-__global__ void k_init(int32_t* parent, int32_t* border, int n) {
+__global__ void k_init(int32_t* parent, int32_t* border, int n, int keepParent) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    parent[p] = p;
+    if (!keepParent) parent[p] = p;
     border[p] = INT_MAX;
 }
 
@@ -82,15 +82,21 @@ __device__ __forceinline__ bool tile_of(const ClusterArgs& a, int64_t t, Tile& t
 // value only costs a redundant unite.
 __global__ void __launch_bounds__(128) k_union_tiles(ClusterArgs a) {
     __shared__ int croot[64];
+    __shared__ unsigned long long newCoreCand;  // carry: candidates that became core this round
     Tile tl;
     if (!tile_of(a, blockIdx.x, tl)) return;
     volatile int* vroot = croot;
+    if (threadIdx.x == 0) newCoreCand = 0ull;
+    __syncthreads();
     if (threadIdx.x < 64) {
         const int c = tl.ct * 64 + threadIdx.x;
         int root = -1;
         if (c < a.m) {
             const int q = __ldg(tl.cand + c);
-            if (a.core[q]) root = find_root(a.parent, q);
+            if (a.core[q]) {
+                root = find_root(a.parent, q);
+                if (a.carry && a.coreEps[q] == a.round) atomicOr(&newCoreCand, 1ull << threadIdx.x);
+            }
         }
         croot[threadIdx.x] = root;
     }
@@ -100,8 +106,12 @@ __global__ void __launch_bounds__(128) k_union_tiles(ClusterArgs a) {
     const int2 mb = __ldg(a.members + row);
     const int p = mb.x;
     if (!a.core[p]) return;
-    uint64_t bits = __ldg(reinterpret_cast<const unsigned long long*>(a.masks) +
-                          ((size_t)p * 2 * a.k + mb.y) * a.W + tl.ct);
+    const size_t at = ((size_t)p * 2 * a.k + mb.y) * a.W + tl.ct;
+    uint64_t bits = __ldg(reinterpret_cast<const unsigned long long*>(a.masks) + at);
+    // carrying over a smaller eps's union-find, only edges that are new (a new
+    // pair, or an endpoint that just became core) can join components
+    if (a.carry && a.coreEps[p] != a.round)
+        bits &= __ldg(reinterpret_cast<const unsigned long long*>(a.newMasks) + at) | newCoreCand;
     if (!bits) return;
     int rp = find_root(a.parent, p);
     while (bits) {
@@ -190,7 +200,7 @@ __global__ void k_labels(ClusterArgs a) {
 int launch_cluster(const ClusterArgs& a, cudaStream_t st) {
     int launches = 0;
     const int g = (a.n + 255) / 256;
-    k_init<<<g, 256, 0, st>>>(a.parent, a.border, a.n);
+    k_init<<<g, 256, 0, st>>>(a.parent, a.border, a.n, a.carry && a.round > 0);
     ++launches;
     k_union_tiles<<<(unsigned)a.nTiles, 128, 0, st>>>(a);
     ++launches;

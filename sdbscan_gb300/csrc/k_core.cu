@@ -176,8 +176,16 @@ __device__ __forceinline__ int visit_point(const CoreArgs& a, uint32_t* km, cons
                     fresh[half] = __ballot_sync(0xffffffffu, isFirst);
                 }
             }
-            if (firstOut && lane == 0)
-                firstOut[((size_t)p * slots + jj) * a.W + wd] = ((uint64_t)fresh[1] << 32) | fresh[0];
+            if (firstOut && lane == 0) {
+                const size_t at = ((size_t)p * slots + jj) * a.W + wd;
+                const uint64_t f64 = ((uint64_t)fresh[1] << 32) | fresh[0];
+                if (a.accumulate) {
+                    firstOut[at] |= f64;
+                    a.newMasks[at] = f64;
+                } else {
+                    firstOut[at] = f64;
+                }
+            }
         }
     }
     __syncwarp();
@@ -269,6 +277,15 @@ __global__ void k_core_emit(CoreArgs a, const int4* __restrict__ sig, const int6
 __global__ void k_core_finish(CoreArgs a) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= a.n) return;
+    if (a.accumulate) {  // this round's pairs are new neighbours: the degree grows
+        const int deg = a.degree[p] + a.aCount[p] + a.inRaw[p];
+        a.degree[p] = deg;
+        if (!a.core[p] && deg >= a.minPts - 1) {
+            a.core[p] = 1;
+            a.coreEps[p] = a.round;
+        }
+        return;
+    }
     const int deg = a.aCount[p] + a.inRaw[p];
     a.degree[p] = deg;
     a.core[p] = deg >= a.minPts - 1 ? 1 : 0;

@@ -275,7 +275,8 @@ __global__ void k_masks_from_dists(DistArgs a) {
             bool pass = false;
             if (c < a.m) {
                 const int cp = __ldg(cand + c);
-                pass = cp != p && __ldg(a.dists + ((size_t)p * 2 * a.k + slot) * a.m + c) <= a.eps;
+                const float dd = __ldg(a.dists + ((size_t)p * 2 * a.k + slot) * a.m + c);
+                pass = cp != p && dd <= a.eps && dd > a.epsLo;
                 if (pass) {
                     atomicAdd(&colCount[col], 1);
                     ++myPass;

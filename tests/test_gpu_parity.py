@@ -267,7 +267,7 @@ def test_eps_sweep_equals_separate_fits(precision):
     sweep's distances are BF16-screened (exact re-decision near every eps)."""
     from sdbscan_gb300 import capi, datasets
     X, _ = datasets.cfg2_mnist_like(8000, 196, seed=81)
-    eps_list = [0.15, 0.2, 0.25, 0.3]
+    eps_list = [0.25, 0.15, 0.3, 0.2, 0.25]  # unsorted, with a repeat: rounds run in ascending eps
     eng = capi.Engine(*X.shape)
     eng.set_params(n_proj=512, topK=8, topM=40, distance="Cosine", random_seed=19, precision=precision)
     labels, ncl = eng.fit_sdbscan_sweep(X, eps_list, 20)
