@@ -25,7 +25,6 @@
 // bounded) for the loads it issued, frees its tensor memory and returns; the
 // host then runs the FP32 kernel instead (launch_rff with the flag as gate).
 #include <cuda.h>
-#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -160,32 +159,6 @@ __global__ void __launch_bounds__(NT, 2) k_rff_tc(const __grid_constant__ CUtens
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
-    return fn;
-}
-
-// rows x ldb BF16 matrix (row stride ldb elements), box of 64 x boxRows, 128-byte swizzle.
-bool encode_bf16(CUtensorMap* m, const void* ptr, int rows, int ldb, int boxRows) {
-    auto fn = encode_fn();
-    if (!fn) return false;
-    const cuuint64_t dims[2] = {(cuuint64_t)ldb, (cuuint64_t)rows};
-    const cuuint64_t strides[1] = {(cuuint64_t)ldb * 2};
-    const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)boxRows};
-    const cuuint32_t estr[2] = {1, 1};
-    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
-              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
 }  // namespace
 
 // Xs: n x 2 ldb BF16 points ([hi | lo] per row), Rs: h x 2 ldb BF16 rows of R
@@ -194,7 +167,8 @@ bool encode_bf16(CUtensorMap* m, const void* ptr, int rows, int ldb, int boxRows
 int launch_rff_tc(const void* Xs, const void* Rs, int n, int h, int ldb, float* E, int32_t* err, cudaStream_t st) {
     if (ldb % BK != 0 || (reinterpret_cast<uintptr_t>(Xs) & 15) || (reinterpret_cast<uintptr_t>(Rs) & 15)) return -1;
     CUtensorMap tmX, tmR;
-    if (!encode_bf16(&tmX, Xs, n, 2 * ldb, BM) || !encode_bf16(&tmR, Rs, h, 2 * ldb, BN)) return -1;
+    if (!tc::encode_bf16_2d(&tmX, Xs, n, 2 * ldb, BK, BM) || !tc::encode_bf16_2d(&tmR, Rs, h, 2 * ldb, BK, BN))
+        return -1;
     const size_t sm = (size_t)STAGES * STAGE_BYTES + 1024;
     if (cudaFuncSetAttribute(k_rff_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return -1;
