@@ -73,7 +73,11 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
     extern __shared__ __align__(1024) unsigned char smraw[];
     __shared__ uint64_t bars[STAGES];
     __shared__ uint32_t tmemBase;
-    __shared__ int rowPoint[TM], rowSlot[TM], colPoint[TN], colCount[TN];
+    // tile ids: the next tile's are loaded under this tile's epilogue, which
+    // by then holds its own row's ids in registers (column ids by tile
+    // parity); kept small so three CTAs still share an SM's shared memory
+    __shared__ int rowPoints[TM], colPoints[2][TN], colCount[TN];
+    __shared__ uint8_t rowSlots[TM];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t base = (smem_u32(smraw) + 1023u) & ~1023u;  // 1024-aligned operand tiles
@@ -96,7 +100,10 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
     const int nk = ldb / TKB;
     const int64_t total = *a.tileTotal;
 
-    for (int64_t t = blockIdx.x; t < total; t += gridDim.x) {
+    // The next tile's ids and first STAGES - 1 stages are loaded before the
+    // current tile's epilogue (its MMAs are done by then), so the gathers
+    // overlap the epilogue.
+    auto load_meta = [&](int64_t t, int b) {
         const int l = a.tileList[t];
         const int64_t ti = t - a.tileOff[l];
         const int mt = (int)(ti / a.nct), ct = (int)(ti % a.nct);
@@ -107,44 +114,53 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
             const int64_t q = mbeg + i;
             if (q < mend) {
                 const int2 mb = a.members[q];
-                rowPoint[i] = mb.x;
-                rowSlot[i] = mb.y;
+                rowPoints[i] = mb.x;
+                rowSlots[i] = (uint8_t)mb.y;
             } else {
-                rowPoint[i] = -1;
-                rowSlot[i] = 0;
+                rowPoints[i] = -1;
+                rowSlots[i] = 0;
             }
         }
         for (int j = tid; j < TN; j += NT) {
             const int c = ct * TN + j;
-            colPoint[j] = c < a.m ? cand[c] : -1;
-            colCount[j] = 0;
+            colPoints[b][j] = c < a.m ? cand[c] : -1;
         }
-        __syncthreads();
-
-        auto load_stage = [&](int stage, int kc) {
-            const uint32_t sA = base + stage * STAGE_BYTES, sB = sA + A_BYTES;
-            const int k0 = kc * TKB;
+    };
+    auto load_stage = [&](int b, int stage, int kc) {
+        const uint32_t sA = base + stage * STAGE_BYTES, sB = sA + A_BYTES;
+        const int k0 = kc * TKB;
 #pragma unroll
-            for (int it = 0; it < (TM * 8) / NT; ++it) {  // 8 per thread
-                const int idx = tid + it * NT, row = idx >> 3, c = idx & 7;
-                const int p = rowPoint[row];
-                const bool ok = p >= 0;
-                cp_async16(sA + sw128(row, c), ok ? Xb + (size_t)p * ldb + k0 + c * 8 : Xb, ok);
-            }
+        for (int it = 0; it < (TM * 8) / NT; ++it) {  // 8 per thread
+            const int idx = tid + it * NT, row = idx >> 3, c = idx & 7;
+            const int p = rowPoints[row];
+            const bool ok = p >= 0;
+            cp_async16(sA + sw128(row, c), ok ? Xb + (size_t)p * ldb + k0 + c * 8 : Xb, ok);
+        }
 #pragma unroll
-            for (int it = 0; it < (TN * 8) / NT; ++it) {  // 4 per thread
-                const int idx = tid + it * NT, row = idx >> 3, c = idx & 7;
-                const int p = colPoint[row];
-                const bool ok = p >= 0;
-                cp_async16(sB + sw128(row, c), ok ? Xb + (size_t)p * ldb + k0 + c * 8 : Xb, ok);
-            }
-        };
-
-        // prologue
+        for (int it = 0; it < (TN * 8) / NT; ++it) {  // 4 per thread
+            const int idx = tid + it * NT, row = idx >> 3, c = idx & 7;
+            const int p = colPoints[b][row];
+            const bool ok = p >= 0;
+            cp_async16(sB + sw128(row, c), ok ? Xb + (size_t)p * ldb + k0 + c * 8 : Xb, ok);
+        }
+    };
+    auto prologue = [&](int b) {
         for (int s = 0; s < STAGES - 1; ++s) {
-            if (s < nk) load_stage(s, s);
+            if (s < nk) load_stage(b, s, s);
             asm volatile("cp.async.commit_group;\n" ::);
         }
+    };
+    for (int j = tid; j < TN; j += NT) colCount[j] = 0;  // re-zeroed after each tile's use
+    if ((int64_t)blockIdx.x < total) {
+        load_meta(blockIdx.x, 0);
+        __syncthreads();
+        prologue(0);
+    }
+
+    int tb = 0;  // parity of the current tile's buffers
+    for (int64_t t = blockIdx.x; t < total; t += gridDim.x, tb ^= 1) {
+        const int ct = (int)((t - a.tileOff[a.tileList[t]]) % a.nct);
+        const int* colPoint = colPoints[tb];
         for (int kc = 0; kc < nk; ++kc) {
             const int stage = kc % STAGES;
             asm volatile("cp.async.wait_group %0;\n" ::"n"(STAGES - 2));
@@ -165,7 +181,7 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
                     if (!mbar_wait(smem_u32(&bars[ns]), (phaseBits >> ns) & 1u)) timedOut = true;
                     phaseBits ^= 1u << ns;
                 }
-                load_stage(ns, nxt);
+                load_stage(tb, ns, nxt);
             }
             asm volatile("cp.async.commit_group;\n" ::);
         }
@@ -177,10 +193,17 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
         }
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-
         // epilogue: thread tid owns row tid
         const int row = tid;
-        const int p = rowPoint[row];
+        const int p = rowPoints[row];
+        const int mySlot = rowSlots[row];
+        const int64_t tn = t + gridDim.x;
+        if (tn < total) {  // the next tile's gathers start now, under this tile's epilogue
+            __syncthreads();  // every thread holds its row's ids
+            load_meta(tn, tb ^ 1);
+            __syncthreads();
+            prologue(tb ^ 1);
+        }
         uint64_t bits = 0;
         int nPass = 0;
 #pragma unroll 1
@@ -199,7 +222,7 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
                 if (p >= 0 && q >= 0) {
                     const float dist = 1.0f - v[j];
                     if constexpr (SWEEP) {  // keep the screened distance, re-decide near any eps
-                        a.dists[((size_t)p * 2 * a.k + rowSlot[row]) * a.m + ct * TN + col] = dist;
+                        a.dists[((size_t)p * 2 * a.k + mySlot) * a.m + ct * TN + col] = dist;
                         if (p != q)
                             for (int e = 0; e < a.nSweep; ++e) unsure |= fabsf(dist - a.sweepEps[e]) <= kMargin;
                     } else if (p != q) {
@@ -216,7 +239,7 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
                     if (unsure) {
                         const unsigned long long at = at0 + __popc(um & ((1u << lane) - 1u));
                         if ((int64_t)at < qcap)
-                            queue[at] = ((uint64_t)(uint32_t)p << 32) | ((uint32_t)rowSlot[row] << 16) |
+                            queue[at] = ((uint64_t)(uint32_t)p << 32) | ((uint32_t)mySlot << 16) |
                                         (uint32_t)(ct * TN + col);
                         else
                             atomicExch(err, 2);
@@ -230,13 +253,16 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
                 if (lane == 0 && b) atomicAdd(&colCount[col], __popc(b));
             }
         }
-        if (!SWEEP && p >= 0) a.masks[((size_t)p * 2 * a.k + rowSlot[row]) * a.W + ct] = bits;
+        if (!SWEEP && p >= 0) a.masks[((size_t)p * 2 * a.k + mySlot) * a.W + ct] = bits;
         const int wp = warp_sum(nPass);
         if (lane == 0 && wp) atomicAdd(a.pairs, (unsigned long long)wp);
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
         __syncthreads();
         for (int j = tid; j < TN; j += NT)
-            if (colCount[j]) atomicAdd(a.inRaw + colPoint[j], colCount[j]);
+            if (colCount[j]) {
+                atomicAdd(a.inRaw + colPoint[j], colCount[j]);
+                colCount[j] = 0;
+            }
         // a timed-out wait anywhere in the CTA ends the CTA's work (uniformly)
         if (__syncthreads_or(timedOut ? 1 : 0)) {
             if (tid == 0) atomicExch(err, 1);
