@@ -43,7 +43,11 @@ typedef enum { SDB_COSINE = 0, SDB_L1 = 1, SDB_L2 = 2, SDB_CHI2 = 3, SDB_JS = 4 
 
 typedef enum {
     SDB_PREC_FP32 = 0,      /* plain FP32: results identical to the reference's CPU path */
-    SDB_PREC_BF16 = 1       /* BF16 tensor-core screening + FP32 re-decision near eps    */
+    SDB_PREC_BF16 = 1       /* Cosine: BF16 tensor-core screening of the candidate
+                               distances + exact FP32 re-decision near eps (labels
+                               identical to FP32); L1/L2: the random-Fourier embedding
+                               GEMM on the tensor cores in split BF16.  sOPTICS fits
+                               and other distances run as FP32. */
 } sdb_precision;
 
 /* Parameters of sDbscan::set_params (src/sDbscan.h:79-108), same meaning and
@@ -101,7 +105,11 @@ sdb_status sdb_fit_soptics_device(sdb_engine* e, const float* X_device, float ep
  * once, then core points and clusters for every eps in eps[0..n_eps).
  * labels: n_eps x n_points int32 (row i for eps[i]); n_clusters: n_eps.  The
  * reference derives its list as eps + i * rangeEps and writes each labelling
- * to a file; here the caller passes the list and gets the labellings back. */
+ * to a file; here the caller passes the list (any order, repeats allowed) and
+ * gets the labellings back.  The eps values are processed in ascending order,
+ * each adding only its new pairs; every labelling equals a separate
+ * fit_sDbscan at that eps.  BF16 precision screens the distances once for all
+ * eps values (up to 16; longer lists run FP32). */
 sdb_status sdb_fit_sdbscan_sweep(sdb_engine* e, const float* X_host, const float* eps, int32_t n_eps, int32_t minPts,
                                  int32_t* labels, int32_t* n_clusters);
 
@@ -155,6 +163,8 @@ const char* sdb_last_error(sdb_engine* e);
 /* Many independent datasets, each with the same eps sweep, recorded once into
  * one CUDA graph and replayed with a single launch.  No reference counterpart
  * (the reference runs test_sDbscan per dataset, src/sDbscan.cpp:980-1039).
+ * p->precision applies to every set (BF16: screened distances, labels equal
+ * to FP32).
  *   X_device[i]: d_i x n_i column-major data of set i, device memory, kept
  *                valid for the batch's lifetime
  * The batch plans every set once (sizing run), then times graphs with 4, 8,
