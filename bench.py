@@ -293,21 +293,37 @@ def run_batched(args, local, cpu=True):
                           "labels_identical_to_graph": fits_identical,
                           "form": "512 separate fit_sDbscan calls on device-resident data"},
            "n_clusters_eps0.20_first4": [plabels[i][3][1] for i in range(4)]}
-    if cpu:
-        out["cpu_baseline"] = _cpu_batched(sets, eps_list, params)
+    if cpu:  # in a fresh process, like the reference arm
+        out["cpu_baseline"] = _subprocess_json([sys.executable, os.path.abspath(__file__), "--impl", "reference",
+                                                "--batched-cpu"])
     return out
 
 
-def _cpu_batched(sets, eps_list, params, n_sets=6):
-    """The oracle on the smallest n_sets datasets of the batch, all host
-    threads: separate fit_sDbscan calls per eps, and the reference's own
-    index-once sweep (test_sDbscan).  Rates in point-clusterings/s."""
+def _subprocess_json(cmd):
+    """Runs cmd and returns the JSON object of its last output line (None on failure)."""
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=900, env=dict(os.environ, WORLD_SIZE="1",
+                                                                                      RANK="0", LOCAL_RANK="0"))
+        line = [x for x in r.stdout.strip().splitlines() if x.startswith("{")][-1]
+        return json.loads(line)
+    except Exception:
+        return None
+
+
+def _cpu_batched(n_sets=6):
+    """The oracle on the n_sets smallest datasets of the config-5 law (numpy
+    generator), all host threads: separate fit_sDbscan calls per eps, and the
+    reference's own index-once sweep (test_sDbscan).  Point-clusterings/s."""
     from oracle.oracle import Port, build_port
+    from sdbscan_gb300 import datasets
     build_port()
     port = Port()
     threads = os.cpu_count() or 1
+    sets = datasets.cfg5_batch(64, seed=5007)
+    eps_list = [0.05 * (i + 1) for i in range(8)]
+    params = dict(n_proj=1024, topK=5, topM=50, distance="Cosine", random_seed=42)
     order = sorted(range(len(sets)), key=lambda i: sets[i][0].shape[0])[:n_sets]
-    Xs = [sets[i][0].cpu().numpy() for i in order]
+    Xs = [sets[i][0] for i in order]
     kw = dict(dist=params["distance"], n_proj=params["n_proj"], topK=params["topK"], topM=params["topM"],
               seed=params["random_seed"], threads=threads)
     pts = sum(X.shape[0] for X in Xs) * len(eps_list)
@@ -478,15 +494,12 @@ def run_ours(args, cfg):
     stages = {k_: v_ / args.steps for k_, v_ in stage_sum.items()}
     cpu = None
     if ws == 1 and not args.no_cpu:
-        # the same bounded sample the reference arm times: ns points drawn
-        # from the workload's law by the numpy generator
-        ns = min(args.cpu_sample, n)
-        Xs = _host_data(cfg, ns)
-        rate, threads, dt = _cpu_sample_rate(Xs, cfg, ns, kp)
-        cpu = {"value": rate, "unit": "points/s", "cores": threads, "kind": "port",
-               "sample": f"full fit_{'sOptics' if optics else 'sDbscan'} on {ns} points drawn from the "
-                         f"workload's law (numpy generator, seed {cfg['seed']}; oracle/ restatement, OpenMP, "
-                         f"{threads} threads, {dt:.1f} s)"}
+        # the reference arm itself, in a fresh process (this one holds
+        # torch's OpenMP runtime, whose spinning threads would share the cores)
+        ref = _subprocess_json([sys.executable, os.path.abspath(__file__), "--impl", "reference", "--config",
+                                str(args.config), "--steps", "2", "--warmup", "1", "--cpu-sample",
+                                str(args.cpu_sample)])
+        cpu = ref.get("cpu_baseline") if ref else None
     line = {
         "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -532,8 +545,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-bf16", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-cpu", action="store_true", help="(reference arm) time the config-5 CPU baseline only")
     args = ap.parse_args()
     cfg = WORKLOADS[args.config]
+    if args.impl == "reference" and args.batched_cpu:
+        print(json.dumps(_cpu_batched()))
+        return 0
     if args.impl == "reference":
         return run_reference(args, cfg)
     return run_ours(args, cfg)
