@@ -169,8 +169,9 @@ class Port:
 
     # whole fits ----------------------------------------------------------------
     def fit_sdbscan(self, X, eps, minPts, *, dist="Cosine", n_proj=1024, topK=10, topM=50, ker=1024,
-                    sigma=1.0, L=0.4, seed=42, threads=-1):
-        """The reference's fit_sDbscan restated (src/sDbscan.cpp:830-890)."""
+                    sigma=1.0, L=0.4, seed=42, threads=-1, clusterNoise=0, samplingProb=0.01):
+        """The reference's fit_sDbscan restated (src/sDbscan.cpp:830-890), with its
+        sDbscan-1NN noise labelling for clusterNoise = 1 (seeded sampling)."""
         X = np.ascontiguousarray(X, np.float32)
         n, d = X.shape
         ker = d if dist == "Cosine" else ker
@@ -182,6 +183,7 @@ class Port:
         times = np.zeros(5, np.float64)
         ncl = self.L.orc_fit_sdbscan(_p(X), _i(n), _i(d), _i(DIST_CODES[dist]), _i(n_proj), _i(topK), _i(topM),
                                      _i(ker), _f(L), _p(R), _p(bits), _i(fd), _f(eps), _i(minPts), _i(threads),
+                                     _i(clusterNoise), _f(samplingProb), ctypes.c_uint32(seed & 0xFFFFFFFF),
                                      _p(labels), _p(core), _p(times))
         if ncl < 0:
             raise ValueError(f"transform rejected the input (code {-ncl})")
@@ -206,6 +208,17 @@ class Port:
         if r < 0:
             raise ValueError(f"transform rejected the input (code {-r})")
         return labels, ncl, times
+
+    def label_noise(self, P, topK, core, labels, samplingProb, seed):
+        """labelNoise (clusterNoise = 1, src/sDbscan.cpp:648-807) on given projections,
+        top-k rows, core flags and labels (returns the new labels)."""
+        P = np.ascontiguousarray(P, np.float32)
+        n, nproj = P.shape
+        out = np.ascontiguousarray(labels, np.int32).copy()
+        self.L.orc_label_noise(_p(P), _i(n), _i(nproj), _p(np.ascontiguousarray(topK, np.int32)),
+                               _i(topK.shape[1] // 2), _p(np.ascontiguousarray(core, np.uint8)), _f(samplingProb),
+                               ctypes.c_uint32(seed & 0xFFFFFFFF), _p(out))
+        return out
 
     def fit_soptics(self, X, eps, minPts, *, dist="Cosine", n_proj=1024, topK=10, topM=50, ker=1024,
                     sigma=1.0, L=0.4, seed=42, threads=-1, tie_mode=1):

@@ -501,13 +501,68 @@ int64_t orc_form_optics(int n, const uint8_t* core, const float* coreDist, const
     return no;
 }
 
+// ---- sDbscan-1NN noise labelling (labelNoise, src/sDbscan.cpp:648-807) ------
+// clusterNoise == 1: every point left as noise takes the label of the sampled
+// core point whose projections best match its top-k vectors: the estimate
+// sum_k P[c][close_k] - P[c][far_k] (accumulated in that order, :786-793), the
+// first maximum over the sampled cores in ascending index order (:798-806).
+// The cores are sampled with probability fProb = samplingProb n / #cores when
+// #cores >= samplingProb n (:683-699).  The reference draws with the unseeded
+// rand(); here point p is sampled iff fmix32(seed + 0x9E3779B9 (p + 1)) 2^-32
+// <= fProb (MurmurHash3's 32-bit finaliser), the engine's rule.
+static inline uint32_t fmix32(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+
+void orc_label_noise(const float* P, int n, int nproj, const int* topK, int k, const uint8_t* core,
+                     float samplingProb, uint32_t seed, int32_t* labels) {
+    int numCore = 0;
+    for (int p = 0; p < n; ++p) numCore += core[p] ? 1 : 0;
+    float fProb = 1.0f;
+    if ((float)numCore >= samplingProb * (float)n) fProb = samplingProb * (float)n / (float)numCore;
+    std::vector<int> cores;
+    for (int p = 0; p < n; ++p) {
+        if (!core[p]) continue;
+        const double u = (double)fmix32(seed + 0x9E3779B9u * (uint32_t)(p + 1)) * (1.0 / 4294967296.0);
+        if (fProb == 1.0f || u <= (double)fProb) cores.push_back(p);
+    }
+    if (cores.empty()) return;  // no cluster to join (the reference indexes labels_[-1] here)
+    std::vector<int32_t> base(labels, labels + n);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int x = 0; x < n; ++x) {
+        if (base[x] != -1) continue;
+        const int* tk = topK + (size_t)x * 2 * k;
+        float best = -2147483648.0f;  // NEG_INF (Header.h:20)
+        int bestCore = -1;
+        for (int c : cores) {
+            const float* pc = P + (size_t)c * nproj;
+            float v = 0.0f;
+            for (int j = 0; j < k; ++j) {
+                v += pc[tk[j]];
+                v -= pc[tk[j + k]];
+            }
+            if (v > best) {
+                best = v;
+                bestCore = c;
+            }
+        }
+        if (bestCore >= 0) labels[x] = base[bestCore];
+    }
+}
+
 // ---- whole fits, for the CPU baseline (src/sDbscan.cpp:830-890, 1711-1769) ---
 // X: d x n column-major, not modified.  bits: 3*fhtDim; R may be null unless
 // L1/L2.  times[5]: transform, index, core, cluster/optics, total (seconds).
 // Returns n_clusters_ (fit_sdbscan) or 0, or a negative transform error.
 int orc_fit_sdbscan(const float* X, int n, int d, int code, int nproj, int k, int m, int ker, float L,
                     const float* R, const uint8_t* bits, int fhtDim, float eps, int minPts, int threads,
-                    int32_t* labels, uint8_t* core, double* times) {
+                    int clusterNoise, float samplingProb, uint32_t seed, int32_t* labels, uint8_t* core,
+                    double* times) {
     if (threads > 0) omp_set_num_threads(threads);
     Timer tm, all;
     std::vector<float> Xc(X, X + (size_t)n * d);
@@ -519,7 +574,7 @@ int orc_fit_sdbscan(const float* X, int n, int d, int code, int nproj, int k, in
     orc_project(Xc.data(), n, d, code, ker, L, R, bits, fhtDim, nproj, P.data());
     orc_topk(P.data(), n, nproj, k, topK.data());
     orc_topm(P.data(), n, nproj, m, topM.data());
-    std::vector<float>().swap(P);
+    if (clusterNoise != 1) std::vector<float>().swap(P);
     times[1] = tm.lap();
     std::vector<int32_t> deg(n);
     orc_find_core(Xc.data(), n, d, code, topK.data(), k, topM.data(), m, eps, minPts, 0, 0, core, deg.data());
@@ -528,6 +583,7 @@ int orc_fit_sdbscan(const float* X, int n, int d, int code, int nproj, int k, in
     std::vector<int32_t> idx(orc_neighbors_total(n));
     orc_neighbors_export(n, off.data(), idx.data(), nullptr);
     const int ncl = orc_form_cluster(n, core, off.data(), idx.data(), labels);
+    if (clusterNoise == 1) orc_label_noise(P.data(), n, nproj, topK.data(), k, core, samplingProb, seed, labels);
     times[3] = tm.lap();
     times[4] = all.lap();
     orc_graph_free();

@@ -286,4 +286,24 @@ struct ClusterArgs {
 };
 int launch_cluster(const ClusterArgs& a, cudaStream_t st);
 
+// sDbscan-1NN noise labelling (clusterNoise = 1), after the cluster labels.
+struct NoiseArgs {
+    int n, nproj, k;
+    const float* P;          // n x nproj projections
+    const int32_t* topK;     // n x 2k
+    const uint8_t* core;
+    int32_t* labels;         // in/out
+    float samplingProb;
+    uint32_t seed;
+    int sMax;                // capacity of the sampled-core list
+    int64_t* sampleFlag;     // n + 1 (scanned into indices)
+    int64_t* noiseFlag;      // n + 1
+    int32_t* cores;          // sMax: sampled core point ids, ascending
+    int32_t* noise;          // n: noise point ids
+    float* PcT;              // nproj x sMax
+    int32_t* numCore;        // device scalar
+    int64_t* scanTmp;
+};
+int launch_label_noise(const NoiseArgs& a, cudaStream_t st);
+
 }  // namespace sdb

@@ -96,7 +96,8 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &listOff, &listFill, &members, &tileOff, &tileList, &hubCount, &hubOff, &hubLists, &masks, &inRaw,
             &aCount, &degree, &core, &parent, &border, &rootFlag, &labels, &nClusters, &scanTmp, &errFlags,
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
-            &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig, &Rb, &newMasks, &coreEps};
+            &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig, &Rb, &newMasks, &coreEps, &sampleFlag,
+            &noiseFlag, &noiseCores, &noisePts, &PcT, &numCore};
 }
 
 // ---------------------------------------------------------------------------
@@ -108,7 +109,8 @@ sdb_status sdb_engine::derive() {
     if (p.topK > p.n_proj) return fail(SDB_ERR_ARG, "topK must be <= n_proj");
     if (p.topM > n) return fail(SDB_ERR_ARG, "topM must be <= n_points");
     if (p.distance < SDB_COSINE || p.distance > SDB_JS) return fail(SDB_ERR_ARG, "unknown distance");
-    if (p.clusterNoise != 0) return fail(SDB_ERR_ARG, "clusterNoise != 0 (sDbscan-1NN noise labelling) is not supported");
+    if (p.clusterNoise < 0 || p.clusterNoise > 2)
+        return fail(SDB_ERR_ARG, "clusterNoise must be 0, 1 (sDbscan-1NN) or 2 (neighbour heuristic)");
     if (p.precision != SDB_PREC_FP32 && p.precision != SDB_PREC_BF16) return fail(SDB_ERR_ARG, "unknown precision");
     ker = p.distance == SDB_COSINE ? d : p.ker_n_features;  // src/sDbscan.h:102-104
     if (ker < 1) return fail(SDB_ERR_ARG, "ker_n_features must be >= 1");
@@ -543,6 +545,33 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
             ka.coreEps = i32(coreEps);
         }
         L_(launch_cluster(ka, st));
+        if (p.clusterNoise == 1) {  // sDbscan-1NN labels for the points left as noise
+            const float sp = p.samplingProb;
+            const int sMax = (int)std::min<double>((double)n, 2.0 * std::max(0.0f, sp) * n + 4096.0);
+            if (!ensure(sampleFlag, sizeof(int64_t) * (n + 1)) || !ensure(noiseFlag, sizeof(int64_t) * (n + 1)) ||
+                !ensure(noiseCores, sizeof(int32_t) * sMax) || !ensure(noisePts, sizeof(int32_t) * n) ||
+                !ensure(PcT, sizeof(float) * (size_t)D * sMax) || !ensure(numCore, sizeof(int32_t)))
+                return SDB_ERR_NOMEM;
+            NoiseArgs na{};
+            na.n = n;
+            na.nproj = D;
+            na.k = k;
+            na.P = f32(P);
+            na.topK = i32(topK);
+            na.core = static_cast<const uint8_t*>(core.ptr);
+            na.labels = i32(labels);
+            na.samplingProb = sp;
+            na.seed = (uint32_t)seedUsed;
+            na.sMax = sMax;
+            na.sampleFlag = i64(sampleFlag);
+            na.noiseFlag = i64(noiseFlag);
+            na.cores = i32(noiseCores);
+            na.noise = i32(noisePts);
+            na.PcT = f32(PcT);
+            na.numCore = i32(numCore);
+            na.scanTmp = i64(scanTmp);
+            L_(launch_label_noise(na, st));
+        }
         if (!ok) return fail(SDB_ERR_CUDA, std::string("cluster launch failed: ") + cudaGetErrorString(cudaGetLastError()));
     } else {
         s = optics_stage(ca, launches);

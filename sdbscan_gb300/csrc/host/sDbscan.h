@@ -8,7 +8,9 @@
 //    Eigen::Ref<const MatrixXf> carries) instead of an Eigen reference;
 //  - invalid input throws std::runtime_error where the reference prints and
 //    calls exit(1) (src/Utilities.h:308-324);
-//  - only clusterNoise = 0 is supported (the reference's default).
+//  - clusterNoise = 1 (sDbscan-1NN) samples core points with a seeded rule
+//    instead of the reference's unseeded rand(); every core point is taken
+//    when samplingProb n exceeds their number, as in the reference.
 #pragma once
 
 #include <cstdint>

@@ -6,7 +6,7 @@ one thread on small seeded inputs, and stores inputs and outputs as
 compressed ``.npz`` files.  Run on the development machine where the
 reference sources exist:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fixture names...]
 
 The fixtures are what pins the oracle (and through it the GPU engine) to the
 reference on machines where the reference cannot be built.
@@ -59,12 +59,22 @@ def cases():
     yield "cosine_tiny_60x12", X8, dict(n_proj=16, topK=1, topM=50, distance="Cosine"), 0.3, 3, False
     X9, _ = ds.cfg1_cosine(3000, 64, seed=19)
     yield "cosine_k1_m1_3000x64", X9, dict(n_proj=1024, topK=1, topM=1, distance="Cosine"), 0.2, 2, False
+    # sDbscan-1NN noise labelling; samplingProb = 1 takes every core point, so
+    # the reference's unseeded rand() is never consulted
+    yield "cosine_noise1nn_2000x32", X1, dict(n_proj=256, topK=5, topM=20, distance="Cosine", clusterNoise=1,
+                                               samplingProb=1.0), 0.12, 12, False
+    X10, _ = ds.cfg4_dirichlet(1500, 64, n_comp=5, conc=10, seed=24)  # wider histograms: a third left as noise
+    yield "chi2_noise1nn_1500x64", X10, dict(n_proj=256, topK=5, topM=20, distance="Chi2", ker_n_features=512,
+                                              clusterNoise=1, samplingProb=1.0), 0.2, 12, False
 
 
-def main():
+def main(only=()):
+    """Writes every fixture, or only the named ones."""
     if build_ref() is None:
         sys.exit("the reference sources are not available here; fixtures cannot be regenerated")
     for name, X, params, eps, minPts, optics in cases():
+        if only and name not in only:
+            continue
         n, d = X.shape
         r = Ref(n, d)
         r.set_params(**params, n_threads=1, random_seed=7)
@@ -90,4 +100,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

@@ -35,6 +35,9 @@ def _engine(X, meta):
         kw["ker_n_features"] = meta["ker_n_features"]
     if "ker_sigma" in meta:
         kw["ker_sigma"] = meta["ker_sigma"]
+    for key in ("clusterNoise", "samplingProb"):
+        if key in meta:
+            kw[key] = meta[key]
     eng.set_params(**kw)
     return eng
 
@@ -334,3 +337,28 @@ def test_bf16_rff_embedding_on_tensor_cores():
     rel = np.abs(P1 - P0) / np.linalg.norm(P0, axis=1, keepdims=True)
     assert rel.max() < 2e-3, rel.max()
     assert adjusted_rand_score(out[0][0], out[1][0]) >= 0.99
+
+
+def test_noise_labelling_sampled_matches_oracle(port):
+    """clusterNoise = 1 with sampling (samplingProb n < #cores): the engine and
+    the oracle draw the same cores (seeded rule) and label every noise point
+    the same way; no noise point is left when a cluster exists."""
+    from sdbscan_gb300 import capi, datasets
+    X, _ = datasets.cfg2_mnist_like(12000, 64, seed=77)
+    kw = dict(n_proj=512, topK=6, topM=40, distance="Cosine", random_seed=31)
+    eps, minPts, sp = 0.08, 25, 0.02
+    eng = capi.Engine(*X.shape)
+    eng.set_params(clusterNoise=0, **kw)
+    eng.fit_sdbscan(X, eps, minPts)
+    plain, _ = eng.labels()
+    core, _ = eng.core()
+    assert (plain == -1).sum() > 500 and core.sum() > sp * X.shape[0]  # sampling is exercised
+    eng.set_params(clusterNoise=1, samplingProb=sp, **kw)
+    eng.fit_sdbscan(X, eps, minPts)
+    labels, ncl = eng.labels()
+    want, ncl_o, _, _ = port.fit_sdbscan(X, eps, minPts, dist="Cosine", n_proj=512, topK=6, topM=40, seed=31,
+                                         clusterNoise=1, samplingProb=sp)
+    np.testing.assert_array_equal(labels, want)
+    assert ncl == ncl_o
+    np.testing.assert_array_equal(labels[plain >= 0], plain[plain >= 0])
+    assert (labels == -1).sum() == 0

@@ -65,6 +65,8 @@ def test_oracle_matches_reference_fixture(port, path):
     else:
         np.testing.assert_array_equal(deg[core == 1], z["core_degree"][core == 1])
         labels, ncl = port.form_cluster(core, off, idx)
+        if meta.get("clusterNoise", 0) == 1:  # sDbscan-1NN (samplingProb 1: every core point)
+            labels = port.label_noise(P, topK, core, labels, meta["samplingProb"], meta["random_seed"])
         np.testing.assert_array_equal(labels, z["labels"])
         assert ncl == int(z["n_clusters"])
     port.graph_free()
@@ -103,3 +105,16 @@ def test_oracle_sweep_equals_separate_fits(port):
         l1, n1, _, _ = port.fit_sdbscan(X, e, 20, n_proj=256, topK=5, topM=30, seed=4)
         np.testing.assert_array_equal(labels[i], l1)
         assert ncl[i] == n1
+
+
+@pytest.mark.parametrize("name", ["cosine_noise1nn_2000x32", "chi2_noise1nn_1500x64"])
+def test_whole_fit_noise_labelling_matches_reference(port, name):
+    """fit_sDbscan with clusterNoise = 1 (labelNoise, src/sDbscan.cpp:648-807):
+    noise points take the labels the reference's sDbscan-1NN gives them."""
+    z, meta = _load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    labels, ncl, core, _ = port.fit_sdbscan(z["X"], meta["eps"], meta["minPts"], dist=meta["distance"],
+                                            n_proj=meta["n_proj"], topK=meta["topK"], topM=meta["topM"],
+                                            ker=meta.get("ker_n_features", 1024), seed=7, threads=4,
+                                            clusterNoise=1, samplingProb=meta["samplingProb"])
+    np.testing.assert_array_equal(labels, z["labels"])
+    assert ncl == int(z["n_clusters"])
