@@ -205,6 +205,8 @@ struct DistArgs {
     int nct;              // candidate tiles per list
     float eps;
     float epsLo;          // eps sweeps: k_masks_from_dists keeps epsLo < d <= eps
+    const uint8_t* pairRound;  // eps sweeps (optional): per pair, the first round whose eps >= d
+    int round;
     uint64_t* masks;      // n x 2k x W
     int32_t* inRaw;       // n
     float* dists;         // n x 2k x m (optional)
@@ -217,6 +219,9 @@ struct DistArgs {
 constexpr int kMaxScreenedSweep = 16;
 int launch_dist(const DistArgs& a, cudaStream_t st);
 int launch_masks_from_dists(const DistArgs& a, cudaStream_t st);
+// Eps sweeps: each pair's round (index of the first of the nSweep ascending
+// sweepEps values >= its distance; nSweep when none), n x 2k x m bytes.
+int launch_pair_rounds(const DistArgs& a, uint8_t* rounds, cudaStream_t st);
 int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream_t st);
 int launch_to_bf16_split(const float* Xt, int ld, int n, void* Xs, int ldb, cudaStream_t st);
 int launch_screen_reset(const DistArgs& a, cudaStream_t st);

@@ -97,7 +97,7 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &aCount, &degree, &core, &parent, &border, &rootFlag, &labels, &nClusters, &scanTmp, &errFlags,
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
             &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig, &Rb, &newMasks, &coreEps, &sampleFlag,
-            &noiseFlag, &noiseCores, &noisePts, &PcT, &numCore};
+            &noiseFlag, &noiseCores, &noisePts, &PcT, &numCore, &pairRound};
 }
 
 // ---------------------------------------------------------------------------
@@ -432,9 +432,10 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     // stage needs no host synchronisation and can be captured in a graph.
     if (p.precision == SDB_PREC_BF16 && p.distance == SDB_COSINE && !optics &&
         (!sweep || sw->nEps <= kMaxScreenedSweep)) {
-        if (sweep) {
+        if (sweep) {  // ascending, as the rounds run
             da.nSweep = sw->nEps;
             for (int e = 0; e < sw->nEps; ++e) da.sweepEps[e] = sw->eps[e];
+            std::sort(da.sweepEps, da.sweepEps + sw->nEps);
         }
         const int ldb = (d + 63) / 64 * 64;
         const int64_t qcap = std::max<int64_t>(1 << 20, (int64_t)n * 2 * k * m / 8);
@@ -488,6 +489,13 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     if (sweep) {
         for (int i = 0; i < rounds; ++i) ord[i] = i;
         std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return sw->eps[x] < sw->eps[y]; });
+        if (rounds <= kMaxScreenedSweep) {  // one byte per pair: the round in which it joins
+            da.nSweep = rounds;
+            for (int e = 0; e < rounds; ++e) da.sweepEps[e] = sw->eps[ord[e]];
+            if (!ensure(pairRound, (size_t)n * 2 * k * m)) return SDB_ERR_NOMEM;
+            L_(launch_pair_rounds(da, static_cast<uint8_t*>(pairRound.ptr), st));
+            da.pairRound = static_cast<const uint8_t*>(pairRound.ptr);
+        }
         if (!ensure(newMasks, sizeof(uint64_t) * (size_t)n * 2 * k * W) || !ensure(coreEps, sizeof(int32_t) * n))
             return SDB_ERR_NOMEM;
         SDB_CK(cudaMemsetAsync(degree.ptr, 0, sizeof(int32_t) * n, st));
@@ -503,6 +511,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     if (sweep) {  // this eps: new pairs' masks and reverse counts from the stored distances
         da.eps = sw->eps[eo];
         da.epsLo = ei > 0 ? sw->eps[ord[ei - 1]] : -INFINITY;
+        da.round = ei;
         ca.round = ei;
         SDB_CK(cudaMemsetAsync(inRaw.ptr, 0, sizeof(int32_t) * n, st));
         L_(launch_masks_from_dists(da, st));

@@ -52,7 +52,7 @@ struct sdb_engine {
         members, tileOff, tileList, hubCount, hubOff, hubLists, masks, inRaw, aCount, degree, core, parent, border,
         rootFlag, labels, nClusters, scanTmp, errFlags, counters, E, Rt, signs, compCosh, dists, coreDist, nbOff,
         nbIdx, nbDist, nbFill, hubIdx, kMask, firstMasks, Xb, queue, sweepLabels, sweepNcl, sig, Rb, newMasks,
-        coreEps, sampleFlag, noiseFlag, noiseCores, noisePts, PcT, numCore;
+        coreEps, sampleFlag, noiseFlag, noiseCores, noisePts, PcT, numCore, pairRound;
 
     // results
     bool haveLabels = false, haveOptics = false, haveFit = false, lastOptics = false;

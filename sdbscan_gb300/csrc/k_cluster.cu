@@ -88,30 +88,33 @@ __global__ void __launch_bounds__(128) k_union_tiles(ClusterArgs a) {
     volatile int* vroot = croot;
     if (threadIdx.x == 0) newCoreCand = 0ull;
     __syncthreads();
+    int q = -1;  // this thread's candidate (threads < 64)
     if (threadIdx.x < 64) {
         const int c = tl.ct * 64 + threadIdx.x;
-        int root = -1;
         if (c < a.m) {
-            const int q = __ldg(tl.cand + c);
-            if (a.core[q]) {
-                root = find_root(a.parent, q);
-                if (a.carry && a.coreEps[q] == a.round) atomicOr(&newCoreCand, 1ull << threadIdx.x);
-            }
+            q = __ldg(tl.cand + c);
+            if (a.carry && a.core[q] && a.coreEps[q] == a.round) atomicOr(&newCoreCand, 1ull << threadIdx.x);
         }
-        croot[threadIdx.x] = root;
     }
     __syncthreads();
     const int64_t row = tl.mbeg + threadIdx.x;
-    if (row >= tl.mend) return;
-    const int2 mb = __ldg(a.members + row);
-    const int p = mb.x;
-    if (!a.core[p]) return;
-    const size_t at = ((size_t)p * 2 * a.k + mb.y) * a.W + tl.ct;
-    uint64_t bits = __ldg(reinterpret_cast<const unsigned long long*>(a.masks) + at);
-    // carrying over a smaller eps's union-find, only edges that are new (a new
-    // pair, or an endpoint that just became core) can join components
-    if (a.carry && a.coreEps[p] != a.round)
-        bits &= __ldg(reinterpret_cast<const unsigned long long*>(a.newMasks) + at) | newCoreCand;
+    int p = -1;
+    uint64_t bits = 0;
+    if (row < tl.mend) {
+        const int2 mb = __ldg(a.members + row);
+        if (a.core[mb.x]) {
+            p = mb.x;
+            const size_t at = ((size_t)p * 2 * a.k + mb.y) * a.W + tl.ct;
+            bits = __ldg(reinterpret_cast<const unsigned long long*>(a.masks) + at);
+            // carrying over a smaller eps's union-find, only edges that are new (a
+            // new pair, or an endpoint that just became core) can join components
+            if (a.carry && a.coreEps[p] != a.round)
+                bits &= __ldg(reinterpret_cast<const unsigned long long*>(a.newMasks) + at) | newCoreCand;
+        }
+    }
+    if (!__syncthreads_or(bits != 0)) return;  // nothing to unite in this tile
+    if (threadIdx.x < 64) croot[threadIdx.x] = (q >= 0 && a.core[q]) ? find_root(a.parent, q) : -1;
+    __syncthreads();
     if (!bits) return;
     int rp = find_root(a.parent, p);
     while (bits) {

@@ -219,7 +219,19 @@ __global__ void k_core_dedupe(CoreArgs a, const int4* __restrict__ sig) {
     __syncwarp();
     const int gw = blockIdx.x * (blockDim.x >> 5) + w;
     const int nw = gridDim.x * (blockDim.x >> 5);
+    const int slots = 2 * a.k;
+    const unsigned long long* mk64 = reinterpret_cast<const unsigned long long*>(a.masks);
     for (int p = gw; p < a.n; p += nw) {
+        // a point without a passing pair (common in a sweep round) only clears
+        // its first-occurrence words (this round's words when accumulating)
+        bool any = false;
+        for (int t = (int)lane; t < slots * a.W; t += 32) any |= __ldg(mk64 + (size_t)p * slots * a.W + t) != 0ull;
+        if (!__any_sync(0xffffffffu, any)) {
+            uint64_t* out = a.accumulate ? a.newMasks : a.firstMasks;
+            for (int t = (int)lane; t < slots * a.W; t += 32) out[(size_t)p * slots * a.W + t] = 0ull;
+            if (lane == 0) a.aCount[p] = 0;
+            continue;
+        }
         const int64_t h0 = a.hubOff[p], h1 = a.hubOff[p + 1];
         const bool hub = h1 > h0;
         if (hub) mark_lists(a, listMask, h0, h1, maskWords);

@@ -275,8 +275,13 @@ __global__ void k_masks_from_dists(DistArgs a) {
             bool pass = false;
             if (c < a.m) {
                 const int cp = __ldg(cand + c);
-                const float dd = __ldg(a.dists + ((size_t)p * 2 * a.k + slot) * a.m + c);
-                pass = cp != p && dd <= a.eps && dd > a.epsLo;
+                const size_t at = ((size_t)p * 2 * a.k + slot) * a.m + c;
+                if (a.pairRound != nullptr) {
+                    pass = cp != p && __ldg(a.pairRound + at) == a.round;
+                } else {
+                    const float dd = __ldg(a.dists + at);
+                    pass = cp != p && dd <= a.eps && dd > a.epsLo;
+                }
                 if (pass) {
                     atomicAdd(&colCount[col], 1);
                     ++myPass;
@@ -296,7 +301,25 @@ __global__ void k_masks_from_dists(DistArgs a) {
     if (threadIdx.x == 0 && passTotal) atomicAdd(a.pairs, (unsigned long long)passTotal);
 }
 
+// One pass over the stored distances: the sweep round in which each pair
+// joins (its distance's rank among the ascending eps values), so that every
+// round reads one byte per pair instead of the distance.
+__global__ void k_pair_rounds(const float* __restrict__ dists, size_t count, DistArgs a, uint8_t* __restrict__ rounds) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+        const float d = __ldg(dists + i);
+        int r = 0;
+        while (r < a.nSweep && a.sweepEps[r] < d) ++r;
+        rounds[i] = (uint8_t)r;
+    }
+}
+
 }  // namespace
+
+int launch_pair_rounds(const DistArgs& a, uint8_t* rounds, cudaStream_t st) {
+    const size_t count = (size_t)a.n * 2 * a.k * a.m;
+    k_pair_rounds<<<152 * 16, 256, 0, st>>>(a.dists, count, a, rounds);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
 
 int launch_masks_from_dists(const DistArgs& a, cudaStream_t st) {
     if (a.nTiles <= 0) return 0;
