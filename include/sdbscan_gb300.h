@@ -100,6 +100,15 @@ sdb_status sdb_fit_sdbscan_device(sdb_engine* e, const float* X_device, float ep
 sdb_status sdb_fit_soptics(sdb_engine* e, const float* X_host, float eps, int32_t minPts);
 sdb_status sdb_fit_soptics_device(sdb_engine* e, const float* X_device, float eps, int32_t minPts);
 
+/* loadtxtData (src/Utilities.cpp:57-95), used by load_fit_sDbscan /
+ * load_fit_sOptics (src/sDbscan.cpp:903-966, :1777-1837): reads n_points
+ * lines of n_features whitespace-separated numbers into X_dxn (d x n
+ * column-major, point n's values at X_dxn[n * d ...]), parsed like fscanf
+ * "%f".  No engine and no GPU are involved.  Returns SDB_ERR_ARG when the
+ * file is missing or holds fewer than n_points x n_features numbers (the
+ * reference exits or keeps zeros). */
+sdb_status sdb_load_txt(const char* path, int32_t n_points, int32_t n_features, float* X_dxn);
+
 /* test_sDbscan(X, eps, rangeEps, n_tests, minPts)  (src/sDbscan.h:187,
  * src/sDbscan.cpp:980-1039): the index and the candidate distances are built
  * once, then core points and clusters for every eps in eps[0..n_eps).

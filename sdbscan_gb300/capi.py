@@ -24,7 +24,7 @@ EXPORTS = ["sdb_params_default", "sdb_engine_create", "sdb_engine_destroy", "sdb
            "sdb_clear", "sdb_get_topk", "sdb_get_topm", "sdb_get_core", "sdb_get_core_dist", "sdb_get_projections",
            "sdb_get_counters", "sdb_get_stage_ms", "sdb_engine_stream", "sdb_last_error", "sdb_topm_noalloc",
            "sdb_fit_sdbscan_sweep", "sdb_batch_create", "sdb_batch_run", "sdb_batch_labels", "sdb_batch_lanes",
-           "sdb_batch_destroy", "sdb_batch_last_error"]
+           "sdb_batch_destroy", "sdb_batch_last_error", "sdb_load_txt"]
 
 
 class SdbParams(ctypes.Structure):
@@ -83,6 +83,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.sdb_batch_destroy.argtypes = [vp]
     L.sdb_batch_last_error.argtypes = [vp]
     L.sdb_batch_last_error.restype = ctypes.c_char_p
+    L.sdb_load_txt.argtypes = [ctypes.c_char_p, i32, i32, vp]
     _LIB = L
     return L
 
@@ -218,6 +219,17 @@ class Engine:
 
     def stream(self) -> int:
         return int(self.L.sdb_engine_stream(self.h) or 0)
+
+
+def load_txt(path: str, n_points: int, n_features: int) -> np.ndarray:
+    """sdb_load_txt: n_points lines of n_features numbers -> (n_points, n_features)
+    float32 (= the d x n column-major matrix the fits take), parsed like fscanf "%f"."""
+    L = load()
+    out = np.empty((n_points, n_features), np.float32)
+    s = L.sdb_load_txt(str(path).encode(), n_points, n_features, _ptr(out))
+    if s != 0:
+        raise SdbError(s, f"sdb_load_txt: {path} is missing or holds fewer than {n_points * n_features} numbers")
+    return out
 
 
 def topm_noalloc(proj_dev_ptr: int, n_points: int, n_proj: int, topM: int, out_dev_ptr: int, stream: int = 0) -> None:

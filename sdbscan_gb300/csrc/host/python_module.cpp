@@ -58,5 +58,19 @@ PYBIND11_MODULE(sDbscan, m) {
                 py::gil_scoped_release nogil;
                 s.fit_sOptics(p, eps, minPts);
             },
-            py::arg("X"), py::arg("eps"), py::arg("minPts"));
+            py::arg("X"), py::arg("eps"), py::arg("minPts"))
+        .def(
+            "load_fit_sDbscan",
+            [](sDbscan& s, const std::string& dataset, float eps, int minPts) {
+                py::gil_scoped_release nogil;
+                s.load_fit_sDbscan(dataset, eps, minPts);
+            },
+            py::arg("dataset"), py::arg("eps"), py::arg("minPts"))
+        .def(
+            "load_fit_sOptics",
+            [](sDbscan& s, const std::string& dataset, float eps, int minPts) {
+                py::gil_scoped_release nogil;
+                s.load_fit_sOptics(dataset, eps, minPts);
+            },
+            py::arg("dataset"), py::arg("eps"), py::arg("minPts"));
 }

@@ -4,6 +4,7 @@
 #include <fstream>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 namespace {
 
@@ -107,6 +108,25 @@ void sDbscan::fit_sDbscan(const float* X, float eps, int minPts) {
         std::ofstream out(f);
         for (int v : labels_) out << v << '\n';
     }
+}
+
+// loadtxtData (src/Utilities.cpp:57-95) through the engine library's loader.
+static std::vector<float> load_txt(const std::string& dataset, int n, int d) {
+    std::vector<float> X((size_t)n * d);
+    if (sdb_load_txt(dataset.c_str(), n, d, X.data()) != SDB_OK)
+        throw std::runtime_error("Error: Data file does not exist or holds fewer than n_points x n_features numbers: " +
+                                 dataset);
+    return X;
+}
+
+void sDbscan::load_fit_sDbscan(const std::string& dataset, float eps, int minPts) {
+    const std::vector<float> X = load_txt(dataset, n_, d_);
+    fit_sDbscan(X.data(), eps, minPts);
+}
+
+void sDbscan::load_fit_sOptics(const std::string& dataset, float eps, int minPts) {
+    const std::vector<float> X = load_txt(dataset, n_, d_);
+    fit_sOptics(X.data(), eps, minPts);
 }
 
 void sDbscan::fit_sOptics(const float* X, float eps, int minPts) {

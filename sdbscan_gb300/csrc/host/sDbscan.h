@@ -57,6 +57,10 @@ public:
     void fit_sDbscan(const float* X_dxn, float eps, int minPts);
     // src/sDbscan.h:197 / src/sDbscan.cpp:1711-1769
     void fit_sOptics(const float* X_dxn, float eps, int minPts);
+    // load_fit_sDbscan / load_fit_sOptics (src/sDbscan.h:184, :198): the data
+    // from a text file of n_points lines of n_features numbers, then the fit
+    void load_fit_sDbscan(const std::string& dataset, float eps, int minPts);
+    void load_fit_sOptics(const std::string& dataset, float eps, int minPts);
 
     int n_points() const { return n_; }
     int n_features() const { return d_; }

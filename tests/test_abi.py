@@ -5,6 +5,7 @@ import glob
 import os
 import re
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -51,3 +52,24 @@ def test_null_engine_is_rejected(lib):
     assert lib.sdb_set_params(None, None) == 1
     assert lib.sdb_fit_sdbscan(None, None, ctypes.c_float(0.1), 5) == 1
     assert lib.sdb_last_error(None) == b"null engine"
+
+
+def test_load_txt_parses_like_fscanf(tmp_path):
+    """sdb_load_txt (loadtxtData, src/Utilities.cpp:57-95): n lines of d
+    numbers, float32 values exactly those written (shortest round-trip
+    decimal strings), odd whitespace accepted; short or missing files raise."""
+    from sdbscan_gb300 import capi
+    rng = np.random.default_rng(3)
+    X = (rng.standard_normal((700, 13)) * 10.0 ** rng.integers(-6, 6, (700, 13))).astype(np.float32)
+    X[0, 0], X[1, 1] = 0.0, -1.5
+    path = tmp_path / "data.txt"
+    with open(path, "w") as f:
+        for i, row in enumerate(X):
+            sep = "\t" if i % 3 == 0 else " "
+            f.write(sep.join(np.format_float_positional(v, unique=True, trim="-") if i % 2 else
+                             np.format_float_scientific(v, unique=True) for v in row) + "\n")
+    np.testing.assert_array_equal(capi.load_txt(path, 700, 13), X)
+    with pytest.raises(capi.SdbError):
+        capi.load_txt(path, 701, 13)
+    with pytest.raises(capi.SdbError):
+        capi.load_txt(tmp_path / "missing.txt", 2, 2)

@@ -178,6 +178,29 @@ def test_pybind_dropin_matches_capi():
     assert dbs.n_clusters_ == ncl
 
 
+def test_load_fit_from_text_matches_in_memory_fit(tmp_path):
+    """load_fit_sDbscan / load_fit_sOptics (src/sDbscan.cpp:903-966,
+    :1777-1837): the data read from a text file (one point per line) gives the
+    in-memory fits' results."""
+    from sdbscan_gb300 import datasets
+    from sdbscan_gb300 import sDbscan as mod
+    X, _ = datasets.cfg1_cosine(3000, 24, seed=52)
+    path = tmp_path / "points.txt"
+    np.savetxt(path, X, fmt="%.9g")
+    Xr = np.loadtxt(path, dtype=np.float64).astype(np.float32)  # the values the file holds
+    a = mod.sDbscan(X.shape[0], X.shape[1])
+    a.set_params(n_proj=256, topK=5, topM=20, distance="Cosine", random_seed=9)
+    a.load_fit_sDbscan(str(path), 0.15, 10)
+    b = mod.sDbscan(X.shape[0], X.shape[1])
+    b.set_params(n_proj=256, topK=5, topM=20, distance="Cosine", random_seed=9)
+    b.fit_sDbscan(np.asfortranarray(Xr.T), 0.15, 10)
+    np.testing.assert_array_equal(np.asarray(a.labels_), np.asarray(b.labels_))
+    a.load_fit_sOptics(str(path), 0.2, 10)
+    b.fit_sOptics(np.asfortranarray(Xr.T), 0.2, 10)
+    np.testing.assert_array_equal(np.asarray(a.ordering_), np.asarray(b.ordering_))
+    np.testing.assert_array_equal(np.asarray(a.reachability_), np.asarray(b.reachability_))
+
+
 OPTICS_FIXTURES = [p for p in GOLDEN if _fixture(p)[1]["optics"]]
 
 
