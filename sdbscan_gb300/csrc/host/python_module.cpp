@@ -67,6 +67,21 @@ PYBIND11_MODULE(sDbscan, m) {
             },
             py::arg("dataset"), py::arg("eps"), py::arg("minPts"))
         .def(
+            "test_sDbscan",
+            [](sDbscan& s, const FArray& X, float eps, float rangeEps, int n_tests, int minPts) {
+                const float* p = checked(s, X);
+                py::gil_scoped_release nogil;
+                s.test_sDbscan(p, eps, rangeEps, n_tests, minPts);
+            },
+            py::arg("X"), py::arg("eps"), py::arg("rangeEps"), py::arg("n_tests"), py::arg("minPts"))
+        .def(
+            "load_test_sDbscan",
+            [](sDbscan& s, const std::string& dataset, float eps, float rangeEps, int n_tests, int minPts) {
+                py::gil_scoped_release nogil;
+                s.load_test_sDbscan(dataset, eps, rangeEps, n_tests, minPts);
+            },
+            py::arg("dataset"), py::arg("eps"), py::arg("rangeEps"), py::arg("n_tests"), py::arg("minPts"))
+        .def(
             "load_fit_sOptics",
             [](sDbscan& s, const std::string& dataset, float eps, int minPts) {
                 py::gil_scoped_release nogil;

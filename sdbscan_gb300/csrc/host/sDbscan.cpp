@@ -129,6 +129,30 @@ void sDbscan::load_fit_sOptics(const std::string& dataset, float eps, int minPts
     fit_sOptics(X.data(), eps, minPts);
 }
 
+void sDbscan::test_sDbscan(const float* X, float eps, float rangeEps, int n_tests, int minPts) {
+    if (n_tests < 1) throw std::runtime_error("test_sDbscan: n_tests must be >= 1");
+    std::vector<float> E(n_tests);
+    for (int i = 0; i < n_tests; ++i) E[i] = (float)(eps + 1.0 * i * rangeEps);  // src/sDbscan.cpp:1012
+    std::vector<int32_t> L((size_t)n_tests * n_);
+    std::vector<int32_t> ncl(n_tests);
+    check(sdb_fit_sdbscan_sweep(eng_, X, E.data(), n_tests, minPts, L.data(), ncl.data()), "test_sDbscan");
+    for (int i = 0; i < n_tests; ++i) {  // one labels file per eps (src/sDbscan.cpp:1026-1036)
+        const std::string f = output_ + "_" + dist_str(prm_.distance) + "_Eps_" + int2str(std::lround(1000 * E[i])) +
+                              "_MinPts_" + int2str(minPts) + "_KerFeatures_" +
+                              int2str(prm_.distance == SDB_COSINE ? d_ : prm_.ker_n_features) + "_NumProj_" +
+                              int2str(prm_.n_proj) + "_TopM_" + int2str(prm_.topM) + "_TopK_" + int2str(prm_.topK);
+        std::ofstream out(f);
+        for (int j = 0; j < n_; ++j) out << L[(size_t)i * n_ + j] << '\n';
+    }
+    labels_.assign(L.end() - n_, L.end());
+    n_clusters_ = ncl.back();
+}
+
+void sDbscan::load_test_sDbscan(const std::string& dataset, float eps, float rangeEps, int n_tests, int minPts) {
+    const std::vector<float> X = load_txt(dataset, n_, d_);
+    test_sDbscan(X.data(), eps, rangeEps, n_tests, minPts);
+}
+
 void sDbscan::fit_sOptics(const float* X, float eps, int minPts) {
     check(sdb_fit_soptics(eng_, X, eps, minPts), "fit_sOptics");
     ordering_.assign(n_, 0);

@@ -61,6 +61,11 @@ public:
     // from a text file of n_points lines of n_features numbers, then the fit
     void load_fit_sDbscan(const std::string& dataset, float eps, int minPts);
     void load_fit_sOptics(const std::string& dataset, float eps, int minPts);
+    // test_sDbscan / load_test_sDbscan (src/sDbscan.h:187-188): index once,
+    // then a clustering for eps + i rangeEps (i < n_tests), each written to
+    // its labels file; labels_ keeps the last one
+    void test_sDbscan(const float* X_dxn, float eps, float rangeEps, int n_tests, int minPts);
+    void load_test_sDbscan(const std::string& dataset, float eps, float rangeEps, int n_tests, int minPts);
 
     int n_points() const { return n_; }
     int n_features() const { return d_; }

@@ -201,6 +201,28 @@ def test_load_fit_from_text_matches_in_memory_fit(tmp_path):
     np.testing.assert_array_equal(np.asarray(a.reachability_), np.asarray(b.reachability_))
 
 
+def test_test_sdbscan_writes_each_eps(tmp_path):
+    """test_sDbscan (src/sDbscan.cpp:980-1039) through the drop-in module: one
+    labels file per eps + i rangeEps, each equal to a separate fit at that eps,
+    and labels_ holding the last."""
+    from sdbscan_gb300 import datasets
+    from sdbscan_gb300 import sDbscan as mod
+    X, _ = datasets.cfg1_cosine(4000, 32, seed=53)
+    prefix = str(tmp_path / "run")
+    a = mod.sDbscan(X.shape[0], X.shape[1])
+    a.set_params(n_proj=256, topK=5, topM=20, distance="Cosine", random_seed=9, output=prefix)
+    a.test_sDbscan(np.asfortranarray(X.T), 0.1, 0.05, 3, 10)
+    b = mod.sDbscan(X.shape[0], X.shape[1])
+    b.set_params(n_proj=256, topK=5, topM=20, distance="Cosine", random_seed=9)
+    for i in range(3):
+        e = np.float32(np.float64(np.float32(0.1)) + 1.0 * i * np.float64(np.float32(0.05)))  # the module's float math
+        b.fit_sDbscan(np.asfortranarray(X.T), float(e), 10)
+        f = f"{prefix}_Cosine_Eps_{int(round(1000 * float(e)))}_MinPts_10_KerFeatures_32_NumProj_256_TopM_20_TopK_5"
+        np.testing.assert_array_equal(np.loadtxt(f, dtype=np.int32), np.asarray(b.labels_))
+    np.testing.assert_array_equal(np.asarray(a.labels_), np.asarray(b.labels_))
+    assert a.n_clusters_ == b.n_clusters_
+
+
 OPTICS_FIXTURES = [p for p in GOLDEN if _fixture(p)[1]["optics"]]
 
 
