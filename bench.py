@@ -253,7 +253,7 @@ def run_batched(args, local, cpu=True):
             b.run()
         times = [b.run() for _ in range(args.steps)]
         labels = [[b.labels(i, j) for j in range(len(eps_list))] for i in range(len(sets))]
-        lanes = b.lanes()
+        lanes = (b.lanes(), b.tile_variants())
         b.close()
         return sum(times) / len(times), setup_s, lanes, labels
 
@@ -286,9 +286,11 @@ def run_batched(args, local, cpu=True):
     rate = lambda sec: total_n * len(eps_list) / sec
     out = {"workload": "cfg5_64sets_x8eps", "value": rate(bms / 1e3), "unit": "point-clusterings/s",
            "form": "BF16+recheck, one CUDA graph", "ms_per_batch": bms, "sets": len(sets), "points": total_n,
-           "eps": [round(e, 2) for e in eps_list], "launches_per_batch": 1, "graph_lanes": blanes,
+           "eps": [round(e, 2) for e in eps_list], "launches_per_batch": 1, "graph_lanes": blanes[0],
            "setup_s": bsetup, "labels_identical_to_plain": bf16_identical,
-           "plain_graph": {"value": rate(pms / 1e3), "ms_per_batch": pms, "graph_lanes": planes, "setup_s": psetup},
+           "plain_graph": {"value": rate(pms / 1e3), "ms_per_batch": pms, "graph_lanes": planes[0],
+                           "tile_variants": {str(v): planes[1].count(v) for v in sorted(set(planes[1]))},
+                           "setup_s": psetup},
            "plain_fits": {"value": rate(fits_s), "ms_per_batch": fits_s * 1e3, "fits": len(sets) * len(eps_list),
                           "labels_identical_to_graph": fits_identical,
                           "form": "512 separate fit_sDbscan calls on device-resident data"},

@@ -176,8 +176,10 @@ const char* sdb_last_error(sdb_engine* e);
  * to FP32).
  *   X_device[i]: d_i x n_i column-major data of set i, device memory, kept
  *                valid for the batch's lifetime
- * The batch plans every set once (sizing run), then times graphs with 4, 8,
- * 16, 32 and 64 sets in flight and keeps the fastest (sdb_batch_lanes).
+ * The batch plans every set once (sizing run; with FP32 precision and
+ * topM <= 50 it also times both distance tile shapes per set and keeps the
+ * faster, sdb_batch_tile_variant), then times graphs with 4, 8, 16, 32 and 64
+ * sets in flight and keeps the fastest (sdb_batch_lanes).
  * sdb_batch_run replays it; sdb_batch_labels reads set i's labelling for eps
  * index j. */
 typedef struct sdb_batch sdb_batch;
@@ -187,6 +189,10 @@ sdb_status sdb_batch_create(int32_t n_sets, const int32_t* n_points, const int32
 sdb_status sdb_batch_run(sdb_batch* b, float* elapsed_ms);
 sdb_status sdb_batch_labels(sdb_batch* b, int32_t set, int32_t eps_index, int32_t* labels, int32_t* n_clusters);
 int32_t sdb_batch_lanes(sdb_batch* b);
+/* The plain distance kernel's tile shape the autotuner kept for set i (FP32
+ * precision, topM <= 50): 1 = 128 x 64 tiles on 256 threads, 2 = 128 x 50
+ * tiles on 160 threads; 0 = the default rule (by topM); -1 for a bad index. */
+int32_t sdb_batch_tile_variant(sdb_batch* b, int32_t set);
 void sdb_batch_destroy(sdb_batch* b);
 const char* sdb_batch_last_error(sdb_batch* b);
 

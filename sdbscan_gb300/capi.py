@@ -24,7 +24,8 @@ EXPORTS = ["sdb_params_default", "sdb_engine_create", "sdb_engine_destroy", "sdb
            "sdb_clear", "sdb_get_topk", "sdb_get_topm", "sdb_get_core", "sdb_get_core_dist", "sdb_get_projections",
            "sdb_get_counters", "sdb_get_stage_ms", "sdb_engine_stream", "sdb_last_error", "sdb_topm_noalloc",
            "sdb_fit_sdbscan_sweep", "sdb_batch_create", "sdb_batch_run", "sdb_batch_labels", "sdb_batch_lanes",
-           "sdb_batch_destroy", "sdb_batch_last_error", "sdb_load_txt"]
+           "sdb_batch_destroy", "sdb_batch_last_error", "sdb_load_txt",
+           "sdb_batch_tile_variant"]
 
 
 class SdbParams(ctypes.Structure):
@@ -84,6 +85,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.sdb_batch_last_error.argtypes = [vp]
     L.sdb_batch_last_error.restype = ctypes.c_char_p
     L.sdb_load_txt.argtypes = [ctypes.c_char_p, i32, i32, vp]
+    L.sdb_batch_tile_variant.argtypes = [vp, i32]
+    L.sdb_batch_tile_variant.restype = i32
     _LIB = L
     return L
 
@@ -284,6 +287,10 @@ class Batch:
 
     def lanes(self) -> int:
         return int(self.L.sdb_batch_lanes(self.h))
+
+    def tile_variants(self) -> list[int]:
+        """Per set, the distance tile shape the autotuner kept (see sdb_batch_tile_variant)."""
+        return [int(self.L.sdb_batch_tile_variant(self.h, i)) for i in range(self.ns)]
 
     def close(self):
         if getattr(self, "h", None) and self.h.value:

@@ -4,8 +4,9 @@
 // the buffers and uploads the random signs), then records the whole batch —
 // every dataset's index, distances and per-eps core/cluster stages — into one
 // CUDA graph.  Datasets run on their engines' own streams; at most `lanes` of
-// them run at a time (set i waits for set i - lanes), and the lane count is
-// chosen by timing each candidate graph once (the batch's autotuner).
+// them run at a time (set i waits for set i - lanes).  The batch's autotuner
+// picks, per set, the plain distance kernel's tile shape (timing the set's
+// sweep with each) and then the lane count (timing each candidate graph).
 // sdb_batch_run replays the graph: one launch for all the clusterings.
 #include <cuda_runtime.h>
 
@@ -144,6 +145,25 @@ sdb_status sdb_batch_create(int32_t n_sets, const int32_t* n_points, const int32
             *out = b;
             return batch_fail(b, s, "set " + std::to_string(i) + ": " + e->err);
         }
+        // tile autotuner: when the set's distances run on the plain kernel and
+        // both tile shapes apply (m <= 50), time the distance stage with each
+        if (q.precision == SDB_PREC_FP32 && q.topM <= 50) {
+            float best = 1e30f;
+            int bestV = 0;
+            for (int v : {1, 2}) {
+                e->distVariant = v;
+                s = e->fit(X_device[i], true, eps[0], minPts, false, &sw);
+                if (s != SDB_OK) {
+                    *out = b;
+                    return batch_fail(b, s, "set " + std::to_string(i) + ": " + e->err);
+                }
+                if (e->stageMs[4] < best) {
+                    best = e->stageMs[4];
+                    bestV = v;
+                }
+            }
+            e->distVariant = bestV;
+        }
     }
     // autotune the number of datasets in flight
     float best = 1e30f;
@@ -200,6 +220,11 @@ sdb_status sdb_batch_labels(sdb_batch* b, int32_t set, int32_t eps_index, int32_
 }
 
 int32_t sdb_batch_lanes(sdb_batch* b) { return b ? b->lanes : 0; }
+
+int32_t sdb_batch_tile_variant(sdb_batch* b, int32_t set) {
+    if (!b || set < 0 || set >= (int)b->eng.size()) return -1;
+    return b->eng[set]->distVariant;
+}
 
 void sdb_batch_destroy(sdb_batch* b) {
     if (!b) return;

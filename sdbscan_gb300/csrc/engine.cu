@@ -424,6 +424,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     da.dists = (optics || sweep) ? f32(dists) : nullptr;
     da.pairs = ctr + 3;
     da.topKmat = i32(topK);
+    da.variant = distVariant;
     SDB_CK(cudaMemsetAsync(inRaw.ptr, 0, sizeof(int32_t) * n, st));
     // BF16 tensor-core screening + exact FP32 re-decision near eps (Cosine
     // sDBSCAN fits and eps sweeps of up to kMaxScreenedSweep values).  The

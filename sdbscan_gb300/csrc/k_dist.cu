@@ -237,8 +237,11 @@ template <int DIST, int TX, int CN> int launch_dist_v(const DistArgs& a, cudaStr
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
+// Tile shape: the caller's (autotuned) choice, else exact 50-column tiles for
+// m in 41..50 and 64-column tiles otherwise.
 template <int DIST> int launch_dist_t(const DistArgs& a, cudaStream_t st) {
-    if (a.m > 40 && a.m <= 50) return launch_dist_v<DIST, 10, 5>(a, st);  // exact 50-column tiles
+    const bool fifty = a.variant == 2 ? a.m <= 50 : (a.variant == 0 && a.m > 40 && a.m <= 50);
+    if (fifty) return launch_dist_v<DIST, 10, 5>(a, st);
     return launch_dist_v<DIST, 16, 4>(a, st);
 }
 
