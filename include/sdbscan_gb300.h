@@ -62,8 +62,8 @@ typedef struct {
     int32_t ker_n_features;       /* kerDim (forced to n_features for Cosine)     */
     float ker_sigma;              /* kerSigma (L1/L2 random Fourier features)     */
     float ker_intervalSampling;   /* kerSam (Chi2/JS embeddings)                  */
-    int32_t clusterNoise;         /* noiseClustering: only 0 is supported         */
-    float samplingProb;           /* prob (sDbscan-1NN; unused when clusterNoise=0) */
+    int32_t clusterNoise;         /* noiseClustering: 0, 1 (sDbscan-1NN), 2 (no-op) */
+    float samplingProb;           /* prob: sDbscan-1NN core sampling; sng sample rate */
     int32_t verbose;              /* ver: print per-stage times                   */
     int32_t n_threads;            /* numThreads: accepted for API parity, unused  */
     int32_t random_seed;          /* randomSeed: < 0 means seeded from the clock  */
@@ -121,6 +121,41 @@ sdb_status sdb_load_txt(const char* path, int32_t n_points, int32_t n_features, 
  * eps values (up to 16; longer lists run FP32). */
 sdb_status sdb_fit_sdbscan_sweep(sdb_engine* e, const float* X_host, const float* eps, int32_t n_eps, int32_t minPts,
                                  int32_t* labels, int32_t* n_clusters);
+
+/* set_sngParams(dist, prob, noiseClustering, ver, filename, numThreads,
+ * randomSeed)  (src/sDbscan.h:127-139): sets distance, samplingProb, verbose,
+ * n_threads and random_seed, and clusterNoise = 2 when clusterNoise > 0; the
+ * index parameters keep their values.  Enough for the sng fits below. */
+sdb_status sdb_set_sng_params(sdb_engine* e, int32_t distance, float samplingProb, int32_t clusterNoise,
+                              int32_t verbose, int32_t n_threads, int32_t random_seed);
+
+/* fit_sngDbscan(X, eps, minPts)  (src/sDbscan.h:190, src/sDbscan.cpp:1131-1179):
+ * each point's neighbourhood from ceil(n samplingProb) random draws (both
+ * directions of every draw within eps), core points with >= minPts - 1
+ * neighbours counted with repeats, clusters as fit_sDbscan; samplingProb >= 1
+ * is exact DBSCAN.  With random_seed >= 0 the labels equal the reference's
+ * (every point's generator is seeded alike); with random_seed < 0 one clock
+ * seed is shared by all points.  Switches clusterNoise to 0 (src/sDbscan.cpp:1157).
+ * Results: sdb_get_labels, sdb_get_core (neighbourhood sizes with repeats). */
+sdb_status sdb_fit_sngdbscan(sdb_engine* e, const float* X_host, float eps, int32_t minPts);
+sdb_status sdb_fit_sngdbscan_device(sdb_engine* e, const float* X_device, float eps, int32_t minPts);
+
+/* test_sngDbscan(X, eps, rangeEps, n_tests, minPts)  (src/sDbscan.h:193,
+ * src/sDbscan.cpp:1192-1240): one transform and sample, then a clustering per
+ * eps of eps[0..n_eps).  labels: n_eps x n_points int32; n_clusters: n_eps. */
+sdb_status sdb_fit_sngdbscan_sweep(sdb_engine* e, const float* X_host, const float* eps, int32_t n_eps,
+                                   int32_t minPts, int32_t* labels, int32_t* n_clusters);
+
+/* fit_sngOptics(X, eps, minPts)  (src/sDbscan.h:200, src/sDbscan.cpp:1846-1880):
+ * de-duplicated sampled neighbourhoods with distances, core distances
+ * ((minPts-1)-th smallest), then the ordering and reachability of
+ * fit_sOptics.  The reference seeds each point from std::random_device (not
+ * reproducible); here all points share one seeded sequence of
+ * ceil(samplingProb n) draws (random_seed, or the clock when < 0), each
+ * skipping its own index.  minPts >= 2.  Results: sdb_get_optics,
+ * sdb_get_core, sdb_get_core_dist. */
+sdb_status sdb_fit_sngoptics(sdb_engine* e, const float* X_host, float eps, int32_t minPts);
+sdb_status sdb_fit_sngoptics_device(sdb_engine* e, const float* X_device, float eps, int32_t minPts);
 
 /* labels_ and n_clusters_  (src/sDbscan.h:67-68; python_wrapper.cpp:31-32).
  * labels: n_points int32. */

@@ -77,6 +77,8 @@ class Port:
         L.orc_fit_sdbscan.restype = _i
         L.orc_fit_soptics.restype = _i
         L.orc_fit_sdbscan_sweep.restype = _i
+        L.orc_fit_sngdbscan.restype = _i
+        L.orc_fit_sngoptics.restype = _i
         L.orc_distance.restype = _f
 
     # RNG -------------------------------------------------------------------
@@ -189,6 +191,42 @@ class Port:
             raise ValueError(f"transform rejected the input (code {-ncl})")
         return labels, ncl, core, times
 
+    def fit_sngdbscan(self, X, eps, minPts, *, dist="Cosine", samplingProb=0.01, seed=42, threads=-1):
+        """The reference's fit_sngDbscan restated point by point
+        (src/sDbscan.cpp:416-504, 1131-1179).  Returns (labels, n_clusters,
+        core, degree, times)."""
+        X = np.ascontiguousarray(X, np.float32)
+        n, d = X.shape
+        if seed < 0:
+            raise ValueError("the oracle needs a seed >= 0 (a clock seed cannot be reproduced)")
+        labels = np.zeros(n, np.int32)
+        core = np.zeros(n, np.uint8)
+        deg = np.zeros(n, np.int32)
+        times = np.zeros(5, np.float64)
+        ncl = self.L.orc_fit_sngdbscan(_p(X), _i(n), _i(d), _i(DIST_CODES[dist]), _f(samplingProb), _i(seed),
+                                       _f(eps), _i(minPts), _i(threads), _p(labels), _p(core), _p(deg), _p(times))
+        if ncl < 0:
+            raise ValueError(f"transform rejected the input (code {-ncl})")
+        return labels, ncl, core, deg, times
+
+    def fit_sngoptics(self, X, eps, minPts, *, dist="Cosine", samplingProb=0.01, seed=42, threads=-1):
+        """sngOptics with the engine's shared seeded sample (src/sDbscan.cpp:1484-1583,
+        1846-1880).  Returns (ordering, reachability, core, core_dist, degree, times)."""
+        X = np.ascontiguousarray(X, np.float32)
+        n, d = X.shape
+        ordering = np.zeros(n, np.int32)
+        reach = np.zeros(n, np.float32)
+        core = np.zeros(n, np.uint8)
+        cd = np.zeros(n, np.float32)
+        deg = np.zeros(n, np.int32)
+        times = np.zeros(5, np.float64)
+        r = self.L.orc_fit_sngoptics(_p(X), _i(n), _i(d), _i(DIST_CODES[dist]), _f(samplingProb), _i(seed),
+                                     _f(eps), _i(minPts), _i(threads), _p(ordering), _p(reach), _p(core), _p(cd),
+                                     _p(deg), _p(times))
+        if r < 0:
+            raise ValueError(f"transform rejected the input (code {-r})")
+        return ordering, reach, core, cd, deg, times
+
     def fit_sdbscan_sweep(self, X, eps_list, minPts, *, dist="Cosine", n_proj=1024, topK=10, topM=50, ker=1024,
                           sigma=1.0, L=0.4, seed=42, threads=-1):
         """The reference's index-once sweep restated (test_sDbscan, src/sDbscan.cpp:980-1039)."""
@@ -283,6 +321,19 @@ class Ref:
     def fit_sOptics(self, X, eps, minPts):
         X = np.ascontiguousarray(X, np.float32)
         self.L.ref_fit_soptics(self.h, _p(X), _i(self.n), _i(self.d), _f(eps), _i(minPts))
+
+    def set_sngParams(self, distance="Cosine", samplingProb=0.01, clusterNoise=0, verbose=False, n_threads=1,
+                      random_seed=42):
+        self.L.ref_set_sng_params(self.h, distance.encode(), _f(samplingProb), _i(clusterNoise),
+                                  _i(1 if verbose else 0), _i(n_threads), _i(random_seed))
+
+    def fit_sngDbscan(self, X, eps, minPts):
+        X = np.ascontiguousarray(X, np.float32)
+        self.L.ref_fit_sngdbscan(self.h, _p(X), _i(self.n), _i(self.d), _f(eps), _i(minPts))
+
+    def fit_sngOptics(self, X, eps, minPts):
+        X = np.ascontiguousarray(X, np.float32)
+        self.L.ref_fit_sngoptics(self.h, _p(X), _i(self.n), _i(self.d), _f(eps), _i(minPts))
 
     @property
     def labels_(self):

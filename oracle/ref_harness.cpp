@@ -92,6 +92,18 @@ void ref_fit_soptics(void* h, const float* X, int n, int d, float eps, int minPt
     Ref<const MatrixXf> ref(X, d, n);
     P(h)->fit_sOptics(ref, eps, minPts);
 }
+// sDbscan::set_sngParams (src/sDbscan.h:127-139), positional order kept.
+void ref_set_sng_params(void* h, const char* dist, float prob, int noise, int verbose, int threads, int seed) {
+    P(h)->set_sngParams(string(dist), prob, noise, verbose != 0, "", threads, seed);
+}
+void ref_fit_sngdbscan(void* h, const float* X, int n, int d, float eps, int minPts) {
+    Ref<const MatrixXf> ref(X, d, n);
+    P(h)->fit_sngDbscan(ref, eps, minPts);
+}
+void ref_fit_sngoptics(void* h, const float* X, int n, int d, float eps, int minPts) {
+    Ref<const MatrixXf> ref(X, d, n);
+    P(h)->fit_sngOptics(ref, eps, minPts);
+}
 void ref_clear(void* h) { P(h)->clear(); }
 
 int ref_n_clusters(void* h) { return P(h)->n_clusters_; }

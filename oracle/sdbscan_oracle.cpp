@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <map>
 #include <queue>
 #include <random>
 #include <unordered_map>
@@ -657,6 +658,135 @@ int orc_fit_soptics(const float* X, int n, int d, int code, int nproj, int k, in
     times[3] = tm.lap();
     times[4] = all.lap();
     orc_graph_free();
+    return 0;
+}
+
+// ---- sngDbscan (fit_sngDbscan, src/sDbscan.cpp:1131-1179) --------------------
+// sng_findCorePoints (:416-504) as the reference states it, point by point:
+// point p seeds default_random_engine with `seed` (>= 0 here: a clock seed
+// cannot be reproduced) and draws uniform_int_distribution(0, n - 1) until it
+// has S = ceil(1.0 n samplingProb) draws that are not p; each draw q within
+// eps is pushed into both lists (:459-464).  samplingProb >= 1: every other
+// point, forward only (:466-479).  Core points: list size, repeats counted,
+// >= minPts - 1; other lists cleared (:488-496); then formCluster.
+// labels / core / degree: n.  Returns n_clusters_, or a negative transform
+// error.  times[5] as orc_fit_sdbscan (index = 0).
+int orc_fit_sngdbscan(const float* X, int n, int d, int code, float samplingProb, int seed, float eps, int minPts,
+                      int threads, int32_t* labels, uint8_t* core, int32_t* degree, double* times) {
+    if (threads > 0) omp_set_num_threads(threads);
+    Timer tm, all;
+    std::vector<float> Xc(X, X + (size_t)n * d);
+    int err = orc_transform(Xc.data(), n, d, code);
+    if (err) return -err;
+    times[0] = tm.lap();
+    times[1] = 0.0;
+    const float* Y = Xc.data();
+    std::vector<std::vector<int>> nb(n);
+    if (samplingProb < 1.0) {
+        const long long S = (long long)std::ceil(1.0 * n * samplingProb);
+        std::vector<std::vector<std::pair<int, int>>> found(n);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int p = 0; p < n; ++p) {
+            std::default_random_engine gen((unsigned)seed);
+            std::uniform_int_distribution<> distrib(0, n - 1);
+            for (long long s = 0; s < S;) {
+                const int q = distrib(gen);
+                if (q == p) continue;
+                ++s;
+                if (distance(Y + (size_t)p * d, Y + (size_t)q * d, d, code) <= eps) found[p].push_back({p, q});
+            }
+        }
+        for (int p = 0; p < n; ++p)
+            for (const auto& e : found[p]) {
+                nb[e.first].push_back(e.second);
+                nb[e.second].push_back(e.first);
+            }
+    } else {
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int p = 0; p < n; ++p)
+            for (int q = 0; q < n; ++q)
+                if (q != p && distance(Y + (size_t)p * d, Y + (size_t)q * d, d, code) <= eps) nb[p].push_back(q);
+    }
+    for (int p = 0; p < n; ++p) {
+        degree[p] = (int32_t)nb[p].size();
+        core[p] = degree[p] >= minPts - 1 ? 1 : 0;
+        if (!core[p]) nb[p].clear();
+    }
+    times[2] = tm.lap();
+    std::vector<int64_t> off(n + 1, 0);
+    for (int p = 0; p < n; ++p) off[p + 1] = off[p] + (int64_t)nb[p].size();
+    std::vector<int32_t> idx(off[n]);
+    for (int p = 0; p < n; ++p) std::copy(nb[p].begin(), nb[p].end(), idx.begin() + off[p]);
+    const int ncl = orc_form_cluster(n, core, off.data(), idx.data(), labels);
+    times[3] = tm.lap();
+    times[4] = all.lap();
+    return ncl;
+}
+
+// ---- sngOptics (fit_sngOptics, src/sDbscan.cpp:1846-1880) --------------------
+// sng_findCoreDist (:1484-1583) with the engine's reproducible sample: every
+// point draws the same seeded sequence (the reference seeds each point from
+// std::random_device, :1500-1501) of S = ceil(samplingProb n) (float product,
+// :1490) draws, skipping its own index without replacing it (:1507-1508);
+// each draw within eps is pushed into both lists with its distance; lists are
+// de-duplicated (:1537-1541); core points have >= minPts - 1 distinct
+// neighbours and core distance the (minPts-1)-th smallest (:1543-1555), 0
+// otherwise; then formOptics_scikit with (reachability, id) ties (tie_mode 1).
+int orc_fit_sngoptics(const float* X, int n, int d, int code, float samplingProb, int seed, float eps, int minPts,
+                      int threads, int32_t* ordering, float* reach, uint8_t* core, float* coreDist, int32_t* degree,
+                      double* times) {
+    if (threads > 0) omp_set_num_threads(threads);
+    Timer tm, all;
+    std::vector<float> Xc(X, X + (size_t)n * d);
+    int err = orc_transform(Xc.data(), n, d, code);
+    if (err) return -err;
+    times[0] = tm.lap();
+    times[1] = 0.0;
+    const float* Y = Xc.data();
+    const long long S = (long long)std::ceil(samplingProb * (float)n);
+    std::vector<int> draws;
+    {
+        std::default_random_engine gen((unsigned)seed);
+        std::uniform_int_distribution<> distrib(0, n - 1);
+        for (long long s = 0; s < S; ++s) draws.push_back(distrib(gen));
+    }
+    std::vector<std::vector<std::pair<int, float>>> found(n);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int p = 0; p < n; ++p)
+        for (int q : draws) {
+            if (q == p) continue;
+            const float dd = distance(Y + (size_t)p * d, Y + (size_t)q * d, d, code);
+            if (dd <= eps) found[p].push_back({q, dd});
+        }
+    std::vector<std::map<int, float>> lists(n);
+    for (int p = 0; p < n; ++p)
+        for (const auto& e : found[p]) {
+            lists[p].emplace(e.first, e.second);
+            lists[e.first].emplace(p, e.second);
+        }
+    std::vector<int64_t> off(n + 1, 0);
+    for (int p = 0; p < n; ++p) off[p + 1] = off[p] + (int64_t)lists[p].size();
+    std::vector<int32_t> idx(off[n]);
+    std::vector<float> dist(off[n]);
+    for (int p = 0; p < n; ++p) {
+        int64_t o = off[p];
+        for (const auto& e : lists[p]) {
+            idx[o] = e.first;
+            dist[o++] = e.second;
+        }
+        degree[p] = (int32_t)lists[p].size();
+        core[p] = degree[p] >= minPts - 1 ? 1 : 0;
+        coreDist[p] = 0.0f;
+        if (core[p]) {
+            std::vector<float> v(dist.begin() + off[p], dist.begin() + off[p + 1]);
+            std::nth_element(v.begin(), v.begin() + (minPts - 2), v.end());
+            coreDist[p] = v[minPts - 2];
+        }
+    }
+    times[2] = tm.lap();
+    orc_form_optics(n, core, coreDist, off.data(), idx.data(), dist.data(), 1, ordering, reach);
+    times[3] = tm.lap();
+    times[4] = all.lap();
     return 0;
 }
 

@@ -25,7 +25,8 @@ EXPORTS = ["sdb_params_default", "sdb_engine_create", "sdb_engine_destroy", "sdb
            "sdb_get_counters", "sdb_get_stage_ms", "sdb_engine_stream", "sdb_last_error", "sdb_topm_noalloc",
            "sdb_fit_sdbscan_sweep", "sdb_batch_create", "sdb_batch_run", "sdb_batch_labels", "sdb_batch_lanes",
            "sdb_batch_destroy", "sdb_batch_last_error", "sdb_load_txt",
-           "sdb_batch_tile_variant"]
+           "sdb_batch_tile_variant", "sdb_set_sng_params", "sdb_fit_sngdbscan", "sdb_fit_sngdbscan_device",
+           "sdb_fit_sngdbscan_sweep", "sdb_fit_sngoptics", "sdb_fit_sngoptics_device"]
 
 
 class SdbParams(ctypes.Structure):
@@ -59,7 +60,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.sdb_engine_create.argtypes = [i32, i32, i32, ctypes.POINTER(vp)]
     L.sdb_engine_destroy.argtypes = [vp]
     L.sdb_set_params.argtypes = [vp, ctypes.POINTER(SdbParams)]
-    for f in ("sdb_fit_sdbscan", "sdb_fit_sdbscan_device", "sdb_fit_soptics", "sdb_fit_soptics_device"):
+    for f in ("sdb_fit_sdbscan", "sdb_fit_sdbscan_device", "sdb_fit_soptics", "sdb_fit_soptics_device",
+              "sdb_fit_sngdbscan", "sdb_fit_sngdbscan_device", "sdb_fit_sngoptics", "sdb_fit_sngoptics_device"):
         getattr(L, f).argtypes = [vp, vp, f32, i32]
     L.sdb_get_labels.argtypes = [vp, vp, vp]
     L.sdb_get_optics.argtypes = [vp, vp, vp]
@@ -75,6 +77,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.sdb_last_error.restype = ctypes.c_char_p
     L.sdb_topm_noalloc.argtypes = [vp, i32, i32, i32, vp, vp]
     L.sdb_fit_sdbscan_sweep.argtypes = [vp, vp, vp, i32, i32, vp, vp]
+    L.sdb_fit_sngdbscan_sweep.argtypes = [vp, vp, vp, i32, i32, vp, vp]
+    L.sdb_set_sng_params.argtypes = [vp, i32, f32, i32, i32, i32, i32]
     L.sdb_batch_create.argtypes = [i32, vp, vp, vp, ctypes.POINTER(SdbParams), vp, i32, i32, i32,
                                    ctypes.POINTER(vp)]
     L.sdb_batch_run.argtypes = [vp, ctypes.POINTER(f32)]
@@ -162,6 +166,44 @@ class Engine:
 
     def fit_soptics_device(self, x_dev_ptr: int, eps: float, minPts: int):
         self._check(self.L.sdb_fit_soptics_device(self.h, ctypes.c_void_p(x_dev_ptr), ctypes.c_float(eps), minPts))
+
+    # sngDbscan / sngOptics (src/sDbscan.h:127-139, :190-201) ----------------------
+    def set_sng_params(self, distance="Cosine", samplingProb=0.01, clusterNoise=0, verbose=False, output="",
+                       n_threads=-1, random_seed=-1):
+        p = self.params
+        self._check(self.L.sdb_set_sng_params(self.h, DISTANCES[distance], ctypes.c_float(samplingProb),
+                                              clusterNoise, int(bool(verbose)), n_threads, random_seed))
+        p.distance, p.samplingProb, p.verbose = DISTANCES[distance], samplingProb, int(bool(verbose))
+        p.n_threads, p.random_seed = n_threads, random_seed
+        if clusterNoise > 0:
+            p.clusterNoise = 2
+
+    def fit_sngdbscan(self, X: np.ndarray, eps: float, minPts: int):
+        X = self._host(X)
+        self.params.clusterNoise = 0
+        self._check(self.L.sdb_fit_sngdbscan(self.h, _ptr(X), ctypes.c_float(eps), minPts))
+
+    def fit_sngdbscan_device(self, x_dev_ptr: int, eps: float, minPts: int):
+        self.params.clusterNoise = 0
+        self._check(self.L.sdb_fit_sngdbscan_device(self.h, ctypes.c_void_p(x_dev_ptr), ctypes.c_float(eps), minPts))
+
+    def fit_sngdbscan_sweep(self, X: np.ndarray, eps_list, minPts: int):
+        """test_sngDbscan: one transform and sample, labels for every eps.
+        Returns (labels [n_eps, n], n_clusters [n_eps])."""
+        X = self._host(X)
+        eps = np.ascontiguousarray(eps_list, dtype=np.float32)
+        labels = np.empty((eps.shape[0], self.n), np.int32)
+        ncl = np.empty(eps.shape[0], np.int32)
+        self._check(self.L.sdb_fit_sngdbscan_sweep(self.h, _ptr(X), _ptr(eps), eps.shape[0], minPts, _ptr(labels),
+                                                   _ptr(ncl)))
+        return labels, ncl
+
+    def fit_sngoptics(self, X: np.ndarray, eps: float, minPts: int):
+        X = self._host(X)
+        self._check(self.L.sdb_fit_sngoptics(self.h, _ptr(X), ctypes.c_float(eps), minPts))
+
+    def fit_sngoptics_device(self, x_dev_ptr: int, eps: float, minPts: int):
+        self._check(self.L.sdb_fit_sngoptics_device(self.h, ctypes.c_void_p(x_dev_ptr), ctypes.c_float(eps), minPts))
 
     def _host(self, X):
         X = np.ascontiguousarray(X, dtype=np.float32)

@@ -131,6 +131,8 @@ struct ProjectArgs {
     double ln4;              // JS: log(4.0) as the host computes it
 };
 int launch_project(const ProjectArgs& a, cudaStream_t st);
+// transformData alone into Xt (uses X, ldx, Xt, ld, n, d, dist, scale, err).
+int launch_transform(const ProjectArgs& a, cudaStream_t st);
 
 // Random Fourier features for L1/L2: E[p] = [cos(R x_p), sin(R x_p)].
 // gate (optional): run only if *gate != 0 (the tensor-core embedding failed).
@@ -291,6 +293,54 @@ struct ClusterArgs {
     int32_t* nClusters;   // device scalar
 };
 int launch_cluster(const ClusterArgs& a, cudaStream_t st);
+// Pieces of launch_cluster for callers with their own edge kernels: parent[p]
+// = p and border[p] = INT_MAX; parents of core points set to their roots;
+// cluster ids and labels from core, parent and border (uses n, core, parent,
+// border, rootFlag, scanTmp, labels, nClusters).
+int launch_uf_init(int32_t* parent, int32_t* border, int n, cudaStream_t st);
+int launch_uf_compress(const ClusterArgs& a, cudaStream_t st);
+int launch_cluster_labels(const ClusterArgs& a, cudaStream_t st);
+
+// sngDbscan / sngOptics (src/sDbscan.cpp:416-504, :1484-1583) over one
+// shared sample of columns: every point is a row, every distinct sampled
+// point a column.
+struct SngArgs {
+    const float* Xt;
+    int ld, d, dist, n;
+    const int32_t* cols;   // nU distinct sampled point ids, ascending
+    const int32_t* mult;   // nU: times each was drawn (null: weight 1)
+    const int32_t* colOf;  // n: the point's column, -1 when not sampled
+    int nU, nct;           // columns; 64-column tiles
+    float eps;
+    uint64_t* mask;        // nct x n pass bits (tile-major: word ct * n + p), or null
+    int32_t* rowDeg;       // n: weighted passes of the point's row (atomic adds)
+    int32_t* colCnt;       // nU: passes of each column over all rows
+    unsigned long long* pairs;  // pass counter
+    // extra draws of the sampled points (sngDbscan): (point, drawn point) pairs
+    const int2* extras;
+    uint8_t* extraPass;
+    int nExtra;
+    // sngOptics neighbour lists (CSR filled by the second block pass)
+    const int64_t* nbOff;
+    int32_t* nbFill;
+    int32_t* nbIdx;
+    float* nbDist;
+    int32_t* err;          // set when a list would overflow its slots
+};
+// First block pass: pass bits (mask may be null), row degrees, column counts.
+int launch_sng_block(const SngArgs& a, cudaStream_t st);
+// Second block pass (sngOptics): every passing pair into the CSR lists.
+int launch_sng_emit(const SngArgs& a, cudaStream_t st);
+int launch_sng_extras(const SngArgs& a, cudaStream_t st);
+int launch_sng_col_of(const SngArgs& a, int32_t* colOf, cudaStream_t st);
+// degree / core flags: sngDbscan counts draws (weights), sngOptics distinct neighbours
+int launch_sng_degree(const SngArgs& a, int exact, int optics, int minPts, int32_t* degree, uint8_t* core,
+                      cudaStream_t st);
+// union-find over the core-core pass pairs and border minima (parents of core
+// points compressed in between by the caller)
+int launch_sng_union(const SngArgs& a, const uint8_t* core, int32_t* parent, cudaStream_t st);
+int launch_sng_border(const SngArgs& a, const uint8_t* core, const int32_t* parent, int32_t* border,
+                      cudaStream_t st);
 
 // sDbscan-1NN noise labelling (clusterNoise = 1), after the cluster labels.
 struct NoiseArgs {

@@ -1,0 +1,147 @@
+// The FP32 distance tile shared by the candidate-distance stage (k_dist) and
+// the sampled-neighbourhood block of sngDbscan / sngOptics (k_sng_block):
+// computeDist (src/Utilities.h:212-287) for TM member rows x TX * CN
+// candidate columns.
+//
+// Rows and columns are points of the transformed data (row stride ld, zero
+// padded), named by id in shared memory (-1 for an empty row or column).
+// They are staged through shared memory with cp.async, TK dimensions per
+// stage in STAGES stages; each of the 16 * TX threads owns an 8 x CN block of
+// pairs and accumulates over dimensions in ascending order, one rounding
+// sequence per pair identical to the oracle's, so every distance is
+// bit-identical to the CPU path.
+#pragma once
+
+#include "common.cuh"
+
+namespace sdb {
+namespace dtile {
+
+// Tile rows, dimensions per stage, smem row stride, stages, and the tile
+// grid's candidate columns (and mask bits) per tile.
+constexpr int TM = 128, TK = 32, LDS = TK + 4, STAGES = 2;
+constexpr int TN = 64;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    const int sz = valid ? 16 : 0;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(sz));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+template <int DIST> __device__ __forceinline__ float acc_step(float acc, float a, float b) {
+    if (DIST == DIST_COSINE) {
+        return __fmaf_rn(a, b, acc);
+    } else if (DIST == DIST_L2) {
+        const float t = __fsub_rn(a, b);
+        return __fmaf_rn(t, t, acc);
+    } else if (DIST == DIST_L1) {
+        return __fadd_rn(acc, fabsf(__fsub_rn(a, b)));
+    } else if (DIST == DIST_CHI2) {
+        if (a > 0.0f && b > 0.0f) acc = __fadd_rn(acc, __fdiv_rn(__fmul_rn(a, b), __fadd_rn(a, b)));
+        return acc;
+    } else {  // JS with EPSILON = 1e-6 added to both (src/Utilities.h:248-266)
+        const float x = __fadd_rn(a, 1e-6f), y = __fadd_rn(b, 1e-6f);
+        const float l2 = 0.693147182464599609375f;  // (float)log(2.0)
+        const float s = __fadd_rn(x, y);
+        const float t1 = __fmul_rn(__fdiv_rn(logf(__fdiv_rn(s, x)), l2), x);
+        const float t2 = __fmul_rn(__fdiv_rn(logf(__fdiv_rn(s, y)), l2), y);
+        return __fadd_rn(acc, __fadd_rn(t1, t2));
+    }
+}
+
+template <int DIST> __device__ __forceinline__ float finish(float acc) {
+    if (DIST == DIST_COSINE) return __fsub_rn(1.0f, acc);           // 1 - x.y
+    if (DIST == DIST_L2) return __fsqrt_rn(acc);                    // ||x - y||
+    if (DIST == DIST_L1) return acc;                                 // sum |x - y|
+    if (DIST == DIST_CHI2) return __fsub_rn(1.0f, __fmul_rn(2.0f, acc));  // == (float)(1.0 - 2.0*t), exact
+    return __fsub_rn(1.0f, __fmul_rn(acc, 0.5f));                    // == (float)(1.0 - t/2.0), exact
+}
+
+// One pair on one thread, the same rounding sequence as the tile.
+template <int DIST> __device__ __forceinline__ float pair_distance(const float* __restrict__ x,
+                                                                   const float* __restrict__ y, int d) {
+    float acc = 0.0f;
+    for (int j = 0; j < d; ++j) acc = acc_step<DIST>(acc, __ldg(x + j), __ldg(y + j));
+    return finish<DIST>(acc);
+}
+
+// acc[i][j] = accumulated distance terms of (row ty + 16 i, column tx + TX j)
+// with ty = tid / TX, tx = tid % TX.  As / Bs: STAGES x TM x LDS and
+// STAGES x (TX * CN) x LDS floats of shared memory.  Ends with every copy
+// landed; the caller synchronises before reusing the buffers.
+template <int DIST, int TX, int CN>
+__device__ __forceinline__ void accumulate(const float* __restrict__ Xt, int ld, int d, const int* rowPoint,
+                                           const int* colPoint, float* As, float* Bs, float (&acc)[8][CN]) {
+    constexpr int NT = 16 * TX, TNK = TX * CN;
+    const int tid = threadIdx.x;
+    const int nk = (d + TK - 1) / TK;
+    auto load_stage = [&](int stage, int kc) {
+        float* as = As + stage * TM * LDS;
+        float* bs = Bs + stage * TNK * LDS;
+        const int k0 = kc * TK;
+#pragma unroll
+        for (int idx = tid; idx < TM * TK / 4; idx += NT) {
+            const int row = idx >> 3, c4 = idx & 7;
+            const int p = rowPoint[row];
+            const int col = k0 + c4 * 4;
+            const bool ok = p >= 0 && col < ld;
+            const float* src = ok ? Xt + (size_t)p * ld + col : Xt;
+            cp_async16(as + row * LDS + c4 * 4, src, ok);
+        }
+#pragma unroll
+        for (int idx = tid; idx < TNK * TK / 4; idx += NT) {
+            const int row = idx >> 3, c4 = idx & 7;
+            const int p = colPoint[row];
+            const int col = k0 + c4 * 4;
+            const bool ok = p >= 0 && col < ld;
+            const float* src = ok ? Xt + (size_t)p * ld + col : Xt;
+            cp_async16(bs + row * LDS + c4 * 4, src, ok);
+        }
+    };
+
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < CN; ++j) acc[i][j] = 0.0f;
+
+    const int ty = tid / TX, tx = tid % TX;
+#pragma unroll
+    for (int s = 0; s < STAGES - 1; ++s) {
+        if (s < nk) load_stage(s, s);
+        cp_async_commit();
+    }
+    for (int kc = 0; kc < nk; ++kc) {
+        cp_async_wait<STAGES - 2>();
+        __syncthreads();
+        const int nxt = kc + STAGES - 1;
+        if (nxt < nk) load_stage(nxt % STAGES, nxt);
+        cp_async_commit();
+        const float* as = As + (kc % STAGES) * TM * LDS;
+        const float* bs = Bs + (kc % STAGES) * TNK * LDS;
+#pragma unroll
+        for (int kk = 0; kk < TK; kk += 4) {
+            float4 av[8], bv[CN];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) av[i] = *reinterpret_cast<const float4*>(as + (ty + 16 * i) * LDS + kk);
+#pragma unroll
+            for (int j = 0; j < CN; ++j) bv[j] = *reinterpret_cast<const float4*>(bs + (tx + TX * j) * LDS + kk);
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < CN; ++j) {
+                    float c = acc[i][j];
+                    c = acc_step<DIST>(c, av[i].x, bv[j].x);
+                    c = acc_step<DIST>(c, av[i].y, bv[j].y);
+                    c = acc_step<DIST>(c, av[i].z, bv[j].z);
+                    c = acc_step<DIST>(c, av[i].w, bv[j].w);
+                    acc[i][j] = c;
+                }
+        }
+    }
+    cp_async_wait<0>();
+}
+
+}  // namespace dtile
+}  // namespace sdb

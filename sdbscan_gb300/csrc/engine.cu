@@ -97,7 +97,8 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &aCount, &degree, &core, &parent, &border, &rootFlag, &labels, &nClusters, &scanTmp, &errFlags,
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
             &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig, &Rb, &newMasks, &coreEps, &sampleFlag,
-            &noiseFlag, &noiseCores, &noisePts, &PcT, &numCore, &pairRound};
+            &noiseFlag, &noiseCores, &noisePts, &PcT, &numCore, &pairRound, &sngCols, &sngMult, &sngColOf, &sngExtras,
+            &sngExtraPass, &sngMask, &rowDeg, &colCnt};
 }
 
 // ---------------------------------------------------------------------------
@@ -617,6 +618,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     else haveLabels = true;
     haveFit = true;
     lastOptics = optics;
+    lastSng = false;
     if (p.verbose) {
         std::printf("sdbscan_gb300 %s fit: n=%d d=%d D=%d k=%d m=%d dist=%s eps=%g minPts=%d\n",
                     optics ? "sOPTICS" : "sDBSCAN", n, d, D, k, m, dist_name(p.distance), eps, minPts);
@@ -807,11 +809,18 @@ static sdb_status download(sdb_engine* e, void* dst, const DevBuf& b, size_t byt
     return c == cudaSuccess ? SDB_OK : e->cuda_fail(c, "download");
 }
 
+static sdb_status no_index(sdb_engine* e) {
+    return e->fail(SDB_ERR_STATE, "the last fit was sngDbscan / sngOptics, which builds no index");
+}
 sdb_status sdb_get_topk(sdb_engine* e, int32_t* out) {
-    return e ? download(e, out, e->topK, sizeof(int32_t) * (size_t)e->n * 2 * e->prm.topK) : SDB_ERR_ARG;
+    if (!e) return SDB_ERR_ARG;
+    if (e->lastSng) return no_index(e);
+    return download(e, out, e->topK, sizeof(int32_t) * (size_t)e->n * 2 * e->prm.topK);
 }
 sdb_status sdb_get_topm(sdb_engine* e, int32_t* out) {
-    return e ? download(e, out, e->topM, sizeof(int32_t) * (size_t)e->prm.n_proj * 2 * e->prm.topM) : SDB_ERR_ARG;
+    if (!e) return SDB_ERR_ARG;
+    if (e->lastSng) return no_index(e);
+    return download(e, out, e->topM, sizeof(int32_t) * (size_t)e->prm.n_proj * 2 * e->prm.topM);
 }
 sdb_status sdb_get_core(sdb_engine* e, uint8_t* core, int32_t* degree) {
     if (!e) return SDB_ERR_ARG;
@@ -822,11 +831,13 @@ sdb_status sdb_get_core(sdb_engine* e, uint8_t* core, int32_t* degree) {
 }
 sdb_status sdb_get_core_dist(sdb_engine* e, float* out) {
     if (!e) return SDB_ERR_ARG;
-    if (!e->lastOptics) return e->fail(SDB_ERR_STATE, "core distances exist after sdb_fit_soptics only");
+    if (!e->lastOptics) return e->fail(SDB_ERR_STATE, "core distances exist after an OPTICS fit only");
     return download(e, out, e->coreDist, sizeof(float) * e->n);
 }
 sdb_status sdb_get_projections(sdb_engine* e, float* out) {
-    return e ? download(e, out, e->P, sizeof(float) * (size_t)e->n * e->prm.n_proj) : SDB_ERR_ARG;
+    if (!e) return SDB_ERR_ARG;
+    if (e->lastSng) return no_index(e);
+    return download(e, out, e->P, sizeof(float) * (size_t)e->n * e->prm.n_proj);
 }
 sdb_status sdb_get_counters(sdb_engine* e, int64_t* out, int32_t n_out) {
     if (!e || !out) return SDB_ERR_ARG;

@@ -31,6 +31,7 @@ struct sdb_engine {
     int n = 0, d = 0, device = 0;
     sdb_params prm{};
     bool paramsSet = false;
+    bool sngParamsSet = false;  // set_sngParams (enough for the sng fits)
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[9] = {};
     // host input is uploaded in segments on a second stream, each segment's
@@ -52,10 +53,12 @@ struct sdb_engine {
         members, tileOff, tileList, hubCount, hubOff, hubLists, masks, inRaw, aCount, degree, core, parent, border,
         rootFlag, labels, nClusters, scanTmp, errFlags, counters, E, Rt, signs, compCosh, dists, coreDist, nbOff,
         nbIdx, nbDist, nbFill, hubIdx, kMask, firstMasks, Xb, queue, sweepLabels, sweepNcl, sig, Rb, newMasks,
-        coreEps, sampleFlag, noiseFlag, noiseCores, noisePts, PcT, numCore, pairRound;
+        coreEps, sampleFlag, noiseFlag, noiseCores, noisePts, PcT, numCore, pairRound, sngCols, sngMult, sngColOf,
+        sngExtras, sngExtraPass, sngMask, rowDeg, colCnt;
 
     // results
     bool haveLabels = false, haveOptics = false, haveFit = false, lastOptics = false;
+    bool lastSng = false;  // the last fit was sngDbscan / sngOptics (no index state)
     std::vector<int32_t> hostOrdering;
     std::vector<float> hostReach;
     int32_t* hostErr = nullptr;
@@ -76,6 +79,11 @@ struct sdb_engine {
                    const SweepSpec* sw = nullptr);
     sdb_status check_flags();
     sdb_status optics_stage(const sdb::CoreArgs& ca, int& launches);
+    sdb_status optics_order(int64_t total);
+    // sngDbscan (optics = false; every eps of epsList, labels of eps i to
+    // labelsOut + i n when given) or sngOptics (one eps)
+    sdb_status fit_sng(const float* X, bool xOnDevice, const float* epsList, int nEps, int minPts, bool optics,
+                       int32_t* labelsOut = nullptr, int32_t* nclOut = nullptr);
 
     static float* f32(DevBuf& b) { return static_cast<float*>(b.ptr); }
     static int32_t* i32(DevBuf& b) { return static_cast<int32_t*>(b.ptr); }

@@ -87,5 +87,47 @@ PYBIND11_MODULE(sDbscan, m) {
                 py::gil_scoped_release nogil;
                 s.load_fit_sOptics(dataset, eps, minPts);
             },
+            py::arg("dataset"), py::arg("eps"), py::arg("minPts"))
+        // sngDbscan / sngOptics (python/python_wrapper.cpp:26-27, :56-64)
+        .def("set_sngParams", &sDbscan::set_sngParams, py::arg("distance") = "Cosine", py::arg("samplingProb") = 0.01,
+             py::arg("clusterNoise") = 0, py::arg("verbose") = false, py::arg("output") = "",
+             py::arg("n_threads") = -1, py::arg("random_seed") = -1)
+        .def(
+            "fit_sngDbscan",
+            [](sDbscan& s, const FArray& X, float eps, int minPts) {
+                const float* p = checked(s, X);
+                py::gil_scoped_release nogil;
+                s.fit_sngDbscan(p, eps, minPts);
+            },
+            py::arg("X"), py::arg("eps"), py::arg("minPts"))
+        .def(
+            "test_sngDbscan",
+            [](sDbscan& s, const FArray& X, float eps, float rangeEps, int n_tests, int minPts) {
+                const float* p = checked(s, X);
+                py::gil_scoped_release nogil;
+                s.test_sngDbscan(p, eps, rangeEps, n_tests, minPts);
+            },
+            py::arg("X"), py::arg("eps"), py::arg("rangeEps"), py::arg("n_tests"), py::arg("minPts"))
+        .def(
+            "load_test_sngDbscan",
+            [](sDbscan& s, const std::string& dataset, float eps, float rangeEps, int n_tests, int minPts) {
+                py::gil_scoped_release nogil;
+                s.load_test_sngDbscan(dataset, eps, rangeEps, n_tests, minPts);
+            },
+            py::arg("dataset"), py::arg("eps"), py::arg("rangeEps"), py::arg("n_tests"), py::arg("minPts"))
+        .def(
+            "fit_sngOptics",
+            [](sDbscan& s, const FArray& X, float eps, int minPts) {
+                const float* p = checked(s, X);
+                py::gil_scoped_release nogil;
+                s.fit_sngOptics(p, eps, minPts);
+            },
+            py::arg("X"), py::arg("eps"), py::arg("minPts"))
+        .def(
+            "load_fit_sngOptics",
+            [](sDbscan& s, const std::string& dataset, float eps, int minPts) {
+                py::gil_scoped_release nogil;
+                s.load_fit_sngOptics(dataset, eps, minPts);
+            },
             py::arg("dataset"), py::arg("eps"), py::arg("minPts"));
 }

@@ -167,3 +167,73 @@ void sDbscan::fit_sOptics(const float* X, float eps, int minPts) {
         for (size_t i = 0; i < ordering_.size(); ++i) out << ordering_[i] << " " << reachability_[i] << '\n';
     }
 }
+
+// ---- sngDbscan / sngOptics ------------------------------------------------------
+
+void sDbscan::set_sngParams(std::string dist, float prob, int noiseClustering, bool ver, std::string filename,
+                            int numThreads, int randomSeed) {
+    const int code = dist_code(dist);
+    check(sdb_set_sng_params(eng_, code, prob, noiseClustering, ver ? 1 : 0, numThreads, randomSeed), "set_sngParams");
+    prm_.distance = code;
+    prm_.samplingProb = prob;
+    if (noiseClustering > 0) prm_.clusterNoise = 2;  // src/sDbscan.h:133-134
+    prm_.verbose = ver ? 1 : 0;
+    prm_.n_threads = numThreads;
+    prm_.random_seed = randomSeed;
+    output_ = filename;
+}
+
+// Output name of the sng fits (src/sDbscan.cpp:1171-1175, :1232-1236, :1872-1876).
+std::string sDbscan::sng_file(float eps, int minPts) const {
+    return output_ + "_" + dist_str(prm_.distance) + "_Eps_" + int2str(std::lround(1000 * eps)) + "_MinPts_" +
+           int2str(minPts) + "_Prob_" + int2str(std::lround(1000 * prm_.samplingProb));
+}
+
+void sDbscan::fit_sngDbscan(const float* X, float eps, int minPts) {
+    check(sdb_fit_sngdbscan(eng_, X, eps, minPts), "fit_sngDbscan");
+    prm_.clusterNoise = 0;  // src/sDbscan.cpp:1157
+    labels_.assign(n_, -1);
+    int32_t nc = 0;
+    check(sdb_get_labels(eng_, labels_.data(), &nc), "fit_sngDbscan (labels)");
+    n_clusters_ = nc;
+    if (prm_.verbose) {  // src/sDbscan.cpp:1170-1178
+        std::ofstream out(sng_file(eps, minPts));
+        for (int v : labels_) out << v << '\n';
+    }
+}
+
+void sDbscan::test_sngDbscan(const float* X, float eps, float rangeEps, int n_tests, int minPts) {
+    if (n_tests < 1) throw std::runtime_error("test_sngDbscan: n_tests must be >= 1");
+    std::vector<float> E(n_tests);
+    for (int i = 0; i < n_tests; ++i) E[i] = (float)(eps + 1.0 * i * rangeEps);  // src/sDbscan.cpp:1221
+    std::vector<int32_t> L((size_t)n_tests * n_);
+    std::vector<int32_t> ncl(n_tests);
+    check(sdb_fit_sngdbscan_sweep(eng_, X, E.data(), n_tests, minPts, L.data(), ncl.data()), "test_sngDbscan");
+    for (int i = 0; i < n_tests; ++i) {  // one labels file per eps (src/sDbscan.cpp:1232-1238)
+        std::ofstream out(sng_file(E[i], minPts));
+        for (int j = 0; j < n_; ++j) out << L[(size_t)i * n_ + j] << '\n';
+    }
+    labels_.assign(L.end() - n_, L.end());
+    n_clusters_ = ncl.back();
+}
+
+void sDbscan::load_test_sngDbscan(const std::string& dataset, float eps, float rangeEps, int n_tests, int minPts) {
+    const std::vector<float> X = load_txt(dataset, n_, d_);
+    test_sngDbscan(X.data(), eps, rangeEps, n_tests, minPts);
+}
+
+void sDbscan::fit_sngOptics(const float* X, float eps, int minPts) {
+    check(sdb_fit_sngoptics(eng_, X, eps, minPts), "fit_sngOptics");
+    ordering_.assign(n_, 0);
+    reachability_.assign(n_, 0.0f);
+    check(sdb_get_optics(eng_, ordering_.data(), reachability_.data()), "fit_sngOptics (results)");
+    if (!output_.empty()) {  // src/sDbscan.cpp:1871-1879
+        std::ofstream out(sng_file(eps, minPts));
+        for (size_t i = 0; i < ordering_.size(); ++i) out << ordering_[i] << " " << reachability_[i] << '\n';
+    }
+}
+
+void sDbscan::load_fit_sngOptics(const std::string& dataset, float eps, int minPts) {
+    const std::vector<float> X = load_txt(dataset, n_, d_);
+    fit_sngOptics(X.data(), eps, minPts);
+}

@@ -67,12 +67,25 @@ public:
     void test_sDbscan(const float* X_dxn, float eps, float rangeEps, int n_tests, int minPts);
     void load_test_sDbscan(const std::string& dataset, float eps, float rangeEps, int n_tests, int minPts);
 
+    // sngDbscan / sngOptics (src/sDbscan.h:127-139, :190-201): the sampled
+    // neighbourhood baselines.  With randomSeed >= 0, fit_sngDbscan's labels
+    // equal the reference's; sngOptics shares one seeded sample across points
+    // where the reference draws each point's from std::random_device.
+    void set_sngParams(std::string dist = "Cosine", float prob = 0.01, int noiseClustering = 0, bool ver = false,
+                       std::string filename = "", int numThreads = -1, int randomSeed = -1);
+    void fit_sngDbscan(const float* X_dxn, float eps, int minPts);
+    void test_sngDbscan(const float* X_dxn, float eps, float rangeEps, int n_tests, int minPts);
+    void load_test_sngDbscan(const std::string& dataset, float eps, float rangeEps, int n_tests, int minPts);
+    void fit_sngOptics(const float* X_dxn, float eps, int minPts);
+    void load_fit_sngOptics(const std::string& dataset, float eps, int minPts);
+
     int n_points() const { return n_; }
     int n_features() const { return d_; }
     sdb_engine* engine() { return eng_; }
 
 private:
     void push_params();
+    std::string sng_file(float eps, int minPts) const;
     void check(sdb_status s, const char* what);
     int n_, d_;
     sdb_params prm_;

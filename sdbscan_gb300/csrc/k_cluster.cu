@@ -11,40 +11,12 @@
 //    there is no cluster (:619, :633).
 // Union-find hooks the larger root under the smaller one, so each root is
 // its component's minimum index and ids follow from a prefix sum over roots.
-#include "common.cuh"
+#include "uf.cuh"
 
 #include <climits>
 
 namespace sdb {
 namespace {
-
-__device__ __forceinline__ int load_parent(const int32_t* parent, int x) { return __ldcg(parent + x); }
-
-__device__ int find_root(int32_t* parent, int x) {
-    while (true) {
-        const int px = load_parent(parent, x);
-        if (px == x) return x;
-        const int gx = load_parent(parent, px);
-        if (gx != px) parent[x] = gx;  // path halving: gx is an ancestor of x forever
-        x = px;
-    }
-}
-
-__device__ void unite(int32_t* parent, int a, int b) {
-    while (true) {
-        a = find_root(parent, a);
-        b = find_root(parent, b);
-        if (a == b) return;
-        if (a > b) {
-            const int t = a;
-            a = b;
-            b = t;
-        }
-        const int old = atomicCAS(parent + b, b, a);
-        if (old == b) return;
-        b = old;
-    }
-}
 
 __global__ void k_init(int32_t* parent, int32_t* border, int n, int keepParent) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -219,6 +191,26 @@ int launch_cluster(const ClusterArgs& a, cudaStream_t st) {
     k_labels<<<g, 256, 0, st>>>(a);
     ++launches;
     return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
+}
+
+// The union-find steps for callers with their own edge kernels (sngDbscan).
+int launch_uf_init(int32_t* parent, int32_t* border, int n, cudaStream_t st) {
+    k_init<<<(n + 255) / 256, 256, 0, st>>>(parent, border, n, 0);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int launch_uf_compress(const ClusterArgs& a, cudaStream_t st) {
+    k_compress<<<(a.n + 255) / 256, 256, 0, st>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int launch_cluster_labels(const ClusterArgs& a, cudaStream_t st) {
+    k_root_flags<<<(a.n + 1 + 255) / 256, 256, 0, st>>>(a);
+    if (cudaPeekAtLastError() != cudaSuccess) return -1;
+    const int r = launch_scan_i64(a.rootFlag, a.rootFlag, (size_t)a.n + 1, a.scanTmp, st);
+    if (r < 0) return -1;
+    k_labels<<<(a.n + 255) / 256, 256, 0, st>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? r + 2 : -1;
 }
 
 }  // namespace sdb

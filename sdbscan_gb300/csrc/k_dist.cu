@@ -17,55 +17,17 @@
 //  - inRaw[candidate] += number of members of this tile that pass (the
 //    reverse edges n -> candidate, src/sDbscan.cpp:293-294);
 //  - optionally the distance of every (member, candidate) pair (sOPTICS).
-#include "common.cuh"
+#include "dist_tile.cuh"
 
 namespace sdb {
 namespace {
 
-// Tile rows, dimensions per stage, smem row stride, stages.  The candidate
-// columns per tile are TX * CN (TX column groups of CN columns, 16 row groups
-// of 8 rows): <16, 4> gives 64 columns on 256 threads (any m, one 64-bit mask
-// word per tile) and <10, 5> exactly 50 columns on 160 threads (m in 41..50,
-// no padded columns).
-constexpr int TM = 128, TK = 32, LDS = TK + 4, STAGES = 2;
-constexpr int TN = 64;  // the tile grid's candidate columns (and mask bits) per tile
+using namespace dtile;
 
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    const int sz = valid ? 16 : 0;
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(sz));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
-
-template <int DIST> __device__ __forceinline__ float acc_step(float acc, float a, float b) {
-    if (DIST == DIST_COSINE) {
-        return __fmaf_rn(a, b, acc);
-    } else if (DIST == DIST_L2) {
-        const float t = __fsub_rn(a, b);
-        return __fmaf_rn(t, t, acc);
-    } else if (DIST == DIST_L1) {
-        return __fadd_rn(acc, fabsf(__fsub_rn(a, b)));
-    } else if (DIST == DIST_CHI2) {
-        if (a > 0.0f && b > 0.0f) acc = __fadd_rn(acc, __fdiv_rn(__fmul_rn(a, b), __fadd_rn(a, b)));
-        return acc;
-    } else {  // JS with EPSILON = 1e-6 added to both (src/Utilities.h:248-266)
-        const float x = __fadd_rn(a, 1e-6f), y = __fadd_rn(b, 1e-6f);
-        const float l2 = 0.693147182464599609375f;  // (float)log(2.0)
-        const float s = __fadd_rn(x, y);
-        const float t1 = __fmul_rn(__fdiv_rn(logf(__fdiv_rn(s, x)), l2), x);
-        const float t2 = __fmul_rn(__fdiv_rn(logf(__fdiv_rn(s, y)), l2), y);
-        return __fadd_rn(acc, __fadd_rn(t1, t2));
-    }
-}
-
-template <int DIST> __device__ __forceinline__ float finish(float acc) {
-    if (DIST == DIST_COSINE) return __fsub_rn(1.0f, acc);           // 1 - x.y
-    if (DIST == DIST_L2) return __fsqrt_rn(acc);                    // ||x - y||
-    if (DIST == DIST_L1) return acc;                                 // sum |x - y|
-    if (DIST == DIST_CHI2) return __fsub_rn(1.0f, __fmul_rn(2.0f, acc));  // == (float)(1.0 - 2.0*t), exact
-    return __fsub_rn(1.0f, __fmul_rn(acc, 0.5f));                    // == (float)(1.0 - t/2.0), exact
-}
+// Candidate columns per tile are TX * CN (TX column groups of CN columns, 16
+// row groups of 8 rows): <16, 4> gives 64 columns on 256 threads (any m, one
+// 64-bit mask word per tile) and <10, 5> exactly 50 columns on 160 threads
+// (m in 41..50, no padded columns).
 
 template <int DIST, int TX, int CN>
 __global__ void __launch_bounds__(16 * TX, TX == 10 ? 3 : 2) k_dist(DistArgs a) {
@@ -113,72 +75,9 @@ __global__ void __launch_bounds__(16 * TX, TX == 10 ? 3 : 2) k_dist(DistArgs a) 
     if (tid == 0) passTotal = 0;
     __syncthreads();
 
-    const int nk = (a.d + TK - 1) / TK;
-    auto load_stage = [&](int stage, int kc) {
-        float* as = As + stage * TM * LDS;
-        float* bs = Bs + stage * TNK * LDS;
-        const int k0 = kc * TK;
-#pragma unroll
-        for (int idx = tid; idx < TM * TK / 4; idx += NT) {
-            const int row = idx >> 3, c4 = idx & 7;
-            const int p = rowPoint[row];
-            const int col = k0 + c4 * 4;
-            const bool ok = p >= 0 && col < a.ld;
-            const float* src = ok ? a.Xt + (size_t)p * a.ld + col : a.Xt;
-            cp_async16(as + row * LDS + c4 * 4, src, ok);
-        }
-#pragma unroll
-        for (int idx = tid; idx < TNK * TK / 4; idx += NT) {
-            const int row = idx >> 3, c4 = idx & 7;
-            const int p = colPoint[row];
-            const int col = k0 + c4 * 4;
-            const bool ok = p >= 0 && col < a.ld;
-            const float* src = ok ? a.Xt + (size_t)p * a.ld + col : a.Xt;
-            cp_async16(bs + row * LDS + c4 * 4, src, ok);
-        }
-    };
-
     float acc[8][CN];
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-        for (int j = 0; j < CN; ++j) acc[i][j] = 0.0f;
-
+    accumulate<DIST, TX, CN>(a.Xt, a.ld, a.d, rowPoint, colPoint, As, Bs, acc);
     const int ty = tid / TX, tx = tid % TX;
-#pragma unroll
-    for (int s = 0; s < STAGES - 1; ++s) {
-        if (s < nk) load_stage(s, s);
-        cp_async_commit();
-    }
-    for (int kc = 0; kc < nk; ++kc) {
-        cp_async_wait<STAGES - 2>();
-        __syncthreads();
-        const int nxt = kc + STAGES - 1;
-        if (nxt < nk) load_stage(nxt % STAGES, nxt);
-        cp_async_commit();
-        const float* as = As + (kc % STAGES) * TM * LDS;
-        const float* bs = Bs + (kc % STAGES) * TNK * LDS;
-#pragma unroll
-        for (int kk = 0; kk < TK; kk += 4) {
-            float4 av[8], bv[CN];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) av[i] = *reinterpret_cast<const float4*>(as + (ty + 16 * i) * LDS + kk);
-#pragma unroll
-            for (int j = 0; j < CN; ++j) bv[j] = *reinterpret_cast<const float4*>(bs + (tx + TX * j) * LDS + kk);
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-#pragma unroll
-                for (int j = 0; j < CN; ++j) {
-                    float c = acc[i][j];
-                    c = acc_step<DIST>(c, av[i].x, bv[j].x);
-                    c = acc_step<DIST>(c, av[i].y, bv[j].y);
-                    c = acc_step<DIST>(c, av[i].z, bv[j].z);
-                    c = acc_step<DIST>(c, av[i].w, bv[j].w);
-                    acc[i][j] = c;
-                }
-        }
-    }
-    cp_async_wait<0>();
 
     // epilogue
     int myPass = 0;

@@ -416,6 +416,24 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
     if (l == 0 && localTies) atomicAdd(a.ties, (unsigned long long)localTies);
 }
 
+// transformData alone (src/Utilities.h:289-335) for the fits that use no
+// projections (sngDbscan / sngOptics): Xt[p][e] = X[p][e] / scale[p] for
+// Cosine (norm) and Chi2 / JS (sum), X[p][e] for L1 / L2, zero past d up to
+// ld.  One thread per element of Xt, coalesced.
+__global__ void k_transform_rows(const float* __restrict__ X, int ldx, int n, int d, int ld, int dist,
+                                 const float* __restrict__ scale, float* __restrict__ Xt) {
+    const size_t total = (size_t)n * ld;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int p = (int)(i / ld), e = (int)(i % ld);
+        float t = 0.0f;
+        if (e < d) {
+            t = __ldg(X + (size_t)p * ldx + e);
+            if (dist == DIST_COSINE || dist == DIST_CHI2 || dist == DIST_JS) t = __fdiv_rn(t, scale[p]);
+        }
+        Xt[i] = t;
+    }
+}
+
 template <int NJ, int EMB>
 int launch_project_nje(const ProjectArgs& a, const float* scale, cudaStream_t st) {
     const int warps = 4;
@@ -467,6 +485,17 @@ int launch_project(const ProjectArgs& a, cudaStream_t st) {
         default: return -1;
     }
     return r < 0 ? -1 : r + 1;
+}
+
+int launch_transform(const ProjectArgs& a, cudaStream_t st) {
+    if (a.n <= 0) return 0;
+    k_colstats<<<(a.n + kCsPoints - 1) / kCsPoints, kCsPoints, 0, st>>>(a.X, a.ldx, 0, a.n, a.d, a.dist, a.scale,
+                                                                        a.err);
+    if (cudaPeekAtLastError() != cudaSuccess) return -1;
+    const size_t total = (size_t)a.n * a.ld;
+    const int grid = (int)std::min<size_t>((total + 255) / 256, (size_t)152 * 16);
+    k_transform_rows<<<grid, 256, 0, st>>>(a.X, a.ldx, a.n, a.d, a.ld, a.dist, a.scale, a.Xt);
+    return cudaPeekAtLastError() == cudaSuccess ? 2 : -1;
 }
 
 }  // namespace sdb

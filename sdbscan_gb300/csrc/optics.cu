@@ -95,6 +95,14 @@ sdb_status sdb_engine::optics_stage(const CoreArgs& ca, int& launches) {
     if (r < 0) return fail(SDB_ERR_CUDA, "core distance launch failed");
     launches += r;
 
+    return optics_order(total);
+}
+
+// Downloads the CSR neighbour lists (nbOff / nbIdx / nbDist), core flags and
+// core distances of the last fit and runs the ordering on the host.
+sdb_status sdb_engine::optics_order(int64_t total) {
+    cudaStream_t st = stream;
+    cudaError_t e;
     std::vector<int64_t> hOff(n + 1);
     std::vector<int32_t> hIdx(total);
     std::vector<float> hDist(total), hCd(n);

@@ -68,10 +68,43 @@ def cases():
                                               clusterNoise=1, samplingProb=1.0), 0.2, 12, False
 
 
+def sng_cases():
+    """sngDbscan fixtures: (name, X, distance, samplingProb, eps, minPts).  The
+    reference seeds every point's generator with random_seed (7 here), so its
+    neighbourhoods are reproducible."""
+    X1, _ = ds.cfg1_cosine(2000, 32, seed=11)
+    yield "sng_cosine_2000x32", X1, "Cosine", 0.05, 0.15, 10
+    yield "sng_cosine_p001_2000x32", X1, "Cosine", 0.01, 0.15, 3
+    X6, _ = ds.cfg1_cosine(800, 16, seed=17)
+    yield "sng_cosine_exact_800x16", X6, "Cosine", 1.0, 0.08, 8
+    X5, _ = ds.cfg3_aniso_l2(1500, 16, n_comp=5, scale=0.1, seed=15)
+    yield "sng_l2_1500x16", X5, "L2", 0.1, 0.5, 10
+    X10, _ = ds.cfg4_dirichlet(1500, 64, n_comp=5, conc=10, seed=24)
+    yield "sng_chi2_1500x64", X10, "Chi2", 0.2, 0.2, 15
+
+
+def main_sng(only=()):
+    for name, X, dist, prob, eps, minPts in sng_cases():
+        if only and name not in only:
+            continue
+        n, d = X.shape
+        r = Ref(n, d)
+        r.set_sngParams(dist, prob, 0, False, 1, 7)
+        r.fit_sngDbscan(X, eps, minPts)
+        off, idx = r.neighbors()
+        out = dict(X=X, labels=r.labels_, n_clusters=np.int32(r.n_clusters_), core=r.core(),
+                   core_degree=np.diff(off).astype(np.int32))
+        meta = dict(distance=dist, samplingProb=prob, eps=eps, minPts=minPts, random_seed=7, n_threads=1)
+        out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(name, "n_clusters", r.n_clusters_, "cores", int(out["core"].sum()))
+
+
 def main(only=()):
     """Writes every fixture, or only the named ones."""
     if build_ref() is None:
         sys.exit("the reference sources are not available here; fixtures cannot be regenerated")
+    main_sng(only)
     for name, X, params, eps, minPts, optics in cases():
         if only and name not in only:
             continue

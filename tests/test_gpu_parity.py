@@ -17,7 +17,8 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
+                if not os.path.basename(p).startswith("sng_"))  # sngDbscan fixtures: tests/test_sng*.py
 EXACT_DISTS = ("Cosine", "Chi2")
 
 

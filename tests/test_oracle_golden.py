@@ -16,7 +16,8 @@ import pytest
 
 from oracle.oracle import fht_dim
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
+                if not os.path.basename(p).startswith("sng_"))  # sngDbscan fixtures: tests/test_sng*.py
 
 
 def _load(path):
