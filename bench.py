@@ -55,6 +55,10 @@ FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # nominal FP32 CUDA-core peak
 # `python -m sdbscan_gb300.profile_fit 1000000 0` (profiles/k_dist_fp32_cfg2.md):
 # 64.44 GB read + 0.646 GB written.
 K_DIST_TRAFFIC_1M = 64.44e9 + 0.646e9
+# sngDBSCAN, the reference's sampling baseline that its benchmark loop runs
+# next to fit_sDbscan (src/main.cpp:57-73): samplingProb 0.01 (the default,
+# 10,000 draws per point at 1M points), seed 42, the workload's eps / minPts.
+SNG_PROB, SNG_SEED = 0.01, 42
 
 
 def _peaks():
@@ -344,6 +348,77 @@ def _cpu_batched(n_sets=6):
                       f"(oracle/ restatement, OpenMP, {threads} threads; sweep {sweep_s:.1f} s, fits {fits_s:.1f} s)"}
 
 
+def _cpu_sng(cfg, n_sample=10000):
+    """The oracle's sngDbscan (point-by-point restatement of
+    sng_findCorePoints) on n_sample points of the workload's law with the
+    same number of draws per point as the full workload (ceil(0.01 n) =
+    10,000 at 1M points), all host threads.  Points/s."""
+    from oracle.oracle import Port, build_port
+    build_port()
+    port = Port()
+    threads = os.cpu_count() or 1
+    Xh = _host_data(cfg, n_sample)
+    draws = -(-cfg["n"] * SNG_PROB // 1)
+    prob = float(draws) / n_sample
+    t0 = time.perf_counter()
+    port.fit_sngdbscan(Xh, cfg["eps"], cfg["minPts"], dist=cfg["distance"], samplingProb=prob, seed=SNG_SEED,
+                       threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n_sample / dt, "unit": "points/s", "cores": threads, "kind": "port",
+            "sample": f"fit_sngDbscan on {n_sample} points of the workload's law, samplingProb {prob:g} "
+                      f"({int(draws)} draws per point, as the full workload), oracle/ restatement, OpenMP, "
+                      f"{threads} threads, {dt:.1f} s"}
+
+
+def run_sng(args, local, X, cfg, cpu=True):
+    """sngDBSCAN on the headline data (n x d resident in HBM): one step =
+    one fit_sngDbscan (transform, sample, dense distance block, degrees,
+    union-find labels).  Dominant kernel: k_sng_block, n x (sampled points) x d."""
+    import torch
+    from sdbscan_gb300 import capi
+    n, d = X.shape
+    eng = capi.Engine(n, d, device=local)
+    eng.set_sng_params(distance=cfg["distance"], samplingProb=SNG_PROB, random_seed=SNG_SEED)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=f"cuda:{local}")
+    for _ in range(max(1, min(args.warmup, 2))):
+        eng.fit_sngdbscan_device(X.data_ptr(), cfg["eps"], cfg["minPts"])
+    torch.cuda.synchronize()
+    steps = max(1, min(args.steps, 3))
+    st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stages, launches = {}, 0
+    st.record(stream)
+    for _ in range(steps):
+        eng.fit_sngdbscan_device(X.data_ptr(), cfg["eps"], cfg["minPts"])
+        for k_, v_ in eng.stage_ms().items():
+            stages[k_] = stages.get(k_, 0.0) + v_ / steps
+        launches += eng.counters()["launches"]
+    en.record(stream)
+    torch.cuda.synchronize()
+    ms = st.elapsed_time(en) / steps
+    c = eng.counters()
+    labels, ncl = eng.labels()
+    core, _ = eng.core()
+    eng.close()
+    flops = float(DIST_FLOPS[cfg["distance"]]) * n * c["sng_sampled"] * d
+    achieved = flops / (stages["distances"] / 1e3) / 1e12
+    out = {"metric": "points/sec fit_sngDbscan (sampled-neighbourhood baseline)", "value": n / (ms / 1e3),
+           "unit": "points/s", "ms_per_step": ms, "steps": steps, "gpu_launches": launches,
+           "config": {"samplingProb": SNG_PROB, "random_seed": SNG_SEED, "eps": cfg["eps"], "minPts": cfg["minPts"],
+                      "draws_per_point": int(-(-n * SNG_PROB // 1)), "distinct_sampled": c["sng_sampled"],
+                      "extra_draws": c["sng_extra"]},
+           "roofline": {"bound": "fp32", "kernel": f"k_sng_block<{cfg['distance']}>", "achieved": achieved,
+                        "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": achieved / FP32_PEAK_TFLOPS,
+                        "traffic": None, "flops_per_launch": flops, "kernel_ms": stages["distances"],
+                        "peak_source": "nominal FP32 CUDA-core peak (152 SMs x 128 lanes x 2 flop x 2.07 GHz)"},
+           "stage_ms": stages,
+           "result": {"n_clusters": int(ncl), "cores": int(core.sum()), "noise": int((labels < 0).sum())},
+           "cpu_baseline": None}
+    if cpu:
+        out["cpu_baseline"] = _subprocess_json([sys.executable, os.path.abspath(__file__), "--impl", "reference",
+                                                "--config", str(args.config), "--sng-cpu"])
+    return out
+
+
 def run_ours(args, cfg):
     import numpy as np
     import torch
@@ -470,6 +545,9 @@ def run_ours(args, cfg):
     assert all(np.array_equal(a, b) for a, b in zip(res_e2e[:1], res[:1])), "host-input and device-input fits disagree"
     d2h = n * 8 if optics else n * 4 + 4
 
+    sng = None
+    if not args.no_sng and cfg["workload"].startswith("cfg2"):
+        sng = run_sng(args, local, X, cfg, cpu=ws == 1 and not args.no_cpu)
     batched = None
     if not args.no_batched and cfg["workload"].startswith("cfg2"):
         batched = run_batched(args, local, cpu=ws == 1 and not args.no_cpu)
@@ -525,6 +603,7 @@ def run_ours(args, cfg):
         "stage_ms": stages,
         "bf16_screening": bf16,
         "batched": batched,
+        "sng": sng,
         "result": ({"reachable": int((res[1] >= 0).sum()), "max_reachability": float(res[1].max())} if optics else
                    {"n_clusters": res[1], "noise": int((labels < 0).sum())}) |
                   {"topk_ties": counters["topk_ties"], "topm_ties": counters["topm_ties"],
@@ -548,10 +627,15 @@ def main():
     ap.add_argument("--no-bf16", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-cpu", action="store_true", help="(reference arm) time the config-5 CPU baseline only")
+    ap.add_argument("--no-sng", action="store_true")
+    ap.add_argument("--sng-cpu", action="store_true", help="(reference arm) time the sngDbscan CPU baseline only")
     args = ap.parse_args()
     cfg = WORKLOADS[args.config]
     if args.impl == "reference" and args.batched_cpu:
         print(json.dumps(_cpu_batched()))
+        return 0
+    if args.impl == "reference" and args.sng_cpu:
+        print(json.dumps(_cpu_sng(cfg)))
         return 0
     if args.impl == "reference":
         return run_reference(args, cfg)

@@ -189,7 +189,9 @@ sdb_status sdb_get_projections(sdb_engine* e, float* proj);
  * pairs within eps. out[0]=topk ties, out[1]=topm ties, out[2]=launches,
  * out[3]=directed candidate pairs within eps (with duplicates),
  * out[4]=pairs re-decided in FP32 by the BF16 screening mode,
- * out[5]=BF16 screening stages redone on the plain path (engine lifetime). */
+ * out[5]=BF16 screening stages redone on the plain path (engine lifetime),
+ * out[6]=distinct sampled points and out[7]=extra draws of the last
+ * sngDbscan / sngOptics fit. */
 sdb_status sdb_get_counters(sdb_engine* e, int64_t* out, int32_t n_out);
 
 /* Device time of each stage of the last fit in milliseconds (CUDA events):

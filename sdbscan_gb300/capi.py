@@ -251,10 +251,10 @@ class Engine:
         return out
 
     def counters(self) -> dict:
-        out = np.zeros(6, np.int64)
-        self._check(self.L.sdb_get_counters(self.h, _ptr(out), 6))
+        out = np.zeros(8, np.int64)
+        self._check(self.L.sdb_get_counters(self.h, _ptr(out), 8))
         return dict(topk_ties=int(out[0]), topm_ties=int(out[1]), launches=int(out[2]), pairs=int(out[3]),
-                    rechecked=int(out[4]), fallbacks=int(out[5]))
+                    rechecked=int(out[4]), fallbacks=int(out[5]), sng_sampled=int(out[6]), sng_extra=int(out[7]))
 
     def stage_ms(self) -> dict:
         out = np.zeros(9, np.float32)

@@ -841,9 +841,10 @@ sdb_status sdb_get_projections(sdb_engine* e, float* out) {
 }
 sdb_status sdb_get_counters(sdb_engine* e, int64_t* out, int32_t n_out) {
     if (!e || !out) return SDB_ERR_ARG;
-    int64_t v[6] = {(int64_t)e->hostCounters[0], (int64_t)e->hostCounters[1], (int64_t)e->launchCount,
-                    (int64_t)e->hostCounters[3], (int64_t)e->hostCounters[4], (int64_t)e->fallbacks};
-    for (int i = 0; i < n_out && i < 6; ++i) out[i] = v[i];
+    int64_t v[8] = {(int64_t)e->hostCounters[0], (int64_t)e->hostCounters[1], (int64_t)e->launchCount,
+                    (int64_t)e->hostCounters[3], (int64_t)e->hostCounters[4], (int64_t)e->fallbacks,
+                    (int64_t)e->sngColsLast, (int64_t)e->sngExtraLast};
+    for (int i = 0; i < n_out && i < 8; ++i) out[i] = v[i];
     return SDB_OK;
 }
 sdb_status sdb_get_stage_ms(sdb_engine* e, float* ms, int32_t n_ms) {

@@ -65,6 +65,7 @@ struct sdb_engine {
     unsigned long long* hostCounters = nullptr;
     int launchCount = 0;
     int64_t fallbacks = 0;  // BF16 screening fits redone on the plain path
+    int sngColsLast = 0, sngExtraLast = 0;  // sampled columns and extra draws of the last sng fit
     int distVariant = 0;    // plain distance tile shape (DistArgs::variant), set by the batch's autotuner
     float stageMs[9] = {};
 

@@ -116,6 +116,8 @@ sdb_status sdb_engine::fit_sng(const float* X, bool xOnDevice, const float* epsL
     const int nU = (int)smp.cols.size();
     const int nct = (nU + 63) / 64;
     const int nExtra = (int)smp.extras.size();
+    sngColsLast = nU;
+    sngExtraLast = nExtra;
 
     bool ok = true;
     if (!xOnDevice) ok &= ensure(Xin, sizeof(float) * (size_t)n * d);
