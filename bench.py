@@ -374,6 +374,7 @@ def run_sng(args, local, X, cfg, cpu=True):
     """sngDBSCAN on the headline data (n x d resident in HBM): one step =
     one fit_sngDbscan (transform, sample, dense distance block, degrees,
     union-find labels).  Dominant kernel: k_sng_block, n x (sampled points) x d."""
+    import numpy as np
     import torch
     from sdbscan_gb300 import capi
     n, d = X.shape
@@ -398,9 +399,37 @@ def run_sng(args, local, X, cfg, cpu=True):
     c = eng.counters()
     labels, ncl = eng.labels()
     core, _ = eng.core()
-    eng.close()
     flops = float(DIST_FLOPS[cfg["distance"]]) * n * c["sng_sampled"] * d
     achieved = flops / (stages["distances"] / 1e3) / 1e12
+    # BF16 screening (Cosine): the block on the tensor cores, pairs near eps
+    # re-decided in FP32; the labels must equal the FP32 fit's
+    bf16 = None
+    if cfg["distance"] == "Cosine" and not args.no_bf16:
+        eng.set_precision(capi.PREC_BF16)
+        for _ in range(max(1, min(args.warmup, 2))):
+            eng.fit_sngdbscan_device(X.data_ptr(), cfg["eps"], cfg["minPts"])
+        torch.cuda.synchronize()
+        bstages = {}
+        st.record(stream)
+        for _ in range(steps):
+            eng.fit_sngdbscan_device(X.data_ptr(), cfg["eps"], cfg["minPts"])
+            for k_, v_ in eng.stage_ms().items():
+                bstages[k_] = bstages.get(k_, 0.0) + v_ / steps
+        en.record(stream)
+        torch.cuda.synchronize()
+        bms = st.elapsed_time(en) / steps
+        bl, bn = eng.labels()
+        bc = eng.counters()
+        _, bf16_peak, src = _peaks()
+        bach = 2.0 * n * c["sng_sampled"] * d / (bstages["distances"] / 1e3) / 1e12
+        bf16 = {"value": n / (bms / 1e3), "unit": "points/s", "ms_per_step": bms, "stage_ms": bstages,
+                "labels_identical": bool(np.array_equal(bl, labels)) and bn == ncl,
+                "rechecked_pairs": bc["rechecked"], "fallbacks": bc["fallbacks"],
+                "roofline": {"bound": "tensor", "kernel": "distance stage: k_sng_tc + k_sng_recheck",
+                             "achieved": bach, "peak": bf16_peak, "unit": "TFLOP/s", "frac": bach / bf16_peak,
+                             "traffic": None, "stage_ms": bstages["distances"],
+                             "peak_source": f"{src} bf16_tflops_sustained (timed inside the fit)"}}
+    eng.close()
     out = {"metric": "points/sec fit_sngDbscan (sampled-neighbourhood baseline)", "value": n / (ms / 1e3),
            "unit": "points/s", "ms_per_step": ms, "steps": steps, "gpu_launches": launches,
            "config": {"samplingProb": SNG_PROB, "random_seed": SNG_SEED, "eps": cfg["eps"], "minPts": cfg["minPts"],
@@ -412,6 +441,7 @@ def run_sng(args, local, X, cfg, cpu=True):
                         "peak_source": "nominal FP32 CUDA-core peak (152 SMs x 128 lanes x 2 flop x 2.07 GHz)"},
            "stage_ms": stages,
            "result": {"n_clusters": int(ncl), "cores": int(core.sum()), "noise": int((labels < 0).sum())},
+           "bf16_screening": bf16,
            "cpu_baseline": None}
     if cpu:
         out["cpu_baseline"] = _subprocess_json([sys.executable, os.path.abspath(__file__), "--impl", "reference",

@@ -84,6 +84,11 @@ void sdb_engine_destroy(sdb_engine* e);
  * set_clusterNoise  (src/sDbscan.h:79-124, :170-180). */
 sdb_status sdb_set_params(sdb_engine* e, const sdb_params* p);
 
+/* set_precision: SDB_PREC_FP32 or SDB_PREC_BF16 alone, without the index
+ * parameter checks of sdb_set_params (for the sng fits).  No reference
+ * counterpart (the reference computes in FP32 only). */
+sdb_status sdb_set_precision(sdb_engine* e, int32_t precision);
+
 /* fit_sDbscan(const Ref<const MatrixXf>& X, float eps, int minPts)
  * (src/sDbscan.h:183, src/sDbscan.cpp:830-890).  X_host: d x n column-major
  * host memory (pinned memory makes the upload faster).  Results stay in the
@@ -138,6 +143,8 @@ sdb_status sdb_set_sng_params(sdb_engine* e, int32_t distance, float samplingPro
  * seed is shared by all points.  Switches clusterNoise to 0 (src/sDbscan.cpp:1157).
  * Results: sdb_get_labels, sdb_get_core (neighbourhood sizes with repeats). */
 sdb_status sdb_fit_sngdbscan(sdb_engine* e, const float* X_host, float eps, int32_t minPts);
+/* (With SDB_PREC_BF16 and Cosine the distance block is screened on the tensor
+ * cores and every pair near eps re-decided in FP32: the same labels.) */
 sdb_status sdb_fit_sngdbscan_device(sdb_engine* e, const float* X_device, float eps, int32_t minPts);
 
 /* test_sngDbscan(X, eps, rangeEps, n_tests, minPts)  (src/sDbscan.h:193,

@@ -26,7 +26,7 @@ EXPORTS = ["sdb_params_default", "sdb_engine_create", "sdb_engine_destroy", "sdb
            "sdb_fit_sdbscan_sweep", "sdb_batch_create", "sdb_batch_run", "sdb_batch_labels", "sdb_batch_lanes",
            "sdb_batch_destroy", "sdb_batch_last_error", "sdb_load_txt",
            "sdb_batch_tile_variant", "sdb_set_sng_params", "sdb_fit_sngdbscan", "sdb_fit_sngdbscan_device",
-           "sdb_fit_sngdbscan_sweep", "sdb_fit_sngoptics", "sdb_fit_sngoptics_device"]
+           "sdb_fit_sngdbscan_sweep", "sdb_fit_sngoptics", "sdb_fit_sngoptics_device", "sdb_set_precision"]
 
 
 class SdbParams(ctypes.Structure):
@@ -79,6 +79,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.sdb_fit_sdbscan_sweep.argtypes = [vp, vp, vp, i32, i32, vp, vp]
     L.sdb_fit_sngdbscan_sweep.argtypes = [vp, vp, vp, i32, i32, vp, vp]
     L.sdb_set_sng_params.argtypes = [vp, i32, f32, i32, i32, i32, i32]
+    L.sdb_set_precision.argtypes = [vp, i32]
     L.sdb_batch_create.argtypes = [i32, vp, vp, vp, ctypes.POINTER(SdbParams), vp, i32, i32, i32,
                                    ctypes.POINTER(vp)]
     L.sdb_batch_run.argtypes = [vp, ctypes.POINTER(f32)]
@@ -177,6 +178,11 @@ class Engine:
         p.n_threads, p.random_seed = n_threads, random_seed
         if clusterNoise > 0:
             p.clusterNoise = 2
+
+    def set_precision(self, precision: int):
+        """PREC_FP32 or PREC_BF16 alone (no index parameter checks)."""
+        self._check(self.L.sdb_set_precision(self.h, precision))
+        self.params.precision = precision
 
     def fit_sngdbscan(self, X: np.ndarray, eps: float, minPts: int):
         X = self._host(X)

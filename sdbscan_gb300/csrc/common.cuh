@@ -326,12 +326,21 @@ struct SngArgs {
     int32_t* nbIdx;
     float* nbDist;
     int32_t* err;          // set when a list would overflow its slots
+    const int32_t* gate;   // optional: the FP32 block runs only if *gate != 0 (the BF16 screening failed)
+    const uint64_t* heavy; // nct words: bit set for the columns drawn more than once (null: none)
 };
 // First block pass: pass bits (mask may be null), row degrees, column counts.
 int launch_sng_block(const SngArgs& a, cudaStream_t st);
 // Second block pass (sngOptics): every passing pair into the CSR lists.
 int launch_sng_emit(const SngArgs& a, cudaStream_t st);
 int launch_sng_extras(const SngArgs& a, cudaStream_t st);
+// BF16 screening of the block (Cosine, sngDbscan): Ub = BF16 sampled rows
+// (nU x ldb); then the tensor-core block, the exact re-decision of the queued
+// pairs and, when the screening failed (*gate != 0), the reset of the counts
+// before the gated FP32 block.
+int launch_sng_gather_bf16(const SngArgs& a, void* Ub, int ldb, cudaStream_t st);
+int launch_sng_tc(const SngArgs& a, const void* Xb, const void* Ub, int ldb, uint64_t* queue, int64_t qcap,
+                  unsigned long long* qcount, int32_t* gate, cudaStream_t st);
 int launch_sng_col_of(const SngArgs& a, int32_t* colOf, cudaStream_t st);
 // degree / core flags: sngDbscan counts draws (weights), sngOptics distinct neighbours
 int launch_sng_degree(const SngArgs& a, int exact, int optics, int minPts, int32_t* degree, uint8_t* core,

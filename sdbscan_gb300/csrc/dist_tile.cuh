@@ -67,6 +67,37 @@ template <int DIST> __device__ __forceinline__ float pair_distance(const float* 
     return finish<DIST>(acc);
 }
 
+// Exact Cosine distances of 32 pairs, one per lane of the calling warp:
+// rows[0..31] point at the lanes' first rows, rows[32..63] at their second
+// rows (transformed data, stride ld, zero padded; rows in the warp's shared
+// memory, written before the call and synchronised with __syncwarp).  Both
+// rows of every pair are staged through tile (64 x 33 floats of the warp's
+// shared memory) 32 dimensions at a time with coalesced loads, the next chunk
+// prefetched into registers; each lane runs its pair's sequential fmaf chain
+// in ascending dimension order (fmaf(0, 0, s) = s past d), the plain path's
+// arithmetic.  Returns 1 - dot.
+__device__ __forceinline__ float warp_staged_cosine(const float* const* rows, float (*tile)[33], int ld) {
+    const int lane = threadIdx.x & 31;
+    float stage[64];
+#pragma unroll
+    for (int r = 0; r < 64; ++r) stage[r] = lane < ld ? __ldg(rows[r] + lane) : 0.0f;
+    float s = 0.0f;
+    for (int c = 0; c < ld; c += 32) {
+#pragma unroll
+        for (int r = 0; r < 64; ++r) tile[r][lane] = stage[r];
+        __syncwarp();
+        const int cn = c + 32 + lane;
+        if (c + 32 < ld) {
+#pragma unroll
+            for (int r = 0; r < 64; ++r) stage[r] = cn < ld ? __ldg(rows[r] + cn) : 0.0f;
+        }
+#pragma unroll
+        for (int t = 0; t < 32; ++t) s = __fmaf_rn(tile[lane][t], tile[32 + lane][t], s);
+        __syncwarp();
+    }
+    return __fsub_rn(1.0f, s);
+}
+
 // acc[i][j] = accumulated distance terms of (row ty + 16 i, column tx + TX j)
 // with ty = tid / TX, tx = tid % TX.  As / Bs: STAGES x TM x LDS and
 // STAGES x (TX * CN) x LDS floats of shared memory.  Ends with every copy

@@ -98,7 +98,7 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
             &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig, &Rb, &newMasks, &coreEps, &sampleFlag,
             &noiseFlag, &noiseCores, &noisePts, &PcT, &numCore, &pairRound, &sngCols, &sngMult, &sngColOf, &sngExtras,
-            &sngExtraPass, &sngMask, &rowDeg, &colCnt};
+            &sngExtraPass, &sngMask, &rowDeg, &colCnt, &sngUb, &sngHeavy};
 }
 
 // ---------------------------------------------------------------------------
@@ -634,6 +634,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
 sdb_status sdb_engine::check_flags() {
     if (hostErr[4]) fallbacks += 1;  // the screened stage was redone on the plain path
     if (hostErr[5]) fallbacks += 1;  // the tensor-core embedding was redone in FP32
+    if (hostErr[7]) fallbacks += 1;  // the sngDbscan block was redone in FP32
     if (hostErr[0]) return fail(SDB_ERR_NEGATIVE, "X is not non-negative (Chi2/JS need nonnegative data)");
     if (hostErr[1])
         return fail(SDB_ERR_ZERO_POINT, prm.distance == SDB_COSINE ? "X has a point of zero norm (Cosine)"
@@ -729,6 +730,13 @@ sdb_status sdb_set_params(sdb_engine* e, const sdb_params* p) {
     sdb_status s = e->derive();
     if (s != SDB_OK) e->paramsSet = false;
     return s;
+}
+
+sdb_status sdb_set_precision(sdb_engine* e, int32_t precision) {
+    if (!e) return SDB_ERR_ARG;
+    if (precision != SDB_PREC_FP32 && precision != SDB_PREC_BF16) return e->fail(SDB_ERR_ARG, "unknown precision");
+    e->prm.precision = precision;
+    return SDB_OK;
 }
 
 sdb_status sdb_fit_sdbscan(sdb_engine* e, const float* X, float eps, int32_t minPts) {

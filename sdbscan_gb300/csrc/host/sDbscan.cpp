@@ -92,7 +92,10 @@ void sDbscan::set_topK(int k) { prm_.topK = k; push_params(); }
 void sDbscan::set_proj(int p) { prm_.n_proj = p; push_params(); }
 void sDbscan::set_clusterNoise(int c) { prm_.clusterNoise = c; push_params(); }
 void sDbscan::set_threads(int t) { prm_.n_threads = t; }
-void sDbscan::set_precision(int precision) { prm_.precision = precision; push_params(); }
+void sDbscan::set_precision(int precision) {
+    check(sdb_set_precision(eng_, precision), "set_precision");
+    prm_.precision = precision;
+}
 
 void sDbscan::fit_sDbscan(const float* X, float eps, int minPts) {
     check(sdb_fit_sdbscan(eng_, X, eps, minPts), "fit_sDbscan");

@@ -27,6 +27,7 @@
 #include <cuda_bf16.h>
 
 #include "common.cuh"
+#include "dist_tile.cuh"
 #include "tc_common.cuh"
 
 namespace sdb {
@@ -275,15 +276,9 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
 }
 
-// Exact FP32 re-decision of the queued pairs: the plain path's sequential
-// fmaf dot over ascending dimensions, so the decision equals k_dist's.
-// Exact re-decision of the queued pairs.  A warp takes 32 queue entries, one
-// per lane.  Both rows of every pair are staged through shared memory 32
-// dimensions at a time with coalesced 128-byte row loads (the next chunk is
-// loaded into registers while the current one is consumed), and each lane runs
-// its own pair's sequential fmaf chain out of shared memory in ascending
-// dimension order: the plain path's arithmetic, so the same bits.  Dimensions
-// past d are the zero padding of Xt, and fmaf(0, 0, s) = s.
+// Exact re-decision of the queued pairs: a warp takes 32 queue entries, one
+// per lane, and computes their distances with the plain path's sequential
+// FP32 dot (dtile::warp_staged_cosine), so the decision equals k_dist's.
 constexpr int RC_WARPS = 4;
 
 __global__ void __launch_bounds__(RC_WARPS * 32) k_recheck(DistArgs a, const uint64_t* __restrict__ queue,
@@ -310,24 +305,7 @@ __global__ void __launch_bounds__(RC_WARPS * 32) k_recheck(DistArgs a, const uin
         rows[w][lane] = a.Xt + (size_t)p * a.ld;
         rows[w][32 + lane] = a.Xt + (size_t)q * a.ld;
         __syncwarp();
-        float stage[64];
-#pragma unroll
-        for (int r = 0; r < 64; ++r) stage[r] = lane < a.ld ? __ldg(rows[w][r] + lane) : 0.0f;
-        float s = 0.0f;
-        for (int c = 0; c < a.ld; c += 32) {
-#pragma unroll
-            for (int r = 0; r < 64; ++r) tile[w][r][lane] = stage[r];
-            __syncwarp();
-            const int cn = c + 32 + lane;
-            if (c + 32 < a.ld) {
-#pragma unroll
-                for (int r = 0; r < 64; ++r) stage[r] = cn < a.ld ? __ldg(rows[w][r] + cn) : 0.0f;
-            }
-#pragma unroll
-            for (int t = 0; t < 32; ++t) s = __fmaf_rn(tile[w][lane][t], tile[w][32 + lane][t], s);
-            __syncwarp();
-        }
-        const float dist = __fsub_rn(1.0f, s);
+        const float dist = dtile::warp_staged_cosine(rows[w], tile[w], a.ld);
         if (a.dists != nullptr) {  // eps sweep: store the exact distance; masks follow per eps
             if (valid) a.dists[((size_t)p * 2 * a.k + slot) * a.m + col] = dist;
             __syncwarp();

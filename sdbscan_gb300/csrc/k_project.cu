@@ -419,18 +419,36 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
 // transformData alone (src/Utilities.h:289-335) for the fits that use no
 // projections (sngDbscan / sngOptics): Xt[p][e] = X[p][e] / scale[p] for
 // Cosine (norm) and Chi2 / JS (sum), X[p][e] for L1 / L2, zero past d up to
-// ld.  One thread per element of Xt, coalesced.
+// ld.  A warp per row, four elements per lane access (16-byte loads and
+// stores when the rows are 16-byte aligned), rows grid-stride.
 __global__ void k_transform_rows(const float* __restrict__ X, int ldx, int n, int d, int ld, int dist,
                                  const float* __restrict__ scale, float* __restrict__ Xt) {
-    const size_t total = (size_t)n * ld;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const int p = (int)(i / ld), e = (int)(i % ld);
-        float t = 0.0f;
-        if (e < d) {
-            t = __ldg(X + (size_t)p * ldx + e);
-            if (dist == DIST_COSINE || dist == DIST_CHI2 || dist == DIST_JS) t = __fdiv_rn(t, scale[p]);
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const bool divide = dist == DIST_COSINE || dist == DIST_CHI2 || dist == DIST_JS;
+    const bool vec = (ldx & 3) == 0 && (d & 3) == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < n; p += warps) {
+        const float sc = divide ? scale[p] : 1.0f;
+        const float* x = X + (size_t)p * ldx;
+        float* y = Xt + (size_t)p * ld;
+        for (int e = lane * 4; e < ld; e += 128) {  // ld is a multiple of 4
+            float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (vec && e + 3 < d) {
+                v = __ldg(reinterpret_cast<const float4*>(x + e));
+            } else {
+                if (e < d) v.x = __ldg(x + e);
+                if (e + 1 < d) v.y = __ldg(x + e + 1);
+                if (e + 2 < d) v.z = __ldg(x + e + 2);
+                if (e + 3 < d) v.w = __ldg(x + e + 3);
+            }
+            if (divide) {  // padding stays 0 (0 / sc = 0 for the sc > 0 the checks allow)
+                v.x = e < d ? __fdiv_rn(v.x, sc) : 0.0f;
+                v.y = e + 1 < d ? __fdiv_rn(v.y, sc) : 0.0f;
+                v.z = e + 2 < d ? __fdiv_rn(v.z, sc) : 0.0f;
+                v.w = e + 3 < d ? __fdiv_rn(v.w, sc) : 0.0f;
+            }
+            *reinterpret_cast<float4*>(y + e) = v;
         }
-        Xt[i] = t;
     }
 }
 
@@ -492,8 +510,8 @@ int launch_transform(const ProjectArgs& a, cudaStream_t st) {
     k_colstats<<<(a.n + kCsPoints - 1) / kCsPoints, kCsPoints, 0, st>>>(a.X, a.ldx, 0, a.n, a.d, a.dist, a.scale,
                                                                         a.err);
     if (cudaPeekAtLastError() != cudaSuccess) return -1;
-    const size_t total = (size_t)a.n * a.ld;
-    const int grid = (int)std::min<size_t>((total + 255) / 256, (size_t)152 * 16);
+    if (a.ld & 3) return -1;
+    const int grid = (int)std::min<int64_t>(((int64_t)a.n + 7) / 8, (int64_t)152 * 16);
     k_transform_rows<<<grid, 256, 0, st>>>(a.X, a.ldx, a.n, a.d, a.ld, a.dist, a.scale, a.Xt);
     return cudaPeekAtLastError() == cudaSuccess ? 2 : -1;
 }

@@ -45,6 +45,7 @@ size_t block_smem() {
 // (a few MB) stay L2-resident.
 template <int DIST, bool EMIT>
 __global__ void __launch_bounds__(kNT, 2) k_sng_block(SngArgs a) {
+    if (a.gate != nullptr && __ldg(a.gate) == 0) return;  // the BF16 screening succeeded
     extern __shared__ __align__(16) float sm[];
     float* As = sm;                           // STAGES x TM x LDS
     float* Bs = As + STAGES * TM * LDS;       // STAGES x 64 x LDS
@@ -188,17 +189,34 @@ __global__ void k_sng_degree(SngArgs a, int exact, int optics, int minPts, int32
     core[p] = deg >= minPts - 1 ? 1 : 0;
 }
 
-// Thread per row: core rows unite with their passing core columns.
-__global__ void k_sng_union(SngArgs a, const uint8_t* __restrict__ core, int32_t* parent) {
+// Thread per row, 256 consecutive rows per CTA, walking the mask words in
+// step: for each word with a passing bit in the CTA, the roots of its 64
+// columns are found once and cached in shared memory, and a core row unites
+// only where its own root differs from a passing core column's cached root.
+// A cached value is an ancestor of its column (parents only move up), so
+// equality proves the same set; a stale value only costs a redundant unite.
+__global__ void __launch_bounds__(256) k_sng_union(SngArgs a, const uint8_t* __restrict__ core, int32_t* parent) {
+    __shared__ int croot[kTNK];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.n || !core[p]) return;
+    const bool active = p < a.n && core[p];
+    if (!__syncthreads_or(active)) return;
+    int rp = active ? find_root(parent, p) : -1;
     for (int ct = 0; ct < a.nct; ++ct) {
-        uint64_t w = __ldg(reinterpret_cast<const unsigned long long*>(a.mask) + (size_t)ct * a.n + p);
+        uint64_t w = active ? __ldg(reinterpret_cast<const unsigned long long*>(a.mask) + (size_t)ct * a.n + p) : 0;
+        if (!__syncthreads_or(w != 0)) continue;  // also orders the previous word's reads of croot
+        if (threadIdx.x < kTNK) {
+            const int c = ct * kTNK + threadIdx.x;
+            const int q = c < a.nU ? __ldg(a.cols + c) : -1;
+            croot[threadIdx.x] = (q >= 0 && core[q]) ? find_root(parent, q) : -1;
+        }
+        __syncthreads();
         while (w) {
             const int j = __ffsll((long long)w) - 1;
             w &= w - 1;
-            const int q = __ldg(a.cols + ct * kTNK + j);
-            if (core[q]) unite(parent, p, q);
+            const int cr = croot[j];
+            if (cr < 0 || cr == rp) continue;
+            unite(parent, rp, cr);
+            rp = find_root(parent, rp);
         }
     }
 }
@@ -210,28 +228,41 @@ __global__ void k_sng_extras_union(SngArgs a, const uint8_t* __restrict__ core, 
     }
 }
 
-// Border minima (parents of core points are roots here): a core row offers
-// its root to its non-core columns; a non-core row takes the smallest root of
-// its core columns.
-__global__ void k_sng_border(SngArgs a, const uint8_t* __restrict__ core, const int32_t* __restrict__ parent,
-                             int32_t* border) {
+// Border minima (parents of core points are roots here), over the same
+// word-synchronous walk: a non-core row takes the smallest root among its
+// passing core columns; the roots that core rows offer to a non-core column
+// are reduced in shared memory first, one global atomic per column and word.
+__global__ void __launch_bounds__(256) k_sng_border(SngArgs a, const uint8_t* __restrict__ core,
+                                                   const int32_t* __restrict__ parent, int32_t* border) {
+    __shared__ int croot[kTNK], cbest[kTNK];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.n) return;
-    const bool pc = core[p];
+    const bool valid = p < a.n;
+    const bool pc = valid && core[p];
     const int rp = pc ? __ldcg(parent + p) : INT_MAX;
     int best = INT_MAX;
     for (int ct = 0; ct < a.nct; ++ct) {
-        uint64_t w = __ldg(reinterpret_cast<const unsigned long long*>(a.mask) + (size_t)ct * a.n + p);
+        uint64_t w = valid ? __ldg(reinterpret_cast<const unsigned long long*>(a.mask) + (size_t)ct * a.n + p) : 0;
+        if (!__syncthreads_or(w != 0)) continue;
+        if (threadIdx.x < kTNK) {
+            const int c = ct * kTNK + threadIdx.x;
+            const int q = c < a.nU ? __ldg(a.cols + c) : -1;
+            croot[threadIdx.x] = (q >= 0 && core[q]) ? __ldcg(parent + q) : INT_MAX;
+            cbest[threadIdx.x] = INT_MAX;
+        }
+        __syncthreads();
         while (w) {
             const int j = __ffsll((long long)w) - 1;
             w &= w - 1;
-            const int q = __ldg(a.cols + ct * kTNK + j);
+            const int cr = croot[j];
             if (pc) {
-                if (!core[q] && __ldcg(border + q) > rp) atomicMin(border + q, rp);
-            } else if (core[q]) {
-                best = min(best, __ldcg(parent + q));
+                if (cr == INT_MAX) atomicMin(&cbest[j], rp);  // a non-core column (set bits are valid columns)
+            } else {
+                best = min(best, cr);
             }
         }
+        __syncthreads();
+        if (threadIdx.x < kTNK && cbest[threadIdx.x] != INT_MAX)
+            atomicMin(border + __ldg(a.cols + ct * kTNK + threadIdx.x), cbest[threadIdx.x]);
     }
     if (best != INT_MAX) atomicMin(border + p, best);
 }

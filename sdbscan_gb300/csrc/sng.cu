@@ -3,7 +3,9 @@
 //
 // Pipeline (engine stream): upload X -> transformData (k_colstats +
 // k_transform_rows) -> the host's sample (columns, multiplicities, extra
-// draws) uploaded -> k_sng_block (+ k_sng_extras) -> k_sng_degree ->
+// draws) uploaded -> k_sng_block, or with BF16 precision (Cosine sngDbscan)
+// k_sng_tc + k_sng_recheck with the FP32 block as gated fallback
+// (+ k_sng_extras) -> k_sng_degree ->
 //   sngDbscan: union-find over the pass bits, border minima, labels;
 //   sngOptics: second block pass into CSR lists, core distances, ordering.
 //
@@ -201,6 +203,27 @@ sdb_status sdb_engine::fit_sng(const float* X, bool xOnDevice, const float* epsL
     sa.nExtra = nExtra;
     sa.err = i32(errFlags) + 6;
     L_(launch_sng_col_of(sa, i32(sngColOf), st));
+    // BF16 screening of the block (Cosine sngDbscan): BF16 copies of every
+    // row and of the sampled rows, a queue for the pairs near eps
+    const bool screen = !optics && p.precision == SDB_PREC_BF16 && p.distance == SDB_COSINE && nU > 0;
+    const int ldb = (d + 63) / 64 * 64;
+    int64_t qcap = 0;
+    std::vector<uint64_t> heavy;  // per 64-column word: the columns drawn more than once
+    if (screen) {
+        qcap = std::min<int64_t>((int64_t)1 << 31, std::max<int64_t>((int64_t)1 << 22, (int64_t)n * nU / 16));
+        if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * ldb) || !ensure(sngUb, sizeof(uint16_t) * (size_t)nU * ldb) ||
+            !ensure(queue, sizeof(uint64_t) * (size_t)qcap) || !ensure(sngHeavy, sizeof(uint64_t) * nct))
+            return SDB_ERR_NOMEM;
+        L_(launch_to_bf16(f32(Xt), ld, n, Xb.ptr, ldb, st));
+        L_(launch_sng_gather_bf16(sa, sngUb.ptr, ldb, st));
+        if (sa.mult != nullptr) {
+            heavy.assign(nct, 0ull);
+            for (int c = 0; c < nU; ++c)
+                if (smp.mult[c] > 1) heavy[c >> 6] |= 1ull << (c & 63);
+            SDB_CK(cudaMemcpyAsync(sngHeavy.ptr, heavy.data(), sizeof(uint64_t) * nct, cudaMemcpyHostToDevice, st));
+            sa.heavy = static_cast<const uint64_t*>(sngHeavy.ptr);
+        }
+    }
     if (!ok) return fail(SDB_ERR_CUDA, "sample setup launch failed");
     SDB_CK(cudaEventRecord(ev[4], st));
 
@@ -208,7 +231,19 @@ sdb_status sdb_engine::fit_sng(const float* X, bool xOnDevice, const float* epsL
         sa.eps = epsList[ei];
         SDB_CK(cudaMemsetAsync(rowDeg.ptr, 0, sizeof(int32_t) * n, st));
         SDB_CK(cudaMemsetAsync(colCnt.ptr, 0, sizeof(int32_t) * std::max(nU, 1), st));
-        if (nct) L_(launch_sng_block(sa, st));
+        bool plain = nct > 0;
+        if (screen) {
+            // the FP32 block runs after the screening only if its flag was
+            // raised (queue overflow or a timed-out wait): one small readback
+            SDB_CK(cudaMemsetAsync(ctr + 4, 0, sizeof(unsigned long long), st));
+            L_(launch_sng_tc(sa, Xb.ptr, sngUb.ptr, ldb, static_cast<uint64_t*>(queue.ptr), qcap, ctr + 4,
+                             i32(errFlags) + 7, st));
+            if (!ok) return fail(SDB_ERR_CUDA, "tensor-core sample distance launch failed");
+            SDB_CK(cudaMemcpyAsync(hostErr + 7, i32(errFlags) + 7, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+            SDB_CK(cudaStreamSynchronize(st));
+            plain = hostErr[7] != 0;
+        }
+        if (plain) L_(launch_sng_block(sa, st));
         L_(launch_sng_extras(sa, st));
         if (!ok) return fail(SDB_ERR_CUDA, "sample distance launch failed");
         if (ei == 0) SDB_CK(cudaEventRecord(ev[5], st));
@@ -291,9 +326,9 @@ sdb_status sdb_engine::fit_sng(const float* X, bool xOnDevice, const float* epsL
     if (optics) haveOptics = true;
     else haveLabels = true;
     if (p.verbose) {
-        std::printf("sdbscan_gb300 %s fit: n=%d d=%d dist=%s samplingProb=%g sampled=%d extra=%d eps=%g minPts=%d\n",
+        std::printf("sdbscan_gb300 %s fit: n=%d d=%d dist=%s samplingProb=%g sampled=%d extra=%d eps=%g minPts=%d%s\n",
                     optics ? "sngOPTICS" : "sngDBSCAN", n, d, dist_label(p.distance), p.samplingProb, nU, nExtra,
-                    epsList[0], minPts);
+                    epsList[0], minPts, screen ? " (BF16 screening)" : "");
         const char* names[9] = {"upload", "transform", "-", "sample", "distances", "core", "cluster/optics",
                                 "readback", "total"};
         for (int i = 0; i < 9; ++i) std::printf("  %-14s %9.3f ms\n", names[i], stageMs[i]);

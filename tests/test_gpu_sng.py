@@ -87,6 +87,32 @@ def test_fit_sngdbscan_matches_oracle(port, case):
     eng.close()
 
 
+@pytest.mark.parametrize("prob,eps,minPts", [(0.05, 0.2, 20), (1.0, 0.15, 50), (0.3, 0.25, 100)])
+def test_sngdbscan_bf16_screening_is_exact(port, prob, eps, minPts):
+    """BF16 precision (Cosine): the block on the tensor cores, pairs within
+    the margin re-decided in FP32 -- degrees, core flags and labels equal the
+    oracle's, with pairs actually re-decided and no fallback.  MNIST-like data
+    (thousands of pairs within 0.009 of eps; well-separated vMF clusters have
+    none)."""
+    from sdbscan_gb300 import capi, datasets
+    X = datasets.cfg2_mnist_like(5000, 196, seed=13)[0]
+    eng = _sng_engine(X, "Cosine", prob, 21)
+    eng.set_precision(capi.PREC_BF16)
+    eng.fit_sngdbscan(X, eps, minPts)
+    labels, ncl = eng.labels()
+    core, deg = eng.core()
+    c = eng.counters()
+    l2, n2, c2, d2, _ = port.fit_sngdbscan(X, eps, minPts, samplingProb=prob, seed=21, threads=8)
+    np.testing.assert_array_equal(deg, d2)
+    np.testing.assert_array_equal(core, c2)
+    np.testing.assert_array_equal(labels, l2)
+    assert ncl == n2
+    assert c["rechecked"] > 0 and c["fallbacks"] == 0
+    labels_sw, _ = eng.fit_sngdbscan_sweep(X, [eps, eps + 0.05], minPts)
+    np.testing.assert_array_equal(labels_sw[0], l2)
+    eng.close()
+
+
 def test_sngdbscan_sweep_equals_separate_fits(port):
     """test_sngDbscan (src/sDbscan.cpp:1192-1240): one transform and sample,
     each eps's labels equal a separate fit (and the oracle's)."""
