@@ -348,7 +348,7 @@ def _cpu_batched(n_sets=6):
                       f"(oracle/ restatement, OpenMP, {threads} threads; sweep {sweep_s:.1f} s, fits {fits_s:.1f} s)"}
 
 
-def _cpu_sng(cfg, n_sample=10000):
+def _cpu_sng(cfg, n_sample=20000):
     """The oracle's sngDbscan (point-by-point restatement of
     sng_findCorePoints) on n_sample points of the workload's law with the
     same number of draws per point as the full workload (ceil(0.01 n) =
@@ -360,6 +360,7 @@ def _cpu_sng(cfg, n_sample=10000):
     Xh = _host_data(cfg, n_sample)
     draws = -(-cfg["n"] * SNG_PROB // 1)
     prob = float(draws) / n_sample
+    assert prob < 1.0, "the sample must stay in the sampled branch (samplingProb < 1)"
     t0 = time.perf_counter()
     port.fit_sngdbscan(Xh, cfg["eps"], cfg["minPts"], dist=cfg["distance"], samplingProb=prob, seed=SNG_SEED,
                        threads=threads)
