@@ -89,6 +89,14 @@ sdb_status sdb_set_params(sdb_engine* e, const sdb_params* p);
  * counterpart (the reference computes in FP32 only). */
 sdb_status sdb_set_precision(sdb_engine* e, int32_t precision);
 
+/* Tile shape of the plain FP32 distance kernel (a tuning control; no
+ * reference counterpart): 0 = by topM (default: shape 3 for topM in 41..50,
+ * else 1), 1 = 128 x 64 tiles on 256 threads, 2 = 128 x 50 on 160 threads
+ * (32 dimensions per stage, 2 stages), 3 = 128 x 50 with 16 dimensions per
+ * stage in 4 stages.  The 50-column shapes apply when topM <= 50 (else shape
+ * 1).  Any shape gives the same bits. */
+sdb_status sdb_set_tile_variant(sdb_engine* e, int32_t variant);
+
 /* fit_sDbscan(const Ref<const MatrixXf>& X, float eps, int minPts)
  * (src/sDbscan.h:183, src/sDbscan.cpp:830-890).  X_host: d x n column-major
  * host memory (pinned memory makes the upload faster).  Results stay in the
@@ -221,8 +229,8 @@ const char* sdb_last_error(sdb_engine* e);
  *   X_device[i]: d_i x n_i column-major data of set i, device memory, kept
  *                valid for the batch's lifetime
  * The batch plans every set once (sizing run; with FP32 precision and
- * topM <= 50 it also times both distance tile shapes per set and keeps the
- * faster, sdb_batch_tile_variant), then times graphs with 4, 8, 16, 32 and 64
+ * topM <= 50 it also times the three distance tile shapes per set and keeps
+ * the fastest, sdb_batch_tile_variant), then times graphs with 4, 8, 16, 32 and 64
  * sets in flight and keeps the fastest (sdb_batch_lanes).
  * sdb_batch_run replays it; sdb_batch_labels reads set i's labelling for eps
  * index j. */
@@ -234,8 +242,8 @@ sdb_status sdb_batch_run(sdb_batch* b, float* elapsed_ms);
 sdb_status sdb_batch_labels(sdb_batch* b, int32_t set, int32_t eps_index, int32_t* labels, int32_t* n_clusters);
 int32_t sdb_batch_lanes(sdb_batch* b);
 /* The plain distance kernel's tile shape the autotuner kept for set i (FP32
- * precision, topM <= 50): 1 = 128 x 64 tiles on 256 threads, 2 = 128 x 50
- * tiles on 160 threads; 0 = the default rule (by topM); -1 for a bad index. */
+ * precision, topM <= 50; the shapes of sdb_set_tile_variant, 1..3); 0 = the
+ * default rule (by topM); -1 for a bad index. */
 int32_t sdb_batch_tile_variant(sdb_batch* b, int32_t set);
 void sdb_batch_destroy(sdb_batch* b);
 const char* sdb_batch_last_error(sdb_batch* b);

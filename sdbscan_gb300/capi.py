@@ -26,7 +26,8 @@ EXPORTS = ["sdb_params_default", "sdb_engine_create", "sdb_engine_destroy", "sdb
            "sdb_fit_sdbscan_sweep", "sdb_batch_create", "sdb_batch_run", "sdb_batch_labels", "sdb_batch_lanes",
            "sdb_batch_destroy", "sdb_batch_last_error", "sdb_load_txt",
            "sdb_batch_tile_variant", "sdb_set_sng_params", "sdb_fit_sngdbscan", "sdb_fit_sngdbscan_device",
-           "sdb_fit_sngdbscan_sweep", "sdb_fit_sngoptics", "sdb_fit_sngoptics_device", "sdb_set_precision"]
+           "sdb_fit_sngdbscan_sweep", "sdb_fit_sngoptics", "sdb_fit_sngoptics_device", "sdb_set_precision",
+           "sdb_set_tile_variant"]
 
 
 class SdbParams(ctypes.Structure):
@@ -80,6 +81,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.sdb_fit_sngdbscan_sweep.argtypes = [vp, vp, vp, i32, i32, vp, vp]
     L.sdb_set_sng_params.argtypes = [vp, i32, f32, i32, i32, i32, i32]
     L.sdb_set_precision.argtypes = [vp, i32]
+    L.sdb_set_tile_variant.argtypes = [vp, i32]
     L.sdb_batch_create.argtypes = [i32, vp, vp, vp, ctypes.POINTER(SdbParams), vp, i32, i32, i32,
                                    ctypes.POINTER(vp)]
     L.sdb_batch_run.argtypes = [vp, ctypes.POINTER(f32)]
@@ -183,6 +185,10 @@ class Engine:
         """PREC_FP32 or PREC_BF16 alone (no index parameter checks)."""
         self._check(self.L.sdb_set_precision(self.h, precision))
         self.params.precision = precision
+
+    def set_tile_variant(self, variant: int):
+        """Tile shape of the plain FP32 distance kernel (0 = by topM; see the header)."""
+        self._check(self.L.sdb_set_tile_variant(self.h, variant))
 
     def fit_sngdbscan(self, X: np.ndarray, eps: float, minPts: int):
         X = self._host(X)

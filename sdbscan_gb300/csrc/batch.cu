@@ -146,11 +146,11 @@ sdb_status sdb_batch_create(int32_t n_sets, const int32_t* n_points, const int32
             return batch_fail(b, s, "set " + std::to_string(i) + ": " + e->err);
         }
         // tile autotuner: when the set's distances run on the plain kernel and
-        // both tile shapes apply (m <= 50), time the distance stage with each
+        // the tile shapes all apply (m <= 50), time the distance stage with each
         if (q.precision == SDB_PREC_FP32 && q.topM <= 50) {
             float best = 1e30f;
             int bestV = 0;
-            for (int v : {1, 2}) {
+            for (int v : {1, 2, 3}) {
                 e->distVariant = v;
                 s = e->fit(X_device[i], true, eps[0], minPts, false, &sw);
                 if (s != SDB_OK) {

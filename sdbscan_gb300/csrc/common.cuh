@@ -209,7 +209,7 @@ struct DistArgs {
     float epsLo;          // eps sweeps: k_masks_from_dists keeps epsLo < d <= eps
     const uint8_t* pairRound;  // eps sweeps (optional): per pair, the first round whose eps >= d
     int round;
-    int variant;               // plain distance tiles: 0 by m, 1: 128 x 64 (256 threads), 2: 128 x 50 (160 threads)
+    int variant;               // plain distance tiles: 0 by m, 1: 128 x 64 (256 threads), 2-3: 128 x 50 (160 threads; k_dist.cu)
     uint64_t* masks;      // n x 2k x W
     int32_t* inRaw;       // n
     float* dists;         // n x 2k x m (optional)

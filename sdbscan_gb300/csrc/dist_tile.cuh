@@ -99,36 +99,38 @@ __device__ __forceinline__ float warp_staged_cosine(const float* const* rows, fl
 }
 
 // acc[i][j] = accumulated distance terms of (row ty + 16 i, column tx + TX j)
-// with ty = tid / TX, tx = tid % TX.  As / Bs: STAGES x TM x LDS and
-// STAGES x (TX * CN) x LDS floats of shared memory.  Ends with every copy
-// landed; the caller synchronises before reusing the buffers.
-template <int DIST, int TX, int CN>
+// with ty = tid / TX, tx = tid % TX.  KT dimensions per stage, NST stages:
+// As / Bs are NST x TM x (KT + 4) and NST x (TX * CN) x (KT + 4) floats of
+// shared memory (the +4 keeps the float4 fragment reads of consecutive rows
+// in different bank groups).  Ends with every copy landed; the caller
+// synchronises before reusing the buffers.
+template <int DIST, int TX, int CN, int KT = TK, int NST = STAGES>
 __device__ __forceinline__ void accumulate(const float* __restrict__ Xt, int ld, int d, const int* rowPoint,
                                            const int* colPoint, float* As, float* Bs, float (&acc)[8][CN]) {
-    constexpr int NT = 16 * TX, TNK = TX * CN;
+    constexpr int NT = 16 * TX, TNK = TX * CN, LDK = KT + 4, CPR = KT / 4;  // CPR: 16-byte chunks per row
     const int tid = threadIdx.x;
-    const int nk = (d + TK - 1) / TK;
+    const int nk = (d + KT - 1) / KT;
     auto load_stage = [&](int stage, int kc) {
-        float* as = As + stage * TM * LDS;
-        float* bs = Bs + stage * TNK * LDS;
-        const int k0 = kc * TK;
+        float* as = As + stage * TM * LDK;
+        float* bs = Bs + stage * TNK * LDK;
+        const int k0 = kc * KT;
 #pragma unroll
-        for (int idx = tid; idx < TM * TK / 4; idx += NT) {
-            const int row = idx >> 3, c4 = idx & 7;
+        for (int idx = tid; idx < TM * CPR; idx += NT) {
+            const int row = idx / CPR, c4 = idx % CPR;
             const int p = rowPoint[row];
             const int col = k0 + c4 * 4;
             const bool ok = p >= 0 && col < ld;
             const float* src = ok ? Xt + (size_t)p * ld + col : Xt;
-            cp_async16(as + row * LDS + c4 * 4, src, ok);
+            cp_async16(as + row * LDK + c4 * 4, src, ok);
         }
 #pragma unroll
-        for (int idx = tid; idx < TNK * TK / 4; idx += NT) {
-            const int row = idx >> 3, c4 = idx & 7;
+        for (int idx = tid; idx < TNK * CPR; idx += NT) {
+            const int row = idx / CPR, c4 = idx % CPR;
             const int p = colPoint[row];
             const int col = k0 + c4 * 4;
             const bool ok = p >= 0 && col < ld;
             const float* src = ok ? Xt + (size_t)p * ld + col : Xt;
-            cp_async16(bs + row * LDS + c4 * 4, src, ok);
+            cp_async16(bs + row * LDK + c4 * 4, src, ok);
         }
     };
 
@@ -139,25 +141,25 @@ __device__ __forceinline__ void accumulate(const float* __restrict__ Xt, int ld,
 
     const int ty = tid / TX, tx = tid % TX;
 #pragma unroll
-    for (int s = 0; s < STAGES - 1; ++s) {
+    for (int s = 0; s < NST - 1; ++s) {
         if (s < nk) load_stage(s, s);
         cp_async_commit();
     }
     for (int kc = 0; kc < nk; ++kc) {
-        cp_async_wait<STAGES - 2>();
+        cp_async_wait<NST - 2>();
         __syncthreads();
-        const int nxt = kc + STAGES - 1;
-        if (nxt < nk) load_stage(nxt % STAGES, nxt);
+        const int nxt = kc + NST - 1;
+        if (nxt < nk) load_stage(nxt % NST, nxt);
         cp_async_commit();
-        const float* as = As + (kc % STAGES) * TM * LDS;
-        const float* bs = Bs + (kc % STAGES) * TNK * LDS;
+        const float* as = As + (kc % NST) * TM * LDK;
+        const float* bs = Bs + (kc % NST) * TNK * LDK;
 #pragma unroll
-        for (int kk = 0; kk < TK; kk += 4) {
+        for (int kk = 0; kk < KT; kk += 4) {
             float4 av[8], bv[CN];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) av[i] = *reinterpret_cast<const float4*>(as + (ty + 16 * i) * LDS + kk);
+            for (int i = 0; i < 8; ++i) av[i] = *reinterpret_cast<const float4*>(as + (ty + 16 * i) * LDK + kk);
 #pragma unroll
-            for (int j = 0; j < CN; ++j) bv[j] = *reinterpret_cast<const float4*>(bs + (tx + TX * j) * LDS + kk);
+            for (int j = 0; j < CN; ++j) bv[j] = *reinterpret_cast<const float4*>(bs + (tx + TX * j) * LDK + kk);
 #pragma unroll
             for (int i = 0; i < 8; ++i)
 #pragma unroll

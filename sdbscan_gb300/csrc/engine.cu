@@ -732,6 +732,13 @@ sdb_status sdb_set_params(sdb_engine* e, const sdb_params* p) {
     return s;
 }
 
+sdb_status sdb_set_tile_variant(sdb_engine* e, int32_t variant) {
+    if (!e) return SDB_ERR_ARG;
+    if (variant < 0 || variant > 3) return e->fail(SDB_ERR_ARG, "tile variant must be 0..3");
+    e->distVariant = variant;
+    return SDB_OK;
+}
+
 sdb_status sdb_set_precision(sdb_engine* e, int32_t precision) {
     if (!e) return SDB_ERR_ARG;
     if (precision != SDB_PREC_FP32 && precision != SDB_PREC_BF16) return e->fail(SDB_ERR_ARG, "unknown precision");

@@ -189,31 +189,46 @@ __global__ void k_sng_degree(SngArgs a, int exact, int optics, int minPts, int32
     core[p] = deg >= minPts - 1 ? 1 : 0;
 }
 
-// Thread per row, 256 consecutive rows per CTA, walking the mask words in
-// step: for each word with a passing bit in the CTA, the roots of its 64
-// columns are found once and cached in shared memory, and a core row unites
-// only where its own root differs from a passing core column's cached root.
-// A cached value is an ancestor of its column (parents only move up), so
-// equality proves the same set; a stale value only costs a redundant unite.
+// The cluster kernels run on a 2-D grid: 256 consecutive rows (a thread per
+// row) x a group of kGroup consecutive mask words.  A CTA loads its rows'
+// words at once, finds the roots of the group's 64 kGroup columns in parallel
+// and caches them in shared memory; the many independent CTAs hide the
+// latency of the finds.  A core row unites only where its own root differs
+// from a passing core column's cached root.  A cached value is an ancestor
+// of its column (parents only move up), so equality proves the same set; a
+// stale value only costs a redundant unite.
+constexpr int kGroup = 8;
+
 __global__ void __launch_bounds__(256) k_sng_union(SngArgs a, const uint8_t* __restrict__ core, int32_t* parent) {
-    __shared__ int croot[kTNK];
+    __shared__ int croot[kGroup][kTNK];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = p < a.n && core[p];
-    if (!__syncthreads_or(active)) return;
-    int rp = active ? find_root(parent, p) : -1;
-    for (int ct = 0; ct < a.nct; ++ct) {
-        uint64_t w = active ? __ldg(reinterpret_cast<const unsigned long long*>(a.mask) + (size_t)ct * a.n + p) : 0;
-        if (!__syncthreads_or(w != 0)) continue;  // also orders the previous word's reads of croot
-        if (threadIdx.x < kTNK) {
-            const int c = ct * kTNK + threadIdx.x;
-            const int q = c < a.nU ? __ldg(a.cols + c) : -1;
-            croot[threadIdx.x] = (q >= 0 && core[q]) ? find_root(parent, q) : -1;
-        }
-        __syncthreads();
-        while (w) {
-            const int j = __ffsll((long long)w) - 1;
-            w &= w - 1;
-            const int cr = croot[j];
+    const int ct0 = blockIdx.y * kGroup, nw = min(kGroup, a.nct - ct0);
+    uint64_t w[kGroup];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < kGroup; ++k) {
+        w[k] = (active && k < nw)
+                   ? __ldg(reinterpret_cast<const unsigned long long*>(a.mask) + (size_t)(ct0 + k) * a.n + p)
+                   : 0ull;
+        any |= w[k] != 0;
+    }
+    if (!__syncthreads_or(any)) return;
+    for (int e = threadIdx.x; e < nw * kTNK; e += blockDim.x) {
+        const int c = ct0 * kTNK + e;
+        const int q = c < a.nU ? __ldg(a.cols + c) : -1;
+        croot[e / kTNK][e % kTNK] = (q >= 0 && core[q]) ? find_root(parent, q) : -1;
+    }
+    __syncthreads();
+    if (!any) return;
+    int rp = find_root(parent, p);
+#pragma unroll
+    for (int k = 0; k < kGroup; ++k) {
+        uint64_t bits = w[k];
+        while (bits) {
+            const int j = __ffsll((long long)bits) - 1;
+            bits &= bits - 1;
+            const int cr = croot[k][j];
             if (cr < 0 || cr == rp) continue;
             unite(parent, rp, cr);
             rp = find_root(parent, rp);
@@ -228,42 +243,54 @@ __global__ void k_sng_extras_union(SngArgs a, const uint8_t* __restrict__ core, 
     }
 }
 
-// Border minima (parents of core points are roots here), over the same
-// word-synchronous walk: a non-core row takes the smallest root among its
-// passing core columns; the roots that core rows offer to a non-core column
-// are reduced in shared memory first, one global atomic per column and word.
+// Border minima (parents of core points are roots here), on the same 2-D
+// grid: a non-core row takes the smallest root among its passing core
+// columns; the roots that core rows offer to a non-core column are reduced in
+// shared memory first, one global atomic per column and CTA.
 __global__ void __launch_bounds__(256) k_sng_border(SngArgs a, const uint8_t* __restrict__ core,
                                                    const int32_t* __restrict__ parent, int32_t* border) {
-    __shared__ int croot[kTNK], cbest[kTNK];
+    __shared__ int croot[kGroup][kTNK], cbest[kGroup][kTNK];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < a.n;
     const bool pc = valid && core[p];
     const int rp = pc ? __ldcg(parent + p) : INT_MAX;
+    const int ct0 = blockIdx.y * kGroup, nw = min(kGroup, a.nct - ct0);
+    uint64_t w[kGroup];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < kGroup; ++k) {
+        w[k] = (valid && k < nw)
+                   ? __ldg(reinterpret_cast<const unsigned long long*>(a.mask) + (size_t)(ct0 + k) * a.n + p)
+                   : 0ull;
+        any |= w[k] != 0;
+    }
+    if (!__syncthreads_or(any)) return;
+    for (int e = threadIdx.x; e < nw * kTNK; e += blockDim.x) {
+        const int c = ct0 * kTNK + e;
+        const int q = c < a.nU ? __ldg(a.cols + c) : -1;
+        croot[e / kTNK][e % kTNK] = (q >= 0 && core[q]) ? __ldcg(parent + q) : INT_MAX;
+        cbest[e / kTNK][e % kTNK] = INT_MAX;
+    }
+    __syncthreads();
     int best = INT_MAX;
-    for (int ct = 0; ct < a.nct; ++ct) {
-        uint64_t w = valid ? __ldg(reinterpret_cast<const unsigned long long*>(a.mask) + (size_t)ct * a.n + p) : 0;
-        if (!__syncthreads_or(w != 0)) continue;
-        if (threadIdx.x < kTNK) {
-            const int c = ct * kTNK + threadIdx.x;
-            const int q = c < a.nU ? __ldg(a.cols + c) : -1;
-            croot[threadIdx.x] = (q >= 0 && core[q]) ? __ldcg(parent + q) : INT_MAX;
-            cbest[threadIdx.x] = INT_MAX;
-        }
-        __syncthreads();
-        while (w) {
-            const int j = __ffsll((long long)w) - 1;
-            w &= w - 1;
-            const int cr = croot[j];
+#pragma unroll
+    for (int k = 0; k < kGroup; ++k) {
+        uint64_t bits = w[k];
+        while (bits) {
+            const int j = __ffsll((long long)bits) - 1;
+            bits &= bits - 1;
+            const int cr = croot[k][j];
             if (pc) {
-                if (cr == INT_MAX) atomicMin(&cbest[j], rp);  // a non-core column (set bits are valid columns)
+                if (cr == INT_MAX) atomicMin(&cbest[k][j], rp);  // a non-core column (set bits are valid columns)
             } else {
                 best = min(best, cr);
             }
         }
-        __syncthreads();
-        if (threadIdx.x < kTNK && cbest[threadIdx.x] != INT_MAX)
-            atomicMin(border + __ldg(a.cols + ct * kTNK + threadIdx.x), cbest[threadIdx.x]);
     }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nw * kTNK; e += blockDim.x)
+        if (cbest[e / kTNK][e % kTNK] != INT_MAX)
+            atomicMin(border + __ldg(a.cols + ct0 * kTNK + e), cbest[e / kTNK][e % kTNK]);
     if (best != INT_MAX) atomicMin(border + p, best);
 }
 
@@ -343,7 +370,7 @@ int launch_sng_degree(const SngArgs& a, int exact, int optics, int minPts, int32
 int launch_sng_union(const SngArgs& a, const uint8_t* core, int32_t* parent, cudaStream_t st) {
     int launches = 0;
     if (a.nct > 0) {
-        k_sng_union<<<(a.n + 255) / 256, 256, 0, st>>>(a, core, parent);
+        k_sng_union<<<dim3((a.n + 255) / 256, (a.nct + kGroup - 1) / kGroup), 256, 0, st>>>(a, core, parent);
         ++launches;
     }
     if (a.nExtra > 0) {
@@ -357,7 +384,8 @@ int launch_sng_border(const SngArgs& a, const uint8_t* core, const int32_t* pare
                       cudaStream_t st) {
     int launches = 0;
     if (a.nct > 0) {
-        k_sng_border<<<(a.n + 255) / 256, 256, 0, st>>>(a, core, parent, border);
+        k_sng_border<<<dim3((a.n + 255) / 256, (a.nct + kGroup - 1) / kGroup), 256, 0, st>>>(a, core, parent,
+                                                                                          border);
         ++launches;
     }
     if (a.nExtra > 0) {

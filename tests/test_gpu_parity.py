@@ -353,7 +353,7 @@ def test_batch_graph_equals_sweeps(precision):
             assert nb == ncl[j]
     assert b.lanes() >= 1
     # plain distances: the autotuner picked a tile shape per set; BF16 sets screen on the tensor cores
-    assert all(v in ((1, 2) if precision == 0 else (0,)) for v in b.tile_variants())
+    assert all(v in ((1, 2, 3) if precision == 0 else (0,)) for v in b.tile_variants())
     b.close()
     torch.cuda.synchronize()
 
