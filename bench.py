@@ -53,8 +53,8 @@ FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # nominal FP32 CUDA-core peak
 # DRAM bytes (read + write) of one k_dist<Cosine> launch on the 1M x 784
 # workload, from a one-pass ncu capture of
 # `python -m sdbscan_gb300.profile_fit 1000000 0` (profiles/k_dist_fp32_cfg2.md):
-# 64.44 GB read + 0.646 GB written.
-K_DIST_TRAFFIC_1M = 64.44e9 + 0.646e9
+# 23.29 GB read + 0.370 GB written (tiles run in point-chunk order).
+K_DIST_TRAFFIC_1M = 23.29e9 + 0.370e9
 # sngDBSCAN, the reference's sampling baseline that its benchmark loop runs
 # next to fit_sDbscan (src/main.cpp:57-73): samplingProb 0.01 (the default,
 # 10,000 draws per point at 1M points), seed 42, the workload's eps / minPts.

@@ -186,9 +186,22 @@ struct IndexArgs {
     int64_t* hubOff;      // n + 1
     int32_t* hubLists;    // 2*nproj*m: list ids per hub point
     int64_t* scanTmp;
+    // members in point-chunk order and tiles in chunk order (L2 locality of
+    // the gathered rows: the tiles in flight cover a narrow range of points)
+    int chunkPts, nChunks;  // points per chunk; chunks
+    int32_t* chunkOff;      // 2*nproj x nChunks: members of the list from each chunk, scanned per list
+    int32_t* tileKey;       // total tiles: chunk of the tile's first member
+    int64_t* keyOff;        // nChunks + 1 (counts, then scanned, then used as cursors)
+    int32_t* tilePerm;      // total tiles: tiles in chunk order
+    int64_t maxTiles;       // grid bound of the tile kernels
 };
+// Members of every list ordered by point chunk (CTA per chunk).
 int launch_index_count(const IndexArgs& a, cudaStream_t st);
 int launch_index_scatter(const IndexArgs& a, cudaStream_t st);
+// tilePerm: the tiles sorted by the chunk of their first member.
+int launch_tile_order(const IndexArgs& a, cudaStream_t st);
+// Tile id of the b-th launched tile (identity without a permutation).
+__device__ __forceinline__ int64_t tile_at(const int32_t* perm, int64_t b) { return perm != nullptr ? perm[b] : b; }
 int launch_tiles(const IndexArgs& a, int64_t total_tiles, cudaStream_t st);
 int launch_hubs_count(const IndexArgs& a, cudaStream_t st);
 int launch_hubs_scatter(const IndexArgs& a, cudaStream_t st);
@@ -202,6 +215,7 @@ struct DistArgs {
     const int64_t* tileOff;
     int64_t nTiles;       // launch grid (an upper bound)
     const int64_t* tileTotal;  // device: actual number of tiles
+    const int32_t* tilePerm;   // optional: launch order of the tiles (tile_at)
     const int32_t* topM;
     int nproj, m, k, W;   // W = 64-bit mask words per (point, slot)
     int nct;              // candidate tiles per list
@@ -277,6 +291,7 @@ struct ClusterArgs {
     const int32_t* tileList;
     const int64_t* tileOff;
     const int64_t* tileTotal;  // device: actual number of tiles
+    const int32_t* tilePerm;   // optional: launch order of the tiles (tile_at)
     int64_t nTiles;            // launch grid (an upper bound)
     int TM, nct, nproj;
     // eps sweeps: the union-find carries over from the previous (smaller) eps,

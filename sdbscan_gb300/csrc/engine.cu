@@ -98,7 +98,7 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
             &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig, &Rb, &newMasks, &coreEps, &sampleFlag,
             &noiseFlag, &noiseCores, &noisePts, &PcT, &numCore, &pairRound, &sngCols, &sngMult, &sngColOf, &sngExtras,
-            &sngExtraPass, &sngMask, &rowDeg, &colCnt, &sngUb, &sngHeavy};
+            &sngExtraPass, &sngMask, &rowDeg, &colCnt, &sngUb, &sngHeavy, &chunkOff, &tileKey, &keyOff, &tilePerm};
 }
 
 // ---------------------------------------------------------------------------
@@ -221,6 +221,9 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
           ensure(errFlags, sizeof(int32_t) * 8) && ensure(counters, sizeof(unsigned long long) * 8) &&
           ensure(signs, sizeof(uint32_t) * hostSigns.size()) &&
           ensure(compCosh, sizeof(double) * std::max<size_t>(1, hostCosh.size()));
+    const int chunkPts = 4096, nChunks = (n + chunkPts - 1) / chunkPts;
+    ok &= ensure(chunkOff, sizeof(int32_t) * (size_t)L * nChunks) && ensure(tileKey, sizeof(int32_t) * maxTiles) &&
+          ensure(keyOff, sizeof(int64_t) * ((size_t)nChunks + 1)) && ensure(tilePerm, sizeof(int32_t) * maxTiles);
     const int maskWords = (L + 31) / 32;
     const size_t maxHubs = std::min<size_t>((size_t)n, (size_t)L * m);
     ok &= ensure(hubIdx, sizeof(int32_t) * n) && ensure(kMask, sizeof(uint32_t) * maxHubs * maskWords) &&
@@ -381,6 +384,13 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     ia.hubOff = i64(hubOff);
     ia.hubLists = i32(hubLists);
     ia.scanTmp = i64(scanTmp);
+    ia.chunkPts = chunkPts;
+    ia.nChunks = nChunks;
+    ia.chunkOff = i32(chunkOff);
+    ia.tileKey = i32(tileKey);
+    ia.keyOff = i64(keyOff);
+    ia.tilePerm = i32(tilePerm);
+    ia.maxTiles = maxTiles;
     SDB_CK(cudaMemsetAsync(listCount.ptr, 0, sizeof(int64_t) * (L + 1), st));
     SDB_CK(cudaMemsetAsync(listFill.ptr, 0, sizeof(int64_t) * L, st));
     SDB_CK(cudaMemsetAsync(hubCount.ptr, 0, sizeof(int32_t) * n, st));
@@ -390,6 +400,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     L_(launch_index_scatter(ia, st));
     L_(launch_tile_offsets(ia, st));
     L_(launch_tiles(ia, 0, st));
+    L_(launch_tile_order(ia, st));
     L_(launch_hubs_count(ia, st));
     L_(launch_i32_to_i64(i32(hubCount), i64(hubOff), n, st));
     L_(launch_scan_i64(i64(hubOff), i64(hubOff), (size_t)n + 1, i64(scanTmp), st));
@@ -412,6 +423,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     da.tileOff = i64(tileOff);
     da.nTiles = maxTiles;
     da.tileTotal = i64(tileOff) + L;
+    da.tilePerm = i32(tilePerm);
     da.topM = i32(topM);
     da.nproj = D;
     da.m = m;
@@ -538,6 +550,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         ka.tileList = i32(tileList);
         ka.tileOff = i64(tileOff);
         ka.tileTotal = i64(tileOff) + L;
+        ka.tilePerm = i32(tilePerm);
         ka.nTiles = maxTiles;
         ka.TM = TMr;
         ka.nct = nct;

@@ -54,7 +54,7 @@ struct sdb_engine {
         rootFlag, labels, nClusters, scanTmp, errFlags, counters, E, Rt, signs, compCosh, dists, coreDist, nbOff,
         nbIdx, nbDist, nbFill, hubIdx, kMask, firstMasks, Xb, queue, sweepLabels, sweepNcl, sig, Rb, newMasks,
         coreEps, sampleFlag, noiseFlag, noiseCores, noisePts, PcT, numCore, pairRound, sngCols, sngMult, sngColOf,
-        sngExtras, sngExtraPass, sngMask, rowDeg, colCnt, sngUb, sngHeavy;
+        sngExtras, sngExtraPass, sngMask, rowDeg, colCnt, sngUb, sngHeavy, chunkOff, tileKey, keyOff, tilePerm;
 
     // results
     bool haveLabels = false, haveOptics = false, haveFit = false, lastOptics = false;

@@ -33,8 +33,9 @@ struct Tile {
     const int32_t* cand;
 };
 
-__device__ __forceinline__ bool tile_of(const ClusterArgs& a, int64_t t, Tile& tl) {
-    if (t >= *a.tileTotal) return false;
+__device__ __forceinline__ bool tile_of(const ClusterArgs& a, int64_t b, Tile& tl) {
+    if (b >= *a.tileTotal) return false;
+    const int64_t t = tile_at(a.tilePerm, b);
     const int l = a.tileList[t];
     const int64_t ti = t - a.tileOff[l];
     const int mt = (int)(ti / a.nct);

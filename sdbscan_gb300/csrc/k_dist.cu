@@ -54,8 +54,8 @@ __global__ void __launch_bounds__(16 * TX, (dist_min_blocks<TX, CN, KT, NST>()))
     __shared__ int passTotal;
 
     const int tid = threadIdx.x;
-    const int64_t t = blockIdx.x;
-    if (t >= *a.tileTotal) return;
+    if ((int64_t)blockIdx.x >= *a.tileTotal) return;
+    const int64_t t = tile_at(a.tilePerm, blockIdx.x);
     const int l = a.tileList[t];
     const int64_t ti = t - a.tileOff[l];
     const int mt = (int)(ti / a.nct), ct = (int)(ti % a.nct);
@@ -169,8 +169,8 @@ template <int DIST> int launch_dist_t(const DistArgs& a, cudaStream_t st) {
 __global__ void k_masks_from_dists(DistArgs a) {
     __shared__ int colCount[TN];
     __shared__ int passTotal;
-    const int64_t t = blockIdx.x;
-    if (t >= *a.tileTotal) return;
+    if ((int64_t)blockIdx.x >= *a.tileTotal) return;
+    const int64_t t = tile_at(a.tilePerm, blockIdx.x);
     const int l = a.tileList[t];
     const int64_t ti = t - a.tileOff[l];
     const int mt = (int)(ti / a.nct), ct = (int)(ti % a.nct);

@@ -104,7 +104,8 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
     // The next tile's ids and first STAGES - 1 stages are loaded before the
     // current tile's epilogue (its MMAs are done by then), so the gathers
     // overlap the epilogue.
-    auto load_meta = [&](int64_t t, int b) {
+    auto load_meta = [&](int64_t tb, int b) {  // tb: launch index, mapped to a tile id
+        const int64_t t = tile_at(a.tilePerm, tb);
         const int l = a.tileList[t];
         const int64_t ti = t - a.tileOff[l];
         const int mt = (int)(ti / a.nct), ct = (int)(ti % a.nct);
@@ -160,7 +161,8 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
 
     int tb = 0;  // parity of the current tile's buffers
     for (int64_t t = blockIdx.x; t < total; t += gridDim.x, tb ^= 1) {
-        const int ct = (int)((t - a.tileOff[a.tileList[t]]) % a.nct);
+        const int64_t tid_ = tile_at(a.tilePerm, t);
+        const int ct = (int)((tid_ - a.tileOff[a.tileList[tid_]]) % a.nct);
         const int* colPoint = colPoints[tb];
         for (int kc = 0; kc < nk; ++kc) {
             const int stage = kc % STAGES;
@@ -211,7 +213,7 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
         for (int c16 = 0; c16 < TN / 16; ++c16) {
             float v[16];
             tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c16 * 16), v);
-            if (dbgAcc != nullptr && t == 0) {  // accumulator of the first tile, for layout checks
+            if (dbgAcc != nullptr && tid_ == 0) {  // accumulator of tile 0, for layout checks
 #pragma unroll
                 for (int j = 0; j < 16; ++j) dbgAcc[row * TN + c16 * 16 + j] = v[j];
             }

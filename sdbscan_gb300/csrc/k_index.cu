@@ -22,53 +22,81 @@ __device__ __forceinline__ int list_of(const int32_t* topK, int p, int slot, int
     return topK[(size_t)p * 2 * k + slot] + (slot >= k ? nproj : 0);
 }
 
-// Per-CTA shared-memory histogram of list ids, flushed with one global add per bin.
+// Members are placed in point-chunk order: CTA c handles the points of chunk
+// c ([c chunkPts, (c + 1) chunkPts)).  k_index_count writes each chunk's
+// per-list counts (list-major, chunkOff[l][c]) and the list totals;
+// k_chunk_scan turns every list's row into offsets; k_index_scatter places
+// the chunk's members from those offsets (order inside a chunk is free).
 __global__ void k_index_count(IndexArgs a) {
     extern __shared__ int hist[];
-    const int L = 2 * a.nproj;
+    const int L = 2 * a.nproj, c = blockIdx.x;
     for (int i = threadIdx.x; i < L; i += blockDim.x) hist[i] = 0;
     __syncthreads();
-    const size_t total = (size_t)a.n * 2 * a.k;
-    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
-        const int p = (int)(q / (2 * a.k)), slot = (int)(q % (2 * a.k));
-        atomicAdd(&hist[list_of(a.topK, p, slot, a.k, a.nproj)], 1);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < L; i += blockDim.x)
-        if (hist[i]) atomicAdd(reinterpret_cast<unsigned long long*>(a.listCount) + i, (unsigned long long)hist[i]);
-}
-
-// Same traversal; each CTA reserves a contiguous range per list, then places
-// its members inside it.
-__global__ void k_index_scatter(IndexArgs a) {
-    extern __shared__ int sh[];
-    const int L = 2 * a.nproj;
-    int* hist = sh;
-    int* base = sh + L;
-    for (int i = threadIdx.x; i < L; i += blockDim.x) hist[i] = 0;
-    __syncthreads();
-    const size_t total = (size_t)a.n * 2 * a.k;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += stride) {
+    const int p0 = c * a.chunkPts, p1 = min(a.n, p0 + a.chunkPts);
+    const size_t q1 = (size_t)p1 * 2 * a.k;
+    for (size_t q = (size_t)p0 * 2 * a.k + threadIdx.x; q < q1; q += blockDim.x) {
         const int p = (int)(q / (2 * a.k)), slot = (int)(q % (2 * a.k));
         atomicAdd(&hist[list_of(a.topK, p, slot, a.k, a.nproj)], 1);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < L; i += blockDim.x) {
-        const int c = hist[i];
-        base[i] = c ? (int)(a.listOff[i] +
-                            (int64_t)atomicAdd(reinterpret_cast<unsigned long long*>(a.listFill) + i,
-                                               (unsigned long long)c))
-                    : 0;
-        hist[i] = 0;
+        a.chunkOff[(size_t)i * a.nChunks + c] = hist[i];
+        if (hist[i]) atomicAdd(reinterpret_cast<unsigned long long*>(a.listCount) + i, (unsigned long long)hist[i]);
     }
+}
+
+// Warp per list: exclusive scan of its chunk counts, in place.
+__global__ void k_chunk_scan(IndexArgs a) {
+    const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (l >= 2 * a.nproj) return;
+    int32_t* row = a.chunkOff + (size_t)l * a.nChunks;
+    int run = 0;
+    for (int c0 = 0; c0 < a.nChunks; c0 += 32) {
+        const int c = c0 + lane;
+        const int v = c < a.nChunks ? row[c] : 0;
+        int incl = v;
+#pragma unroll
+        for (int s = 1; s < 32; s <<= 1) {
+            const int o = __shfl_up_sync(0xffffffffu, incl, s);
+            if (lane >= s) incl += o;
+        }
+        if (c < a.nChunks) row[c] = run + incl - v;
+        run += __shfl_sync(0xffffffffu, incl, 31);
+    }
+}
+
+__global__ void k_index_scatter(IndexArgs a) {
+    extern __shared__ int cursor[];
+    const int L = 2 * a.nproj, c = blockIdx.x;
+    for (int i = threadIdx.x; i < L; i += blockDim.x)
+        cursor[i] = (int)a.listOff[i] + a.chunkOff[(size_t)i * a.nChunks + c];
     __syncthreads();
-    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += stride) {
+    const int p0 = c * a.chunkPts, p1 = min(a.n, p0 + a.chunkPts);
+    const size_t q1 = (size_t)p1 * 2 * a.k;
+    for (size_t q = (size_t)p0 * 2 * a.k + threadIdx.x; q < q1; q += blockDim.x) {
         const int p = (int)(q / (2 * a.k)), slot = (int)(q % (2 * a.k));
-        const int l = list_of(a.topK, p, slot, a.k, a.nproj);
-        const int pos = atomicAdd(&hist[l], 1);
-        a.members[(size_t)base[l] + pos] = make_int2(p, slot);
+        const int pos = atomicAdd(&cursor[list_of(a.topK, p, slot, a.k, a.nproj)], 1);
+        a.members[pos] = make_int2(p, slot);
     }
+}
+
+// Tile order: counting sort of the tiles by the chunk of their first member.
+__global__ void k_tile_keys(IndexArgs a) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.tileOff[2 * a.nproj]) return;
+    const int l = a.tileList[t];
+    const int mt = (int)((t - a.tileOff[l]) / a.nct);
+    const int key = a.members[a.listOff[l] + (int64_t)mt * a.TM].x / a.chunkPts;
+    a.tileKey[t] = key;
+    atomicAdd(reinterpret_cast<unsigned long long*>(a.keyOff) + key, 1ull);
+}
+
+__global__ void k_tile_perm(IndexArgs a) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.tileOff[2 * a.nproj]) return;
+    const unsigned long long pos =
+        atomicAdd(reinterpret_cast<unsigned long long*>(a.keyOff) + a.tileKey[t], 1ull);
+    a.tilePerm[pos] = (int32_t)t;
 }
 
 // tiles per list -> listCount reused as the tile count input of the scan
@@ -199,20 +227,29 @@ int launch_scan_i64(const int64_t* in, int64_t* out, size_t n, int64_t* tmp, cud
 
 int launch_index_count(const IndexArgs& a, cudaStream_t st) {
     const size_t sm = sizeof(int) * 2 * a.nproj;
-    const size_t total = (size_t)a.n * 2 * a.k;
-    int grid = (int)std::min<size_t>((total + 1023) / 1024, 152 * 8);
-    if (grid < 1) grid = 1;
-    k_index_count<<<grid, 1024, sm, st>>>(a);
-    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+    k_index_count<<<a.nChunks, 1024, sm, st>>>(a);
+    if (cudaPeekAtLastError() != cudaSuccess) return -1;
+    const int L = 2 * a.nproj;
+    k_chunk_scan<<<(L * 32 + 255) / 256, 256, 0, st>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 2 : -1;
 }
 
 int launch_index_scatter(const IndexArgs& a, cudaStream_t st) {
-    const size_t sm = sizeof(int) * 4 * a.nproj;
-    const size_t total = (size_t)a.n * 2 * a.k;
-    int grid = (int)std::min<size_t>((total + 1023) / 1024, 152 * 8);
-    if (grid < 1) grid = 1;
-    k_index_scatter<<<grid, 1024, sm, st>>>(a);
+    const size_t sm = sizeof(int) * 2 * a.nproj;
+    k_index_scatter<<<a.nChunks, 1024, sm, st>>>(a);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int launch_tile_order(const IndexArgs& a, cudaStream_t st) {
+    if (a.maxTiles <= 0) return 0;
+    if (cudaMemsetAsync(a.keyOff, 0, sizeof(int64_t) * ((size_t)a.nChunks + 1), st) != cudaSuccess) return -1;
+    const unsigned g = (unsigned)((a.maxTiles + 255) / 256);
+    k_tile_keys<<<g, 256, 0, st>>>(a);
+    if (cudaPeekAtLastError() != cudaSuccess) return -1;
+    const int r = launch_scan_i64(a.keyOff, a.keyOff, (size_t)a.nChunks + 1, a.scanTmp, st);
+    if (r < 0) return -1;
+    k_tile_perm<<<g, 256, 0, st>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? r + 2 : -1;
 }
 
 // Computes tileOff (scan of per-list tile counts) into a.tileOff; tile counts
