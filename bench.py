@@ -21,6 +21,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -126,7 +127,9 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.idx = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu_index}.csv")
+        # the raw samples (the JSON line carries their summary); SDB_CLOCKS_DIR keeps them
+        self.path = os.path.join(os.environ.get("SDB_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"sdbscan_clocks_gpu{gpu_index}_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
