@@ -669,11 +669,14 @@ int orc_fit_soptics(const float* X, int n, int d, int code, int nproj, int k, in
 // eps is pushed into both lists (:459-464).  samplingProb >= 1: every other
 // point, forward only (:466-479).  Core points: list size, repeats counted,
 // >= minPts - 1; other lists cleared (:488-496); then formCluster.
-// labels / core / degree: n.  Returns n_clusters_, or a negative transform
-// error.  times[5] as orc_fit_sdbscan (index = 0).
+// labels / core / degree: n.  Returns n_clusters_, a negative transform
+// error, or -3 for one point with samplingProb < 1 (it can only draw itself).
+// times[5] as orc_fit_sdbscan (index = 0).
 int orc_fit_sngdbscan(const float* X, int n, int d, int code, float samplingProb, int seed, float eps, int minPts,
                       int threads, int32_t* labels, uint8_t* core, int32_t* degree, double* times) {
     if (threads > 0) omp_set_num_threads(threads);
+    if (n < 2 && samplingProb < 1.0 && std::ceil(1.0 * n * samplingProb) >= 1.0)
+        return -3;  // a single point draws only itself: the reference's loop never ends
     Timer tm, all;
     std::vector<float> Xc(X, X + (size_t)n * d);
     int err = orc_transform(Xc.data(), n, d, code);

@@ -106,6 +106,9 @@ sdb_status sdb_engine::fit_sng(const float* X, bool xOnDevice, const float* epsL
     if (optics && minPts < 2) return fail(SDB_ERR_ARG, "minPts must be >= 2 for sngOptics");
     const sdb_params& p = prm;
     if (p.distance < SDB_COSINE || p.distance > SDB_JS) return fail(SDB_ERR_ARG, "unknown distance");
+    if (n < 2 && !optics && p.samplingProb < 1.0 && std::ceil(1.0 * n * p.samplingProb) >= 1.0)
+        return fail(SDB_ERR_ARG, "sngDbscan with samplingProb < 1 needs n_points >= 2 (every draw of a single point "
+                                 "is itself, which the reference's draw loop never gets past)");
     haveLabels = haveOptics = haveFit = false;
     ld = (d + 3) & ~3;
     seedUsed = p.random_seed >= 0 ? p.random_seed

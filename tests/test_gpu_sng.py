@@ -157,6 +157,27 @@ def test_fit_sngoptics_matches_oracle(port, case):
     eng.close()
 
 
+def test_sng_single_point():
+    """One point: sampled sngDbscan cannot draw another point (the reference's
+    draw loop, src/sDbscan.cpp:449-465, never ends), so it is rejected; the
+    exact mode and sngOptics (which skips self draws) give one noise point."""
+    from sdbscan_gb300 import capi
+    X = np.ones((1, 8), np.float32)
+    eng = _sng_engine(X, "Cosine", 0.5, 3)
+    with pytest.raises(capi.SdbError) as e:
+        eng.fit_sngdbscan(X, 0.1, 2)
+    assert e.value.status == 1
+    eng.set_sng_params(distance="Cosine", samplingProb=1.0, random_seed=3)
+    eng.fit_sngdbscan(X, 0.1, 2)
+    labels, ncl = eng.labels()
+    assert labels.tolist() == [-1] and ncl == 2
+    eng.set_sng_params(distance="Cosine", samplingProb=0.5, random_seed=3)
+    eng.fit_sngoptics(X, 0.1, 2)
+    ordering, reach = eng.optics()
+    assert ordering.tolist() == [0] and reach[0] == np.float32(-2147483648.0)
+    eng.close()
+
+
 def test_sng_state_and_argument_errors():
     from sdbscan_gb300 import capi
     X = _data("Cosine", 500)
