@@ -119,7 +119,10 @@ sdb_status sdb_engine::derive() {
     const int mx = std::max(p.n_proj, ker);
     fhtDim = 1 << (int)std::ceil(std::log2((double)mx));  // src/sDbscan.h:107
     if (fhtDim < 16) return fail(SDB_ERR_ARG, "max(n_proj, ker_n_features) must be >= 9");
-    if (fhtDim > 2048) return fail(SDB_ERR_ARG, "max(n_proj, ker_n_features) must be <= 2048");
+    // vectors up to 2048 live in a warp's registers (k_project), up to 16384 in
+    // a CTA's shared memory (k_project_smem); n_proj stays within 2048
+    if (fhtDim > 16384) return fail(SDB_ERR_ARG, "max(n_proj, ker_n_features) must be <= 16384");
+    if (p.n_proj > 2048) return fail(SDB_ERR_ARG, "n_proj must be <= 2048");
     if (p.topK > 31) return fail(SDB_ERR_ARG, "topK must be <= 31");
     ld = (d + 3) & ~3;
     return SDB_OK;

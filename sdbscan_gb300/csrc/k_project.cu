@@ -94,6 +94,45 @@ __global__ void __launch_bounds__(kCsPoints) k_colstats(const float* __restrict_
     scale[p] = s;
 }
 
+// Element e of the Chi2 / JS embedding (src/Utilities.h:132-208) of a
+// transformed row (row: d values): sqrt terms for e < d, then the cos / sin
+// components; zero for e >= ker (the padding up to fhtDim).
+__device__ float embed_chi2js(const ProjectArgs& a, const float* row, int e) {
+    float t = 0.0f;
+    if (e >= a.ker) return t;
+    const float L = a.kerSam;
+    if (e < a.d) {
+        const float xv = row[e];
+        if (xv > 0.0f) {
+            if (a.dist == DIST_CHI2) t = __fsqrt_rn(__fmul_rn(xv, L));
+            else t = (float)__dsqrt_rn(__ddiv_rn(__dmul_rn((double)__fmul_rn(xv, L), 2.0), a.ln4));
+        }
+        return t;
+    }
+    const int comps = ((a.ker / a.d) - 1) / 2;
+    const int q = e - a.d;
+    const int c = q / (2 * a.d) + 1;  // component index
+    const int r = q % (2 * a.d);
+    const int i = r % a.d;
+    const bool isSin = r >= a.d;
+    const float xv = row[i];
+    if (c <= comps && xv > 0.0f) {
+        float f;
+        const double ch = a.compCosh[c - 1];  // cosh(PI*c*L), computed on the host
+        if (a.dist == DIST_CHI2) {
+            f = (float)__dsqrt_rn(__ddiv_rn(__dmul_rn(__dmul_rn(2.0, (double)xv), (double)L), ch));
+        } else {
+            const float cl = __fmul_rn((float)c, L);
+            const float qq = __fadd_rn(1.0f, __fmul_rn(__fmul_rn(4.0f, cl), cl));
+            f = (float)__ddiv_rn(2.0, __dmul_rn(__dmul_rn(a.ln4, (double)qq), ch));
+            f = (float)__dsqrt_rn(__dmul_rn(__dmul_rn(__dmul_rn(2.0, (double)xv), (double)L), (double)f));
+        }
+        const float ang = __fmul_rn(__fmul_rn((float)c, L), logf(xv));
+        t = __fmul_rn(f, isSin ? sinf(ang) : cosf(ang));
+    }
+    return t;
+}
+
 // Warp bitonic sort of 32 u64 keys, one per lane, into descending lane order.
 __device__ __forceinline__ uint64_t warp_sort_desc(uint64_t x) {
     const unsigned l = lane_id();
@@ -292,44 +331,8 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
             // Chi2 / JS embedding (src/Utilities.h:132-208) into the warp's row
             // buffer, lane-strided, then picked up per register below.
             __syncwarp();
-            const float L = a.kerSam;
-            const int comps = ((a.ker / a.d) - 1) / 2;
             float* emb = rowbuf + ((a.d + 3) & ~3);
-            for (int e = (int)l; e < FD; e += 32) {
-                float t = 0.0f;
-                if (e < a.ker) {
-                    if (e < a.d) {
-                        const float xv = rowbuf[e];
-                        if (xv > 0.0f) {
-                            if (a.dist == DIST_CHI2) t = __fsqrt_rn(__fmul_rn(xv, L));
-                            else t = (float)__dsqrt_rn(__ddiv_rn(__dmul_rn((double)__fmul_rn(xv, L), 2.0), a.ln4));
-                        }
-                    } else {
-                        const int q = e - a.d;
-                        const int c = q / (2 * a.d) + 1;  // component index
-                        const int r = q % (2 * a.d);
-                        const int i = r % a.d;
-                        const bool isSin = r >= a.d;
-                        const float xv = rowbuf[i];
-                        if (c <= comps && xv > 0.0f) {
-                            float f;
-                            const double ch = a.compCosh[c - 1];  // cosh(PI*c*L), computed on the host
-                            if (a.dist == DIST_CHI2) {
-                                f = (float)__dsqrt_rn(__ddiv_rn(__dmul_rn(__dmul_rn(2.0, (double)xv), (double)L), ch));
-                            } else {
-                                const float cl = __fmul_rn((float)c, L);
-                                const float qq = __fadd_rn(1.0f, __fmul_rn(__fmul_rn(4.0f, cl), cl));
-                                f = (float)__ddiv_rn(2.0, __dmul_rn(__dmul_rn(a.ln4, (double)qq), ch));
-                                f = (float)__dsqrt_rn(
-                                    __dmul_rn(__dmul_rn(__dmul_rn(2.0, (double)xv), (double)L), (double)f));
-                            }
-                            const float ang = __fmul_rn(__fmul_rn((float)c, L), logf(xv));
-                            t = __fmul_rn(f, isSin ? sinf(ang) : cosf(ang));
-                        }
-                    }
-                }
-                emb[e] = t;
-            }
+            for (int e = (int)l; e < FD; e += 32) emb[e] = embed_chi2js(a, rowbuf, e);
             __syncwarp();
         }
 #pragma unroll
@@ -416,6 +419,143 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
     if (l == 0 && localTies) atomicAdd(a.ties, (unsigned long long)localTies);
 }
 
+// Stage 1 for fhtDim > 2048 (d or ker_n_features above 2048), where the
+// rotation vector no longer fits a warp's registers: a CTA per point at a
+// time, the vector in shared memory.  Same arithmetic as k_project: the
+// transform, the embedding, three rounds of sign flips and FWHT stages in
+// ascending stride order with (a + b, a - b) per butterfly (the pairs of a
+// stage are independent, so their order does not change the bits), then the
+// top-k of each side by repeated block-wide argmax (ties toward the smaller
+// index, boundary ties counted) and the chunk extremes.
+constexpr int kBigThreads = 256;
+
+__device__ __forceinline__ uint64_t block_max_u64(uint64_t v, uint64_t* red) {
+    v = warp_max_u64(v);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        uint64_t x = (int)threadIdx.x < kBigThreads / 32 ? red[threadIdx.x] : 0ull;
+        x = warp_max_u64(x);
+        if (threadIdx.x == 0) red[kBigThreads / 32] = x;
+    }
+    __syncthreads();
+    const uint64_t r = red[kBigThreads / 32];
+    __syncthreads();
+    return r;
+}
+
+template <int EMB>
+__global__ void __launch_bounds__(kBigThreads) k_project_smem(ProjectArgs a, const float* __restrict__ scale) {
+    extern __shared__ float smem[];
+    const int FD = a.fhtDim;
+    const int ldr = (a.d + 3) & ~3;
+    float* v = smem;                                          // FD
+    float* row = v + FD;                                      // ldr: the transformed row
+    __nv_bfloat162* ext = reinterpret_cast<__nv_bfloat162*>(row + ldr);  // nproj
+    uint32_t* taken = reinterpret_cast<uint32_t*>(ext + a.nproj);        // nproj bits
+    __shared__ uint64_t red[kBigThreads / 32 + 1];
+    const int tid = threadIdx.x;
+    const int gEnd = a.chunkEnd > 0 ? a.chunkEnd : (a.n + a.chunk - 1) / a.chunk;
+    int localTies = 0;
+    for (int g = a.chunkBase + blockIdx.x; g < gEnd; g += gridDim.x) {
+        for (int e = tid; e < a.nproj; e += kBigThreads) ext[e] = __floats2bfloat162_rn(-INFINITY, -INFINITY);
+        const int p0 = g * a.chunk, p1 = min(a.n, p0 + a.chunk);
+        for (int p = p0; p < p1; ++p) {
+            const float sc = scale[p];
+            // transformed row -> Xt (zero padded to ld) and the embedding -> v
+            for (int i = tid; i < a.ld; i += kBigThreads) {
+                float t = 0.0f;
+                if (i < a.d) {
+                    t = __ldg(a.X + (size_t)p * a.ldx + i);
+                    if (a.do_transform && EMB != 1) t = __fdiv_rn(t, sc);
+                }
+                a.Xt[(size_t)p * a.ld + i] = t;
+                if (i < ldr) row[i] = t;
+            }
+            __syncthreads();
+            for (int e = tid; e < FD; e += kBigThreads) {
+                float t = 0.0f;
+                if (EMB == 0) t = e < a.d ? row[e] : 0.0f;
+                else if (EMB == 1) t = e < a.ker ? a.E[(size_t)p * a.ker + e] : 0.0f;
+                else t = embed_chi2js(a, row, e);
+                v[e] = t;
+            }
+            __syncthreads();
+            for (int r = 0; r < 3; ++r) {
+                for (int e = tid; e < FD; e += kBigThreads)  // a clear sign bit negates the element
+                    if (!((a.signs[(r * FD + e) >> 5] >> ((r * FD + e) & 31)) & 1u)) v[e] = -v[e];
+                __syncthreads();
+                for (int st = 1; st < FD; st <<= 1) {
+                    for (int b = tid; b < FD / 2; b += kBigThreads) {
+                        const int i = (b / st) * 2 * st + (b % st);
+                        const float x0 = v[i], x1 = v[i + st];
+                        v[i] = __fadd_rn(x0, x1);
+                        v[i + st] = __fsub_rn(x0, x1);
+                    }
+                    __syncthreads();
+                }
+            }
+            for (int e = tid; e < a.nproj; e += kBigThreads) {
+                const float x = v[e];
+                a.P[(size_t)p * a.nproj + e] = x;
+                __nv_bfloat162 b;
+                b.x = __float2bfloat16_rd(x);
+                b.y = __float2bfloat16_rd(-x);
+                ext[e] = __hmax2(ext[e], b);
+            }
+            // top-k per side: (key, smaller index) maxima, k + 1 rounds for the tie test
+            const int want = a.k + 1 <= a.nproj ? a.k + 1 : a.k;
+            for (int side = 0; side < 2; ++side) {
+                for (int e = tid; e < (a.nproj + 31) / 32; e += kBigThreads) taken[e] = 0u;
+                __syncthreads();
+                uint32_t kth = 0, last = 0;
+                for (int it = 0; it < want; ++it) {
+                    uint64_t best = 0;
+                    for (int e = tid; e < a.nproj; e += kBigThreads) {
+                        if ((taken[e >> 5] >> (e & 31)) & 1u) continue;
+                        uint32_t key = key_of(v[e]);
+                        if (side) key = ~key;
+                        const uint64_t pk = ((uint64_t)key << 32) | (uint64_t)(0xffffffffu - (uint32_t)e);
+                        best = pk > best ? pk : best;
+                    }
+                    best = block_max_u64(best, red);
+                    const int e = (int)(0xffffffffu - (uint32_t)best);
+                    if (tid == 0) {
+                        taken[e >> 5] |= 1u << (e & 31);
+                        if (it < a.k) a.topK[(size_t)p * 2 * a.k + side * a.k + it] = e;
+                    }
+                    if (it == a.k - 1) kth = (uint32_t)(best >> 32);
+                    if (it == a.k) last = (uint32_t)(best >> 32);
+                    __syncthreads();
+                }
+                if (want > a.k && kth == last && tid == 0) ++localTies;
+            }
+            __syncthreads();
+        }
+        for (int e = tid; e < a.nproj; e += kBigThreads) {
+            a.chunkMax[(size_t)g * a.nproj + e] = __bfloat162float(ext[e].x);
+            a.chunkMin[(size_t)g * a.nproj + e] = -__bfloat162float(ext[e].y);
+        }
+        __syncthreads();
+    }
+    if (tid == 0 && localTies) atomicAdd(a.ties, (unsigned long long)localTies);
+}
+
+template <int EMB>
+int launch_project_smem(const ProjectArgs& a, const float* scale, cudaStream_t st) {
+    const int G = (a.chunkEnd > 0 ? a.chunkEnd : (a.n + a.chunk - 1) / a.chunk) - a.chunkBase;
+    if (G <= 0) return 0;
+    const size_t sm = sizeof(float) * ((size_t)a.fhtDim + ((a.d + 3) & ~3)) + 4 * (size_t)a.nproj +
+                      4 * (size_t)((a.nproj + 31) / 32);
+    if (sm > 227 * 1024) return -1;
+    if (cudaFuncSetAttribute(k_project_smem<EMB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+        cudaSuccess)
+        return -1;
+    k_project_smem<EMB><<<std::min(G, 152 * 2), kBigThreads, sm, st>>>(a, scale);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
 // transformData alone (src/Utilities.h:289-335) for the fits that use no
 // projections (sngDbscan / sngOptics): Xt[p][e] = X[p][e] / scale[p] for
 // Cosine (norm) and Chi2 / JS (sum), X[p][e] for L1 / L2, zero past d up to
@@ -500,7 +640,11 @@ int launch_project(const ProjectArgs& a, cudaStream_t st) {
         case 512: r = launch_project_nj<16>(a, scale, st); break;
         case 1024: r = launch_project_nj<32>(a, scale, st); break;
         case 2048: r = launch_project_nj<64>(a, scale, st); break;
-        default: return -1;
+        default:
+            if (a.fhtDim < 4096) return -1;
+            if (a.dist == DIST_COSINE) r = launch_project_smem<0>(a, scale, st);
+            else if (a.dist == DIST_L1 || a.dist == DIST_L2) r = launch_project_smem<1>(a, scale, st);
+            else r = launch_project_smem<2>(a, scale, st);
     }
     return r < 0 ? -1 : r + 1;
 }

@@ -63,6 +63,11 @@ def cases():
     # the reference's unseeded rand() is never consulted
     yield "cosine_noise1nn_2000x32", X1, dict(n_proj=256, topK=5, topM=20, distance="Cosine", clusterNoise=1,
                                                samplingProb=1.0), 0.12, 12, False
+    # rotation vectors longer than 2048 (the shared-memory projection path)
+    X11, _ = ds.cfg1_cosine(600, 2100, seed=25)
+    yield "cosine_d2100_fht4096_600", X11, dict(n_proj=256, topK=5, topM=20, distance="Cosine"), 0.15, 8, False
+    yield "chi2_ker4096_1500x64", X4, dict(n_proj=256, topK=5, topM=20, distance="Chi2", ker_n_features=4096), \
+        0.3, 10, False
     X10, _ = ds.cfg4_dirichlet(1500, 64, n_comp=5, conc=10, seed=24)  # wider histograms: a third left as noise
     yield "chi2_noise1nn_1500x64", X10, dict(n_proj=256, topK=5, topM=20, distance="Chi2", ker_n_features=512,
                                               clusterNoise=1, samplingProb=1.0), 0.2, 12, False
