@@ -209,29 +209,21 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
         }
         uint64_t bits = 0;
         int nPass = 0;
+        if constexpr (SWEEP) {
 #pragma unroll 1
         for (int c16 = 0; c16 < TN / 16; ++c16) {
             float v[16];
             tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c16 * 16), v);
-            if (dbgAcc != nullptr && tid_ == 0) {  // accumulator of tile 0, for layout checks
-#pragma unroll
-                for (int j = 0; j < 16; ++j) dbgAcc[row * TN + c16 * 16 + j] = v[j];
-            }
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const int col = c16 * 16 + j;
                 const int q = colPoint[col];
-                bool pass = false, unsure = false;
-                if (p >= 0 && q >= 0) {
+                bool unsure = false;
+                if (p >= 0 && q >= 0) {  // keep the screened distance, re-decide near any eps
                     const float dist = 1.0f - v[j];
-                    if constexpr (SWEEP) {  // keep the screened distance, re-decide near any eps
-                        a.dists[((size_t)p * 2 * a.k + mySlot) * a.m + ct * TN + col] = dist;
-                        if (p != q)
-                            for (int e = 0; e < a.nSweep; ++e) unsure |= fabsf(dist - a.sweepEps[e]) <= kMargin;
-                    } else if (p != q) {
-                        pass = dist <= a.eps - kMargin;
-                        unsure = !pass && dist <= a.eps + kMargin;
-                    }
+                    a.dists[((size_t)p * 2 * a.k + mySlot) * a.m + ct * TN + col] = dist;
+                    if (p != q)
+                        for (int e = 0; e < a.nSweep; ++e) unsure |= fabsf(dist - a.sweepEps[e]) <= kMargin;
                 }
                 const unsigned um = __ballot_sync(0xffffffffu, unsure);
                 if (um) {
@@ -248,13 +240,66 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
                             atomicExch(err, 2);
                     }
                 }
-                if (pass) {
-                    bits |= 1ull << col;
-                    ++nPass;
-                }
-                const unsigned b = __ballot_sync(0xffffffffu, pass);
-                if (lane == 0 && b) atomicAdd(&colCount[col], __popc(b));
             }
+        }
+        } else {
+        // The row's 64 decisions as bit words: pass (screened distance below
+        // eps - margin), unsure (within the margin), near zero (the only place
+        // the point itself can be among the candidates); then the columns
+        // that do not exist, the row's own point and empty rows are masked out.
+        uint64_t uw = 0, zw = 0;
+        const float lo = a.eps - kMargin, hi = a.eps + kMargin;
+#pragma unroll
+        for (int c16 = 0; c16 < TN / 16; ++c16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c16 * 16), v);
+            if (dbgAcc != nullptr && tid_ == 0) {  // accumulator of tile 0, for layout checks
+#pragma unroll
+                for (int j = 0; j < 16; ++j) dbgAcc[row * TN + c16 * 16 + j] = v[j];
+            }
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float dist = 1.0f - v[j];
+                const bool pass = dist <= lo;
+                bits |= (uint64_t)pass << (c16 * 16 + j);
+                uw |= (uint64_t)(!pass && dist <= hi) << (c16 * 16 + j);
+                zw |= (uint64_t)(dist <= kMargin) << (c16 * 16 + j);
+            }
+        }
+        const int nvalid = a.m - ct * TN;
+        uint64_t keep = p < 0 ? 0ull : (nvalid >= 64 ? ~0ull : (1ull << nvalid) - 1ull);
+        for (uint64_t z = zw & keep & (bits | uw); z; z &= z - 1) {  // rare: is the row's point a candidate?
+            const int col = __ffsll((long long)z) - 1;
+            if (colPoint[col] == p) keep &= ~(1ull << col);
+        }
+        bits &= keep;
+        uw &= keep;
+        if (__any_sync(0xffffffffu, uw != 0)) {  // pairs within the margin go to the queue
+            const int cnt = __popcll(uw);
+            if (cnt) {
+                unsigned long long at = atomicAdd(qcount, (unsigned long long)cnt);
+                for (uint64_t u = uw; u; u &= u - 1, ++at) {
+                    const int col = __ffsll((long long)u) - 1;
+                    if ((int64_t)at < qcap)
+                        queue[at] = ((uint64_t)(uint32_t)p << 32) | ((uint32_t)mySlot << 16) |
+                                    (uint32_t)(ct * TN + col);
+                    else
+                        atomicExch(err, 2);
+                }
+            }
+        }
+        nPass = __popcll(bits);
+        int cc0 = 0, cc1 = 0;  // passes of columns lane and lane + 32
+#pragma unroll
+        for (int col = 0; col < TN; ++col) {
+            const int pc = __popc(__ballot_sync(0xffffffffu, (bits >> col) & 1ull));
+            if (lane == (col & 31)) {
+                if (col < 32) cc0 += pc;
+                else cc1 += pc;
+            }
+        }
+        if (cc0) atomicAdd(&colCount[lane], cc0);
+        if (cc1) atomicAdd(&colCount[lane + 32], cc1);
         }
         if (!SWEEP && p >= 0) a.masks[((size_t)p * 2 * a.k + mySlot) * a.W + ct] = bits;
         const int wp = warp_sum(nPass);
