@@ -176,7 +176,6 @@ struct IndexArgs {
     const int32_t* topM;  // nproj x 2m
     int64_t* listCount;   // 2*nproj + 1
     int64_t* listOff;     // 2*nproj + 1
-    int64_t* listFill;    // 2*nproj
     int2* members;        // n*2k (point, slot)
     int TM;               // member rows per distance tile
     int nct;              // candidate tiles per list
@@ -243,8 +242,7 @@ int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream
 int launch_to_bf16_split(const float* Xt, int ld, int n, void* Xs, int ldb, cudaStream_t st);
 int launch_screen_reset(const DistArgs& a, cudaStream_t st);
 int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, uint64_t* queue, int64_t qcap,
-                   unsigned long long* qcount, int32_t* err, int grid, cudaStream_t st,
-                   float* dbgAcc = nullptr);
+                   unsigned long long* qcount, int32_t* err, int grid, cudaStream_t st);
 int launch_recheck(const DistArgs& a, const uint64_t* queue, const unsigned long long* qcount, int64_t qcap,
                    cudaStream_t st);
 
@@ -341,7 +339,6 @@ struct SngArgs {
     int32_t* nbIdx;
     float* nbDist;
     int32_t* err;          // set when a list would overflow its slots
-    const int32_t* gate;   // optional: the FP32 block runs only if *gate != 0 (the BF16 screening failed)
     const uint64_t* heavy; // nct words: bit set for the columns drawn more than once (null: none)
 };
 // First block pass: pass bits (mask may be null), row degrees, column counts.

@@ -93,7 +93,7 @@ void sdb_engine::free_all() {
 
 std::vector<DevBuf*> sdb_engine::all_bufs() {
     return {&Xin, &Xt, &scale, &P, &topK, &chunkMax, &chunkMin, &thr, &cand, &candCount, &topM, &listCount,
-            &listOff, &listFill, &members, &tileOff, &tileList, &hubCount, &hubOff, &hubLists, &masks, &inRaw,
+            &listOff, &members, &tileOff, &tileList, &hubCount, &hubOff, &hubLists, &masks, &inRaw,
             &aCount, &degree, &core, &parent, &border, &rootFlag, &labels, &nClusters, &scanTmp, &errFlags,
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
             &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig, &Rb, &newMasks, &coreEps, &sampleFlag,
@@ -210,7 +210,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
           ensure(thr, sizeof(float) * 2 * D) && ensure(cand, sizeof(uint64_t) * (size_t)L * cap) &&
           ensure(candCount, sizeof(int32_t) * L) && ensure(topM, sizeof(int32_t) * (size_t)D * 2 * m) &&
           ensure(listCount, sizeof(int64_t) * (L + 1)) && ensure(listOff, sizeof(int64_t) * (L + 1)) &&
-          ensure(listFill, sizeof(int64_t) * L) && ensure(members, sizeof(int2) * (size_t)n * 2 * k) &&
+          ensure(members, sizeof(int2) * (size_t)n * 2 * k) &&
           ensure(tileOff, sizeof(int64_t) * (L + 1)) && ensure(tileList, sizeof(int32_t) * (size_t)maxTiles) &&
           ensure(hubCount, sizeof(int32_t) * n) && ensure(hubOff, sizeof(int64_t) * (n + 1)) &&
           ensure(hubLists, sizeof(int32_t) * (size_t)L * m) &&
@@ -377,7 +377,6 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     ia.topM = i32(topM);
     ia.listCount = i64(listCount);
     ia.listOff = i64(listOff);
-    ia.listFill = i64(listFill);
     ia.members = static_cast<int2*>(members.ptr);
     ia.TM = TMr;
     ia.nct = nct;
@@ -395,7 +394,6 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     ia.tilePerm = i32(tilePerm);
     ia.maxTiles = maxTiles;
     SDB_CK(cudaMemsetAsync(listCount.ptr, 0, sizeof(int64_t) * (L + 1), st));
-    SDB_CK(cudaMemsetAsync(listFill.ptr, 0, sizeof(int64_t) * L, st));
     SDB_CK(cudaMemsetAsync(hubCount.ptr, 0, sizeof(int32_t) * n, st));
     SDB_CK(cudaMemsetAsync(hubOff.ptr, 0, sizeof(int64_t) * (n + 1), st));
     L_(launch_index_count(ia, st));

@@ -69,8 +69,7 @@ __device__ __forceinline__ uint32_t sw128(int r, int c) {
 template <bool SWEEP>
 __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat16* __restrict__ Xb, int ldb,
                                                   uint64_t* __restrict__ queue, int64_t qcap,
-                                                  unsigned long long* __restrict__ qcount, int32_t* __restrict__ err,
-                                                  float* __restrict__ dbgAcc) {
+                                                  unsigned long long* __restrict__ qcount, int32_t* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smraw[];
     __shared__ uint64_t bars[STAGES];
     __shared__ uint32_t tmemBase;
@@ -161,8 +160,8 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
 
     int tb = 0;  // parity of the current tile's buffers
     for (int64_t t = blockIdx.x; t < total; t += gridDim.x, tb ^= 1) {
-        const int64_t tid_ = tile_at(a.tilePerm, t);
-        const int ct = (int)((tid_ - a.tileOff[a.tileList[tid_]]) % a.nct);
+        const int64_t tileId = tile_at(a.tilePerm, t);
+        const int ct = (int)((tileId - a.tileOff[a.tileList[tileId]]) % a.nct);
         const int* colPoint = colPoints[tb];
         for (int kc = 0; kc < nk; ++kc) {
             const int stage = kc % STAGES;
@@ -253,10 +252,6 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
         for (int c16 = 0; c16 < TN / 16; ++c16) {
             float v[16];
             tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c16 * 16), v);
-            if (dbgAcc != nullptr && tid_ == 0) {  // accumulator of tile 0, for layout checks
-#pragma unroll
-                for (int j = 0; j < 16; ++j) dbgAcc[row * TN + c16 * 16 + j] = v[j];
-            }
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const float dist = 1.0f - v[j];
@@ -427,12 +422,12 @@ int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream
 }
 
 int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, uint64_t* queue, int64_t qcap,
-                   unsigned long long* qcount, int32_t* err, int grid, cudaStream_t st, float* dbgAcc) {
+                   unsigned long long* qcount, int32_t* err, int grid, cudaStream_t st) {
     const size_t sm = (size_t)STAGES * STAGE_BYTES + 1024;
     auto kern = a.dists != nullptr ? k_dist_tc<true> : k_dist_tc<false>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return -1;
-    kern<<<grid, NT, sm, st>>>(a, static_cast<const __nv_bfloat16*>(Xb), ldb, queue, qcap, qcount, err, dbgAcc);
+    kern<<<grid, NT, sm, st>>>(a, static_cast<const __nv_bfloat16*>(Xb), ldb, queue, qcap, qcount, err);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 

@@ -45,7 +45,6 @@ size_t block_smem() {
 // (a few MB) stay L2-resident.
 template <int DIST, bool EMIT>
 __global__ void __launch_bounds__(kNT, 2) k_sng_block(SngArgs a) {
-    if (a.gate != nullptr && __ldg(a.gate) == 0) return;  // the BF16 screening succeeded
     extern __shared__ __align__(16) float sm[];
     float* As = sm;                           // STAGES x TM x LDS
     float* Bs = As + STAGES * TM * LDS;       // STAGES x 64 x LDS
