@@ -220,7 +220,7 @@ struct DistArgs {
     int nct;              // candidate tiles per list
     float eps;
     float epsLo;          // eps sweeps: k_masks_from_dists keeps epsLo < d <= eps
-    const uint8_t* pairRound;  // eps sweeps (optional): per pair, the first round whose eps >= d
+    const uint8_t* pairRound;  // eps sweeps (optional): per pair, the first round whose eps >= d (rows of W x 64 bytes)
     int round;
     int variant;               // plain distance tiles: 0 by m, 1: 128 x 64 (256 threads), 2-3: 128 x 50 (160 threads; k_dist.cu)
     uint64_t* masks;      // n x 2k x W
@@ -236,7 +236,8 @@ constexpr int kMaxScreenedSweep = 16;
 int launch_dist(const DistArgs& a, cudaStream_t st);
 int launch_masks_from_dists(const DistArgs& a, cudaStream_t st);
 // Eps sweeps: each pair's round (index of the first of the nSweep ascending
-// sweepEps values >= its distance; nSweep when none), n x 2k x m bytes.
+// sweepEps values >= its distance; nSweep when none; 255 for the point's own
+// entry and padding), n x 2k rows of W x 64 bytes.
 int launch_pair_rounds(const DistArgs& a, uint8_t* rounds, cudaStream_t st);
 int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream_t st);
 int launch_to_bf16_split(const float* Xt, int ld, int n, void* Xs, int ldb, cudaStream_t st);

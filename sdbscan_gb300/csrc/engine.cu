@@ -507,7 +507,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         if (rounds <= kMaxScreenedSweep) {  // one byte per pair: the round in which it joins
             da.nSweep = rounds;
             for (int e = 0; e < rounds; ++e) da.sweepEps[e] = sw->eps[ord[e]];
-            if (!ensure(pairRound, (size_t)n * 2 * k * m)) return SDB_ERR_NOMEM;
+            if (!ensure(pairRound, (size_t)n * 2 * k * W * 64)) return SDB_ERR_NOMEM;
             L_(launch_pair_rounds(da, static_cast<uint8_t*>(pairRound.ptr), st));
             da.pairRound = static_cast<const uint8_t*>(pairRound.ptr);
         }

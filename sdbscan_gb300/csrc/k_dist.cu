@@ -196,12 +196,8 @@ __global__ void k_masks_from_dists(DistArgs a) {
             if (c < a.m) {
                 const int cp = __ldg(cand + c);
                 const size_t at = ((size_t)p * 2 * a.k + slot) * a.m + c;
-                if (a.pairRound != nullptr) {
-                    pass = cp != p && __ldg(a.pairRound + at) == a.round;
-                } else {
-                    const float dd = __ldg(a.dists + at);
-                    pass = cp != p && dd <= a.eps && dd > a.epsLo;
-                }
+                const float dd = __ldg(a.dists + at);
+                pass = cp != p && dd <= a.eps && dd > a.epsLo;
                 if (pass) {
                     atomicAdd(&colCount[col], 1);
                     ++myPass;
@@ -223,27 +219,102 @@ __global__ void k_masks_from_dists(DistArgs a) {
 
 // One pass over the stored distances: the sweep round in which each pair
 // joins (its distance's rank among the ascending eps values), so that every
-// round reads one byte per pair instead of the distance.
-__global__ void k_pair_rounds(const float* __restrict__ dists, size_t count, DistArgs a, uint8_t* __restrict__ rounds) {
+// round reads one byte per pair instead of the distance.  Rows (point, slot)
+// are padded to W * 64 bytes so a round reads them with aligned 16-byte
+// loads; padding columns and the point's own entry (a candidate equal to the
+// point, src/sDbscan.cpp:272) get 255, which no round matches.
+__global__ void k_pair_rounds(const float* __restrict__ dists, DistArgs a, uint32_t* __restrict__ rounds) {
+    const int g4 = a.W * 16;  // four-column groups per padded row
+    const size_t count = (size_t)a.n * 2 * a.k * g4;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
-        const float d = __ldg(dists + i);
-        int r = 0;
-        while (r < a.nSweep && a.sweepEps[r] < d) ++r;
-        rounds[i] = (uint8_t)r;
+        const size_t row = i / g4;
+        const int c0 = (int)(i % g4) * 4;
+        const int p = (int)(row / (2 * a.k)), slot = (int)(row % (2 * a.k));
+        const int32_t* cand = a.topM + (size_t)__ldg(a.topKmat + row) * 2 * a.m + (slot >= a.k ? a.m : 0);
+        uint32_t out = 0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int c = c0 + b;
+            int r = 255;
+            if (c < a.m && __ldg(cand + c) != p) {
+                const float d = __ldg(dists + row * a.m + c);
+                r = 0;
+                while (r < a.nSweep && a.sweepEps[r] < d) ++r;
+            }
+            out |= (uint32_t)r << (8 * b);
+        }
+        rounds[i] = out;
+    }
+}
+
+// A round's masks from the pair rounds: thread per member row of a tile; the
+// row's 64 round bytes for this tile come in as four 16-byte loads and are
+// compared four at a time (__vcmpeq4), giving the row's mask word directly;
+// the column counts (reverse edges) are reduced with one ballot per column.
+__global__ void __launch_bounds__(TM) k_masks_from_rounds(DistArgs a) {
+    __shared__ int colCount[TN];
+    if ((int64_t)blockIdx.x >= *a.tileTotal) return;
+    const int64_t t = tile_at(a.tilePerm, blockIdx.x);
+    const int l = a.tileList[t];
+    const int64_t ti = t - a.tileOff[l];
+    const int mt = (int)(ti / a.nct), ct = (int)(ti % a.nct);
+    const int64_t q = a.listOff[l] + (int64_t)mt * TM + threadIdx.x;
+    const bool valid = q < a.listOff[l + 1];
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x < TN) colCount[threadIdx.x] = 0;
+    __syncthreads();
+    uint64_t w = 0;
+    int2 mb = make_int2(0, 0);
+    if (valid) {
+        mb = a.members[q];
+        const uint4* src = reinterpret_cast<const uint4*>(a.pairRound + ((size_t)mb.x * 2 * a.k + mb.y) * (a.W * 64) +
+                                                          (size_t)ct * 64);
+        const uint32_t rr = 0x01010101u * (uint32_t)a.round;
+#pragma unroll
+        for (int v4 = 0; v4 < 4; ++v4) {
+            const uint4 x = __ldg(src + v4);
+            const uint32_t words[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+            for (int k4 = 0; k4 < 4; ++k4) {
+                // low bit of each equal byte, gathered into a nibble
+                const uint32_t eq = __vcmpeq4(words[k4], rr) & 0x01010101u;
+                w |= (uint64_t)((eq * 0x10204080u) >> 28) << (v4 * 16 + k4 * 4);
+            }
+        }
+        a.masks[((size_t)mb.x * 2 * a.k + mb.y) * a.W + ct] = w;
+    }
+    int cc0 = 0, cc1 = 0;  // passes of columns lane and lane + 32 in this warp
+#pragma unroll
+    for (int col = 0; col < TN; ++col) {
+        const int pc = __popc(__ballot_sync(0xffffffffu, (w >> col) & 1ull));
+        if (lane == (col & 31)) {
+            if (col < 32) cc0 += pc;
+            else cc1 += pc;
+        }
+    }
+    if (cc0) atomicAdd(&colCount[lane], cc0);
+    if (cc1) atomicAdd(&colCount[lane + 32], cc1);
+    const int wp = warp_sum(__popcll(w));
+    if (lane == 0 && wp) atomicAdd(a.pairs, (unsigned long long)wp);
+    __syncthreads();
+    if (threadIdx.x < TN && colCount[threadIdx.x]) {
+        const int r = l % a.nproj, side = l / a.nproj;
+        const int c = ct * TN + threadIdx.x;
+        atomicAdd(a.inRaw + __ldg(a.topM + (size_t)r * 2 * a.m + side * a.m + c), colCount[threadIdx.x]);
     }
 }
 
 }  // namespace
 
 int launch_pair_rounds(const DistArgs& a, uint8_t* rounds, cudaStream_t st) {
-    const size_t count = (size_t)a.n * 2 * a.k * a.m;
-    k_pair_rounds<<<152 * 16, 256, 0, st>>>(a.dists, count, a, rounds);
+    k_pair_rounds<<<152 * 16, 256, 0, st>>>(a.dists, a, reinterpret_cast<uint32_t*>(rounds));
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
 int launch_masks_from_dists(const DistArgs& a, cudaStream_t st) {
     if (a.nTiles <= 0) return 0;
-    k_masks_from_dists<<<(unsigned)a.nTiles, 256, 0, st>>>(a);
+    if (a.pairRound != nullptr) k_masks_from_rounds<<<(unsigned)a.nTiles, TM, 0, st>>>(a);
+    else k_masks_from_dists<<<(unsigned)a.nTiles, 256, 0, st>>>(a);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
