@@ -92,8 +92,8 @@ sdb_status sdb_set_params(sdb_engine* e, const sdb_params* p);
 sdb_status sdb_set_precision(sdb_engine* e, int32_t precision);
 
 /* Tile shape of the plain FP32 distance kernel (a tuning control; no
- * reference counterpart): 0 = by topM (default: shape 3 for topM in 41..50,
- * else 1), 1 = 128 x 64 tiles on 256 threads, 2 = 128 x 50 on 160 threads
+ * reference counterpart): 0 = by topM and distance (default: for topM in
+ * 41..50 shape 3 with Cosine, shape 2 otherwise; else 1), 1 = 128 x 64 tiles on 256 threads, 2 = 128 x 50 on 160 threads
  * (32 dimensions per stage, 2 stages), 3 = 128 x 50 with 16 dimensions per
  * stage in 4 stages.  The 50-column shapes apply when topM <= 50 (else shape
  * 1).  Any shape gives the same bits. */
