@@ -29,13 +29,46 @@ using namespace sdb;
 namespace {
 
 // formOptics_scikit with (reachability, point id) order.  reach[] holds
-// NEG_INF (-2^31) for points never reached (src/sDbscan.cpp:1590).
+// NEG_INF (-2^31) for points never reached (src/sDbscan.cpp:1590).  The
+// reference keeps a lazy-deletion heap (Min_PQ_Pair seedSet, :1609); here the
+// seed queue is an indexed 4-ary min-heap on (reach, id) with decrease-key,
+// each unprocessed point in it at most once: the same pop sequence as a lazy
+// heap with that order, with fewer heap operations.
 void form_optics(int n, const uint8_t* core, const float* coreDist, const int64_t* off, const int32_t* idx,
                  const float* dist, int32_t* ordering, float* reach) {
     std::fill(reach, reach + n, kNegInfReach);
     std::vector<uint8_t> done(n, 0);
-    typedef std::pair<float, int> E;
-    std::priority_queue<E, std::vector<E>, std::greater<E>> heap;
+    std::vector<int32_t> pos(n, -1), heap;
+    heap.reserve(4096);
+    auto less = [&](int a, int b) { return reach[a] < reach[b] || (reach[a] == reach[b] && a < b); };
+    auto sift_up = [&](int i) {
+        const int y = heap[i];
+        while (i > 0) {
+            const int par = (i - 1) >> 2;
+            if (!less(y, heap[par])) break;
+            heap[i] = heap[par];
+            pos[heap[i]] = i;
+            i = par;
+        }
+        heap[i] = y;
+        pos[y] = i;
+    };
+    auto sift_down = [&](int i) {
+        const int y = heap[i], sz = (int)heap.size();
+        while (true) {
+            const int c0 = 4 * i + 1;
+            if (c0 >= sz) break;
+            int b = c0;
+            for (int c = c0 + 1; c < std::min(c0 + 4, sz); ++c)
+                if (less(heap[c], heap[b])) b = c;
+            if (!less(heap[b], y)) break;
+            heap[i] = heap[b];
+            pos[heap[i]] = i;
+            i = b;
+        }
+        heap[i] = y;
+        pos[y] = i;
+    };
     int64_t no = 0;
     auto relax = [&](int x) {
         const float cd = coreDist[x];
@@ -43,9 +76,13 @@ void form_optics(int n, const uint8_t* core, const float* coreDist, const int64_
             const int y = idx[t];
             if (done[y]) continue;
             const float r = std::max(cd, dist[t]);
-            if (reach[y] == kNegInfReach || reach[y] > r) {
+            if (reach[y] == kNegInfReach) {
                 reach[y] = r;
-                heap.push(E(r, y));
+                heap.push_back(y);
+                sift_up((int)heap.size() - 1);
+            } else if (reach[y] > r) {
+                reach[y] = r;
+                sift_up(pos[y]);
             }
         }
     };
@@ -56,9 +93,14 @@ void form_optics(int n, const uint8_t* core, const float* coreDist, const int64_
         if (!core[p]) continue;
         relax(p);
         while (!heap.empty()) {
-            const int y = heap.top().second;
-            heap.pop();
-            if (done[y]) continue;
+            const int y = heap[0];
+            const int last = heap.back();
+            heap.pop_back();
+            if (!heap.empty()) {
+                heap[0] = last;
+                sift_down(0);
+            }
+            pos[y] = -1;
             done[y] = 1;
             ordering[no++] = y;
             if (core[y]) relax(y);
