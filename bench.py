@@ -79,6 +79,23 @@ def _dist_env():
     return ws, rank, local
 
 
+def _max_over_ranks(x: float, ws: int, device) -> float:
+    """The largest of every rank's x: a replicated job takes its slowest
+    replica's time."""
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _replica_rate(units_per_rank: float, steps: int, ws: int, seconds: float) -> float:
+    """Whole-job throughput of ws replicas that each process units_per_rank per step."""
+    return ws * units_per_rank * steps / seconds
+
+
 def _host_data(cfg, n):
     """The workload's law, n points, as a numpy (n, d) float32 array."""
     from sdbscan_gb300 import datasets
@@ -504,12 +521,8 @@ def run_ours(args, cfg):
             launches += eng.counters()["launches"]
         end.record(stream)
         barrier()
-    ms = start.elapsed_time(end)
-    if ws > 1:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * n * args.steps / (ms / 1e3)
+    ms = _max_over_ranks(start.elapsed_time(end), ws, f"cuda:{local}")
+    value = _replica_rate(n, args.steps, ws, ms / 1e3)
     counters = eng.counters()
     res = result()
     labels = None if optics else res[0]
@@ -574,8 +587,8 @@ def run_ours(args, cfg):
         for k_, v_ in eng.stage_ms().items():
             e2e_stages[k_] = e2e_stages.get(k_, 0.0) + v_ / args.steps
     barrier()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = ws * n * args.steps / e2e_s
+    e2e_s = _max_over_ranks(time.perf_counter() - t0, ws, f"cuda:{local}")
+    e2e_value = _replica_rate(n, args.steps, ws, e2e_s)
     assert all(np.array_equal(a, b) for a, b in zip(res_e2e[:1], res[:1])), "host-input and device-input fits disagree"
     d2h = n * 8 if optics else n * 4 + 4
 
