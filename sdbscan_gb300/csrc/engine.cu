@@ -124,6 +124,8 @@ sdb_status sdb_engine::derive() {
     if (fhtDim > 16384) return fail(SDB_ERR_ARG, "max(n_proj, ker_n_features) must be <= 16384");
     if (p.n_proj > 2048) return fail(SDB_ERR_ARG, "n_proj must be <= 2048");
     if (p.topK > 31) return fail(SDB_ERR_ARG, "topK must be <= 31");
+    if ((int64_t)n * 2 * p.topK >= ((int64_t)1 << 31))
+        return fail(SDB_ERR_ARG, "n_points * 2 * topK must stay below 2^31 (32-bit member indexing)");
     ld = (d + 3) & ~3;
     return SDB_OK;
 }
