@@ -95,7 +95,7 @@ sdb_status sdb_set_precision(sdb_engine* e, int32_t precision);
  * reference counterpart): 0 = by topM and distance (default: for topM in
  * 41..50 shape 3 with Cosine, shape 2 otherwise; else 1), 1 = 128 x 64 tiles on 256 threads, 2 = 128 x 50 on 160 threads
  * (32 dimensions per stage, 2 stages), 3 = 128 x 50 with 16 dimensions per
- * stage in 4 stages.  The 50-column shapes apply when topM <= 50 (else shape
+ * stage in 4 stages (Cosine; shape 2 for the other distances).  The 50-column shapes apply when topM <= 50 (else shape
  * 1).  Any shape gives the same bits. */
 sdb_status sdb_set_tile_variant(sdb_engine* e, int32_t variant);
 

@@ -151,16 +151,17 @@ template <int DIST, int TX, int CN, int KT = TK, int NST = STAGES> int launch_di
 // dimensions, 2 stages), 3 = 128 x 50 (160 threads, 16 dimensions, 4 stages:
 // the same shared memory, half the work between barriers and twice the loads
 // in flight; 3 % faster than 2 for Cosine at 1M x 784, 2.5 % slower for Chi2
-// at 500K x 512).  The 50-column shapes need m <= 50.
+// at 500K x 512, so the other distances run shape 2 for it).  The 50-column
+// shapes need m <= 50.
 template <int DIST> int launch_dist_t(const DistArgs& a, cudaStream_t st) {
     const bool fits50 = a.m <= 50;
     switch (a.variant) {
         case 2: if (fits50) return launch_dist_v<DIST, 10, 5>(a, st); break;
-        case 3: if (fits50) return launch_dist_v<DIST, 10, 5, 16, 4>(a, st); break;
-        case 0:  // the 4-stage shape pays off for the FMA-bound Cosine tile only (Chi2: 2.5 % slower)
-            if (a.m > 40 && fits50) {
-                if (DIST == DIST_COSINE) return launch_dist_v<DIST, 10, 5, 16, 4>(a, st);
-                return launch_dist_v<DIST, 10, 5>(a, st);
+        case 3:  // the 4-stage shape is built for the FMA-bound Cosine tile only (Chi2: 2.5 % slower)
+        case 0:
+            if (fits50 && (a.variant == 3 || a.m > 40)) {
+                if constexpr (DIST == DIST_COSINE) return launch_dist_v<DIST, 10, 5, 16, 4>(a, st);
+                else return launch_dist_v<DIST, 10, 5>(a, st);
             }
             break;
         default: break;
