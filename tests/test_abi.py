@@ -73,3 +73,24 @@ def test_load_txt_parses_like_fscanf(tmp_path):
         capi.load_txt(path, 701, 13)
     with pytest.raises(capi.SdbError):
         capi.load_txt(tmp_path / "missing.txt", 2, 2)
+
+
+# The reference binding's names (python/python_wrapper.cpp:14-65): every
+# method and result member a caller of the reference module uses.
+REFERENCE_MODULE_NAMES = (
+    "set_params", "set_sngParams", "clear", "set_topM", "set_threads", "set_clusterNoise", "set_topK",
+    "set_kernel_params", "fit_sDbscan", "load_fit_sDbscan", "test_sDbscan", "load_test_sDbscan", "fit_sOptics",
+    "load_fit_sOptics", "fit_sngDbscan", "test_sngDbscan", "load_test_sngDbscan", "fit_sngOptics",
+    "load_fit_sngOptics", "labels_", "n_clusters_", "ordering_", "reachability_")
+
+
+def test_dropin_module_has_every_reference_name():
+    """The pybind module `sDbscan` (importable without a GPU) exposes the
+    reference binding's class with all of its methods and result members."""
+    import importlib
+    try:
+        mod = importlib.import_module("sdbscan_gb300.sDbscan")
+    except ImportError as e:
+        pytest.skip(f"drop-in module not built here: {e}")
+    missing = [n for n in REFERENCE_MODULE_NAMES if not hasattr(mod.sDbscan, n)]
+    assert not missing, missing
