@@ -11,14 +11,18 @@ from sdbscan_gb300 import datasets as ds
 pytestmark = pytest.mark.skipif(not os.path.exists(REF_SO), reason="reference library not built here")
 
 
-@pytest.mark.parametrize("dist,eps,ker", [("Cosine", 0.15, 1024), ("Chi2", 0.3, 512), ("L2", 0.6, 256)])
+def _data(dist, n=3000):
+    if dist in ("Chi2", "JS"):
+        return ds.cfg4_dirichlet(n, 64, n_comp=6, seed=21)[0]
+    if dist in ("L1", "L2"):
+        return ds.cfg3_aniso_l2(n, 16, n_comp=6, scale=0.1, seed=21)[0]
+    return ds.cfg1_cosine(n, 48, seed=21)[0]
+
+
+@pytest.mark.parametrize("dist,eps,ker", [("Cosine", 0.15, 1024), ("Chi2", 0.3, 512), ("L2", 0.6, 256),
+                                          ("L1", 1.5, 256), ("JS", 0.02, 512)])
 def test_multithreaded_fit_labels(port, dist, eps, ker):
-    if dist == "Chi2":
-        X, _ = ds.cfg4_dirichlet(3000, 64, n_comp=6, seed=21)
-    elif dist == "L2":
-        X, _ = ds.cfg3_aniso_l2(3000, 16, n_comp=6, scale=0.1, seed=21)
-    else:
-        X, _ = ds.cfg1_cosine(3000, 48, seed=21)
+    X = _data(dist)
     n, d = X.shape
     r = Ref(n, d)
     r.set_params(n_proj=256, topK=5, topM=20, distance=dist, ker_n_features=ker, ker_sigma=0.5, n_threads=4,
@@ -26,6 +30,41 @@ def test_multithreaded_fit_labels(port, dist, eps, ker):
     r.fit_sDbscan(X, eps, 10)
     labels, ncl, core, _ = port.fit_sdbscan(X, eps, 10, dist=dist, n_proj=256, topK=5, topM=20, ker=ker, sigma=0.5,
                                             seed=3, threads=4)
+    np.testing.assert_array_equal(core, r.core())
+    np.testing.assert_array_equal(labels, r.labels_)
+    assert ncl == r.n_clusters_
+
+
+@pytest.mark.parametrize("dist,eps,ker", [("Cosine", 0.016, 1024), ("Chi2", 0.03, 1024)])
+def test_multithreaded_soptics_core_distances(port, dist, eps, ker):
+    """fit_sOptics with 4 threads: core flags and core distances do not
+    depend on the order in which threads fill the neighbour lists
+    (src/sDbscan.cpp:1428-1446), so they equal the oracle's; the ordering is a
+    permutation of the points (its tie order is thread-dependent)."""
+    X = _data(dist, 2500)
+    n, d = X.shape
+    r = Ref(n, d)
+    r.set_params(n_proj=256, topK=5, topM=20, distance=dist, ker_n_features=ker, n_threads=4, random_seed=5)
+    r.fit_sOptics(X, eps, 10)
+    order, reach, core, cd, _ = port.fit_soptics(X, eps, 10, dist=dist, n_proj=256, topK=5, topM=20, ker=ker,
+                                                 seed=5, threads=4)
+    np.testing.assert_array_equal(core, r.core())
+    np.testing.assert_array_equal(cd, r.core_dist())
+    assert sorted(r.ordering_.tolist()) == list(range(n))
+    np.testing.assert_array_equal(np.sort(order), np.arange(n))
+
+
+@pytest.mark.parametrize("dist,prob,eps", [("Cosine", 0.05, 0.15), ("L2", 0.1, 0.6), ("Cosine", 1.0, 0.1)])
+def test_multithreaded_sngdbscan(port, dist, prob, eps):
+    """fit_sngDbscan with 4 threads and a fixed seed (every point draws the
+    same sequence, src/sDbscan.cpp:437-455): labels, n_clusters_ and core flags
+    equal the oracle's point-by-point restatement."""
+    X = _data(dist, 2000)
+    n, d = X.shape
+    r = Ref(n, d)
+    r.set_sngParams(distance=dist, samplingProb=prob, n_threads=4, random_seed=11)
+    r.fit_sngDbscan(X, eps, 10)
+    labels, ncl, core, _, _ = port.fit_sngdbscan(X, eps, 10, dist=dist, samplingProb=prob, seed=11, threads=4)
     np.testing.assert_array_equal(core, r.core())
     np.testing.assert_array_equal(labels, r.labels_)
     assert ncl == r.n_clusters_
