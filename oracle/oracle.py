@@ -227,6 +227,42 @@ class Port:
             raise ValueError(f"transform rejected the input (code {-r})")
         return ordering, reach, core, cd, deg, times
 
+    def fit_sngdbscan_blocks(self, X, eps, minPts, *, dist="Cosine", samplingProb=0.01, seed=42, block_rows=32,
+                             threads=-1):
+        """sngDbscan under the block-sampled rule (each block of block_rows
+        points draws its own sample; block_rows = 1 is the reference's
+        independent per-point sampling in law).  Returns (labels, n_clusters,
+        core, degree)."""
+        X = np.ascontiguousarray(X, np.float32)
+        n, d = X.shape
+        labels = np.zeros(n, np.int32)
+        core = np.zeros(n, np.uint8)
+        deg = np.zeros(n, np.int32)
+        ncl = self.L.orc_fit_sngdbscan_blocks(_p(X), _i(n), _i(d), _i(DIST_CODES[dist]), _f(samplingProb),
+                                              ctypes.c_uint32(seed & 0xFFFFFFFF), _i(block_rows), _f(eps),
+                                              _i(minPts), _i(threads), _p(labels), _p(core), _p(deg))
+        if ncl < 0:
+            raise ValueError(f"rejected (code {-ncl})")
+        return labels, ncl, core, deg
+
+    def fit_sngoptics_blocks(self, X, eps, minPts, *, dist="Cosine", samplingProb=0.01, seed=42, block_rows=32,
+                             threads=-1):
+        """sngOptics under the block-sampled rule.  Returns (ordering,
+        reachability, core, core_dist, degree)."""
+        X = np.ascontiguousarray(X, np.float32)
+        n, d = X.shape
+        ordering = np.zeros(n, np.int32)
+        reach = np.zeros(n, np.float32)
+        core = np.zeros(n, np.uint8)
+        cd = np.zeros(n, np.float32)
+        deg = np.zeros(n, np.int32)
+        r = self.L.orc_fit_sngoptics_blocks(_p(X), _i(n), _i(d), _i(DIST_CODES[dist]), _f(samplingProb),
+                                            ctypes.c_uint32(seed & 0xFFFFFFFF), _i(block_rows), _f(eps), _i(minPts),
+                                            _i(threads), _p(ordering), _p(reach), _p(core), _p(cd), _p(deg))
+        if r < 0:
+            raise ValueError(f"rejected (code {-r})")
+        return ordering, reach, core, cd, deg
+
     def fit_sdbscan_sweep(self, X, eps_list, minPts, *, dist="Cosine", n_proj=1024, topK=10, topM=50, ker=1024,
                           sigma=1.0, L=0.4, seed=42, threads=-1):
         """The reference's index-once sweep restated (test_sDbscan, src/sDbscan.cpp:980-1039)."""

@@ -793,6 +793,135 @@ int orc_fit_sngoptics(const float* X, int n, int d, int code, float samplingProb
     return 0;
 }
 
+// ---- block-sampled sngDbscan / sngOptics --------------------------------------
+// The reference's unreproducible samples (sngOptics: std::random_device per
+// point, src/sDbscan.cpp:1500-1502; sngDbscan with random_seed < 0: a clock
+// seed per point, :437-440) are independent per point.  This rule keeps their
+// statistics in a form a GPU can tile: the points are cut into blocks of
+// blockRows consecutive indices, and block b draws its own S columns,
+// draw j being q = floor(hi32(splitmix64(key + b S + j)) n / 2^32) with
+// key = splitmix64(seed) (splitmix64: Steele, Lea and Flood, OOPSLA 2014).
+// Every point of block b pairs with each of the block's draws that is not
+// itself (no replacement draw), and each pair within eps is pushed into both
+// lists, as the reference's loops do.  S = ceil(1.0 n samplingProb) for
+// sngDbscan (:449) and ceil(samplingProb n) in float for sngOptics (:1490).
+// blockRows = 1 is the reference's independent sampling exactly in law.
+static inline uint64_t splitmix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static inline int block_draw(uint64_t key, int64_t S, int64_t b, int64_t j, int n) {
+    const uint64_t z = splitmix64(key + (uint64_t)(b * S + j));
+    return (int)(((z >> 32) * (uint64_t)n) >> 32);
+}
+
+// The pairs within eps of every block: found[p] holds (q, dist) for p's own
+// draws.  Returns S.
+static int64_t block_pairs(const float* Y, int n, int d, int code, int64_t S, uint32_t seed, int blockRows, float eps,
+                           std::vector<std::vector<std::pair<int, float>>>& found) {
+    const uint64_t key = splitmix64(seed);
+    const int64_t nb = (n + blockRows - 1) / blockRows;
+    found.assign(n, {});
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t b = 0; b < nb; ++b) {
+        std::vector<int> cols(S);
+        for (int64_t j = 0; j < S; ++j) cols[j] = block_draw(key, S, b, j, n);
+        const int p1 = (int)std::min<int64_t>(n, (b + 1) * blockRows);
+        for (int p = (int)(b * blockRows); p < p1; ++p)
+            for (int q : cols) {
+                if (q == p) continue;
+                const float dd = distance(Y + (size_t)p * d, Y + (size_t)q * d, d, code);
+                if (dd <= eps) found[p].push_back({q, dd});
+            }
+    }
+    return S;
+}
+
+// sngDbscan under the block rule: neighbourhood sizes with repeats counted,
+// core >= minPts - 1, formCluster over the symmetric lists of the cores.
+// samplingProb >= 1 is the exact mode (:466-479), identical to
+// orc_fit_sngdbscan's.  Returns n_clusters_ or a negative transform error.
+int orc_fit_sngdbscan_blocks(const float* X, int n, int d, int code, float samplingProb, uint32_t seed, int blockRows,
+                             float eps, int minPts, int threads, int32_t* labels, uint8_t* core, int32_t* degree) {
+    if (threads > 0) omp_set_num_threads(threads);
+    if (blockRows < 1) return -100;
+    std::vector<float> Xc(X, X + (size_t)n * d);
+    int err = orc_transform(Xc.data(), n, d, code);
+    if (err) return -err;
+    const float* Y = Xc.data();
+    std::vector<std::vector<int>> nb(n);
+    if (samplingProb < 1.0) {
+        std::vector<std::vector<std::pair<int, float>>> found;
+        block_pairs(Y, n, d, code, (int64_t)std::ceil(1.0 * n * samplingProb), seed, blockRows, eps, found);
+        for (int p = 0; p < n; ++p)
+            for (const auto& e : found[p]) {
+                nb[p].push_back(e.first);
+                nb[e.first].push_back(p);
+            }
+    } else {
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int p = 0; p < n; ++p)
+            for (int q = 0; q < n; ++q)
+                if (q != p && distance(Y + (size_t)p * d, Y + (size_t)q * d, d, code) <= eps) nb[p].push_back(q);
+    }
+    for (int p = 0; p < n; ++p) {
+        degree[p] = (int32_t)nb[p].size();
+        core[p] = degree[p] >= minPts - 1 ? 1 : 0;
+        if (!core[p]) nb[p].clear();
+    }
+    std::vector<int64_t> off(n + 1, 0);
+    for (int p = 0; p < n; ++p) off[p + 1] = off[p] + (int64_t)nb[p].size();
+    std::vector<int32_t> idx(off[n]);
+    for (int p = 0; p < n; ++p) std::copy(nb[p].begin(), nb[p].end(), idx.begin() + off[p]);
+    return orc_form_cluster(n, core, off.data(), idx.data(), labels);
+}
+
+// sngOptics under the block rule: de-duplicated lists with distances
+// (:1537-1541), core distance the (minPts-1)-th smallest (:1543-1555), then
+// formOptics_scikit with (reachability, id) ties.  Returns 0 or a negative
+// transform error.
+int orc_fit_sngoptics_blocks(const float* X, int n, int d, int code, float samplingProb, uint32_t seed, int blockRows,
+                             float eps, int minPts, int threads, int32_t* ordering, float* reach, uint8_t* core,
+                             float* coreDist, int32_t* degree) {
+    if (threads > 0) omp_set_num_threads(threads);
+    if (blockRows < 1 || minPts < 2) return -100;
+    std::vector<float> Xc(X, X + (size_t)n * d);
+    int err = orc_transform(Xc.data(), n, d, code);
+    if (err) return -err;
+    std::vector<std::vector<std::pair<int, float>>> found;
+    block_pairs(Xc.data(), n, d, code, (int64_t)std::ceil(samplingProb * (float)n), seed, blockRows, eps, found);
+    std::vector<std::map<int, float>> lists(n);
+    for (int p = 0; p < n; ++p)
+        for (const auto& e : found[p]) {
+            lists[p].emplace(e.first, e.second);
+            lists[e.first].emplace(p, e.second);
+        }
+    std::vector<int64_t> off(n + 1, 0);
+    for (int p = 0; p < n; ++p) off[p + 1] = off[p] + (int64_t)lists[p].size();
+    std::vector<int32_t> idx(off[n]);
+    std::vector<float> dist(off[n]);
+    for (int p = 0; p < n; ++p) {
+        int64_t o = off[p];
+        for (const auto& e : lists[p]) {
+            idx[o] = e.first;
+            dist[o++] = e.second;
+        }
+        degree[p] = (int32_t)lists[p].size();
+        core[p] = degree[p] >= minPts - 1 ? 1 : 0;
+        coreDist[p] = 0.0f;
+        if (core[p]) {
+            std::vector<float> v(dist.begin() + off[p], dist.begin() + off[p + 1]);
+            std::nth_element(v.begin(), v.begin() + (minPts - 2), v.end());
+            coreDist[p] = v[minPts - 2];
+        }
+    }
+    orc_form_optics(n, core, coreDist, off.data(), idx.data(), dist.data(), 1, ordering, reach);
+    return 0;
+}
+
 // Distance of one pair, exposed for tests of the numerical contract.
 float orc_distance(const float* x, const float* y, int d, int code) { return distance(x, y, d, code); }
 

@@ -7,7 +7,9 @@ tests/golden/make_golden.py).  The oracle restates sng_findCorePoints point by
 point and must reproduce labels, n_clusters_, core flags and the core points'
 neighbourhood sizes (repeats counted) exactly.  sngOptics seeds each point
 from std::random_device in the reference, so its restatement (the engine's
-shared seeded sample) is checked for its own invariants here.
+shared seeded sample) is checked for its own invariants here.  The
+block-sampled rule (each block of consecutive points draws its own sample) is
+checked against the reference's unreproducible runs in law: core counts.
 """
 import glob
 import json
@@ -60,3 +62,66 @@ def test_oracle_sngoptics_invariants(port):
     assert np.all(cd[c == 1] <= eps) and np.all(cd[c == 1] >= 0) and np.all(cd[c == 0] == 0)
     reached = r != np.float32(-2147483648.0)
     assert reached.sum() > 0 and np.all(r[reached] >= 0)
+
+
+def _mnist_like():
+    from sdbscan_gb300 import datasets
+    return datasets.cfg2_mnist_like(4000, 64, seed=41)[0]
+
+
+def test_block_rule_is_deterministic_and_exact_mode_unchanged(port):
+    """The block-sampled rule is a function of the seed; at samplingProb >= 1
+    it is the reference's exact DBSCAN, the point-by-point oracle's result."""
+    X = _mnist_like()[:1500]
+    a = port.fit_sngdbscan_blocks(X, 0.2, 10, samplingProb=0.05, seed=9, block_rows=32, threads=4)
+    b = port.fit_sngdbscan_blocks(X, 0.2, 10, samplingProb=0.05, seed=9, block_rows=32, threads=2)
+    for u, v in zip(a, b):
+        np.testing.assert_array_equal(u, v)
+    c = port.fit_sngdbscan_blocks(X, 0.2, 10, samplingProb=0.05, seed=10, block_rows=32, threads=4)
+    assert not np.array_equal(a[3], c[3])
+    e1 = port.fit_sngdbscan_blocks(X, 0.15, 10, samplingProb=1.0, seed=9, block_rows=32, threads=4)
+    l2, n2, c2, d2, _ = port.fit_sngdbscan(X, 0.15, 10, samplingProb=1.0, seed=9, threads=4)
+    np.testing.assert_array_equal(e1[0], l2)
+    np.testing.assert_array_equal(e1[3], d2)
+    o1 = port.fit_sngoptics_blocks(X, 0.2, 10, samplingProb=0.05, seed=9, block_rows=32, threads=4)
+    o2 = port.fit_sngoptics_blocks(X, 0.2, 10, samplingProb=0.05, seed=9, block_rows=32, threads=1)
+    for u, v in zip(o1, o2):
+        np.testing.assert_array_equal(u, v)
+    assert sorted(o1[0].tolist()) == list(range(X.shape[0]))
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__file__), "..", "oracle", "_ref",
+                                                    "libsdbscan_ref.so")), reason="reference library not built here")
+def test_block_rule_keeps_the_reference_statistics(port):
+    """The reference's sngOptics (std::random_device per point) and its
+    unseeded sngDbscan (a clock seed per point) sample independently per
+    point.  Three runs of each against three seeds of the rules: the
+    block-sampled rule (32-point blocks) finds the reference's number of core
+    points within 2 %; one sample shared by all points finds at least 5 %
+    fewer (the deviation the block rule removes)."""
+    from oracle.oracle import Ref
+    X = _mnist_like()
+    n, d = X.shape
+    eps, minPts, prob = 0.2, 10, 0.05
+
+    def ref_cores(optics):
+        out = []
+        for _ in range(3):
+            r = Ref(n, d)
+            r.set_sngParams(distance="Cosine", samplingProb=prob, n_threads=4, random_seed=-1)
+            (r.fit_sngOptics if optics else r.fit_sngDbscan)(X, eps, minPts)
+            out.append(int(r.core().sum()))
+        return float(np.mean(out))
+
+    ref_o, ref_d = ref_cores(True), ref_cores(False)
+    blk_o = np.mean([port.fit_sngoptics_blocks(X, eps, minPts, samplingProb=prob, seed=s, block_rows=32,
+                                               threads=4)[2].sum() for s in range(3)])
+    blk_d = np.mean([port.fit_sngdbscan_blocks(X, eps, minPts, samplingProb=prob, seed=s, block_rows=32,
+                                               threads=4)[2].sum() for s in range(3)])
+    shr_o = np.mean([port.fit_sngoptics(X, eps, minPts, samplingProb=prob, seed=s, threads=4)[2].sum()
+                     for s in range(3)])
+    shr_d = np.mean([port.fit_sngdbscan(X, eps, minPts, samplingProb=prob, seed=s, threads=4)[2].sum()
+                     for s in range(3)])
+    assert abs(blk_o - ref_o) < 0.02 * ref_o, (blk_o, ref_o)
+    assert abs(blk_d - ref_d) < 0.02 * ref_d, (blk_d, ref_d)
+    assert shr_o < 0.95 * ref_o and shr_d < 0.95 * ref_d, (shr_o, shr_d, ref_o, ref_d)
