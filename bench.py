@@ -171,7 +171,16 @@ class ClockSampler:
     def summary(self):
         if not self.proc or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
-        rows = [r.split(", ") for r in open(self.path).read().strip().splitlines() if r.count(",") >= 8]
+        text = open(self.path).read()
+        if "SDB_CLOCKS_DIR" not in os.environ:
+            os.remove(self.path)  # kept only where asked for
+        return self.parse(text)
+
+    @staticmethod
+    def parse(text):
+        """Median SM clock, the maximum clock and the throttle reasons seen in
+        nvidia-smi's CSV rows (FIELDS order, no header, no units)."""
+        rows = [r.split(", ") for r in text.strip().splitlines() if r.count(",") >= 8]
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
