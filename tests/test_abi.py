@@ -94,3 +94,58 @@ def test_dropin_module_has_every_reference_name():
         pytest.skip(f"drop-in module not built here: {e}")
     missing = [n for n in REFERENCE_MODULE_NAMES if not hasattr(mod.sDbscan, n)]
     assert not missing, missing
+
+
+# Keyword names and defaults of the reference binding (python/python_wrapper.cpp:15-51).
+REFERENCE_SIGNATURES = {
+    "set_params": [("n_proj", "1024"), ("topK", "10"), ("topM", "50"), ("distance", "'Cosine'"),
+                   ("ker_n_features", "1024"), ("ker_sigma", "1.0"), ("ker_intervalSampling", "0.4"),
+                   ("clusterNoise", "0"), ("samplingProb", "0.01"), ("verbose", "False"), ("output", "''"),
+                   ("n_threads", "-1"), ("random_seed", "-1")],
+    "set_sngParams": [("distance", "'Cosine'"), ("samplingProb", "0.01"), ("clusterNoise", "0"),
+                      ("verbose", "False"), ("output", "''"), ("n_threads", "-1"), ("random_seed", "-1")],
+    "set_kernel_params": [("distance", "'L2'"), ("ker_n_features", "1024"), ("ker_sigma", "1.0"),
+                          ("ker_intervalSampling", "0.4")],
+    "set_topM": [("topM", None)], "set_topK": [("topK", None)], "set_threads": [("n_threads", None)],
+    "set_clusterNoise": [("clusterNoise", None)],
+    "fit_sDbscan": [("X", None), ("eps", None), ("minPts", None)],
+    "fit_sOptics": [("X", None), ("eps", None), ("minPts", None)],
+    "fit_sngDbscan": [("X", None), ("eps", None), ("minPts", None)],
+    "fit_sngOptics": [("X", None), ("eps", None), ("minPts", None)],
+    "load_fit_sDbscan": [("dataset", None), ("eps", None), ("minPts", None)],
+    "load_fit_sOptics": [("dataset", None), ("eps", None), ("minPts", None)],
+    "load_fit_sngOptics": [("dataset", None), ("eps", None), ("minPts", None)],
+    "test_sDbscan": [("X", None), ("eps", None), ("rangeEps", None), ("n_tests", None), ("minPts", None)],
+    "test_sngDbscan": [("X", None), ("eps", None), ("rangeEps", None), ("n_tests", None), ("minPts", None)],
+    "load_test_sDbscan": [("dataset", None), ("eps", None), ("rangeEps", None), ("n_tests", None), ("minPts", None)],
+    "load_test_sngDbscan": [("dataset", None), ("eps", None), ("rangeEps", None), ("n_tests", None),
+                            ("minPts", None)],
+}
+
+
+def _doc_params(doc):
+    """(name, default) pairs of a pybind11 signature line, self dropped."""
+    import re
+    sig = doc.strip().splitlines()[0]
+    body = sig[sig.index("(") + 1: sig.rindex(")")]
+    while "[" in body:  # drop bracketed type arguments (they hold commas)
+        body = re.sub(r"\[[^\[\]]*\]", "", body)
+    out = []
+    for part in body.split(", "):
+        name = part.split(":")[0].strip()
+        default = part.split(" = ", 1)[1].strip() if " = " in part else None
+        if name != "self":
+            out.append((name, default))
+    return out
+
+
+def test_dropin_keywords_and_defaults_match_reference():
+    import importlib
+    try:
+        mod = importlib.import_module("sdbscan_gb300.sDbscan")
+    except ImportError as e:
+        pytest.skip(f"drop-in module not built here: {e}")
+    for name, want in REFERENCE_SIGNATURES.items():
+        assert _doc_params(getattr(mod.sDbscan, name).__doc__) == want, name
+    init = _doc_params(mod.sDbscan.__init__.__doc__)
+    assert [n for n, _ in init[:2]] == ["n_points", "n_features"]  # python_wrapper.cpp:16
