@@ -149,3 +149,22 @@ def test_dropin_keywords_and_defaults_match_reference():
         assert _doc_params(getattr(mod.sDbscan, name).__doc__) == want, name
     init = _doc_params(mod.sDbscan.__init__.__doc__)
     assert [n for n, _ in init[:2]] == ["n_points", "n_features"]  # python_wrapper.cpp:16
+
+
+def test_no_cpu_fallback_without_a_gpu():
+    """Without a usable CUDA device the engine refuses to start: the C ABI
+    returns SDB_ERR_CUDA and both bindings raise; nothing computes on the CPU."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from sdbscan_gb300 import capi
+    with pytest.raises(capi.SdbError) as e:
+        capi.Engine(10, 4)
+    assert e.value.status == 2
+    import importlib
+    try:
+        mod = importlib.import_module("sdbscan_gb300.sDbscan")
+    except ImportError as err:
+        pytest.skip(f"drop-in module not built here: {err}")
+    with pytest.raises(RuntimeError):
+        mod.sDbscan(10, 4)
