@@ -81,6 +81,14 @@ class Port:
         L.orc_fit_sngoptics.restype = _i
         L.orc_distance.restype = _f
 
+    def set_timing_mode(self, on: bool) -> None:
+        """Cosine / L1 / L2 distances with vectorisable partial sums, at the
+        speed of the reference's Eigen build, for the CPU baseline's timed
+        legs only (the last bits leave the numerical contract).  The setting
+        belongs to the loaded library, so it holds for every Port of the
+        process until it is switched off."""
+        self.L.orc_set_timing_mode(_i(1 if on else 0))
+
     # RNG -------------------------------------------------------------------
     def hd3_bits(self, nbits: int, seed: int) -> np.ndarray:
         out = np.zeros(nbits, np.uint8)

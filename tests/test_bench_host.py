@@ -28,3 +28,24 @@ def test_clock_summary_flags_thermal_and_empty_input():
     s = bench.ClockSampler.parse(na)
     assert s["sm_mhz"] is None and s["sm_max_mhz"] is None and s["reasons"] == []
     assert bench.ClockSampler.parse("")["reasons"] == ["no samples"]
+
+
+def test_cpu_baseline_timing_mode_is_scoped(port):
+    """The CPU baseline's timing mode (vectorised Cosine / L1 / L2 partial
+    sums, the reference's Eigen speed) moves a distance by rounding only, is
+    off by default, and leaves the numerical contract intact once off."""
+    import numpy as np
+    rng = np.random.default_rng(3)
+    x, y = rng.random(784, dtype=np.float32), rng.random(784, dtype=np.float32)
+    x /= np.linalg.norm(x)
+    y /= np.linalg.norm(y)
+    exact = {k: port.distance(x, y, k) for k in ("Cosine", "L1", "L2", "Chi2")}
+    port.set_timing_mode(True)
+    try:
+        fast = {k: port.distance(x, y, k) for k in exact}
+    finally:
+        port.set_timing_mode(False)
+    for k in ("Cosine", "L1", "L2"):
+        assert abs(fast[k] - exact[k]) <= 2e-6 * max(1.0, abs(exact[k])), (k, fast[k], exact[k])
+    assert fast["Chi2"] == exact["Chi2"]  # a scalar loop in the reference too
+    assert {k: port.distance(x, y, k) for k in exact} == exact
