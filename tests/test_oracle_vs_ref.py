@@ -68,3 +68,42 @@ def test_multithreaded_sngdbscan(port, dist, prob, eps):
     np.testing.assert_array_equal(core, r.core())
     np.testing.assert_array_equal(labels, r.labels_)
     assert ncl == r.n_clusters_
+
+
+def test_noise_labelling_with_partial_core_sampling_same_law(port):
+    """sDbscan-1NN with fewer sampled cores than cores (src/sDbscan.cpp:683-706):
+    the reference keeps each core with probability fProb through the unseeded
+    rand(); the engine's rule keeps it iff a hash of (seed, point) falls below
+    fProb.  Same law: no point stays noise, and the labels given to the former
+    noise points agree between a reference run and a run of the rule as often
+    as two reference runs agree with each other."""
+    from oracle.oracle import fht_dim
+    X = ds.cfg1_cosine(3000, 48, seed=21)[0]
+    n, d = X.shape
+    eps, prob = 0.15, 0.02
+    refs = []
+    for _ in range(4):
+        r = Ref(n, d)
+        r.set_params(n_proj=256, topK=5, topM=20, distance="Cosine", clusterNoise=1, samplingProb=prob,
+                     n_threads=4, random_seed=3)
+        r.fit_sDbscan(X, eps, 10)
+        refs.append(r.labels_.copy())
+    base, _, core, _ = port.fit_sdbscan(X, eps, 10, n_proj=256, topK=5, topM=20, seed=3, threads=4)
+    noise = base == -1
+    assert 50 < noise.sum() < 500
+    Xt, _ = port.transform(X, "Cosine")
+    fd = fht_dim(256, d)
+    P = port.project(Xt, "Cosine", d, 0.4, None, port.hd3_bits(3 * fd, 3), fd, 256)
+    topK = port.topk(P, 5)
+    ours = [port.label_noise(P, topK, core, base, prob, 1000 + s) for s in range(4)]
+    for lab in refs + ours:
+        assert (lab != -1).all()
+        np.testing.assert_array_equal(lab[~noise], base[~noise])
+
+    def agree(a, b):
+        return float(np.mean(a[noise] == b[noise]))
+
+    rr = np.mean([agree(refs[i], refs[j]) for i in range(4) for j in range(i + 1, 4)])
+    oo = np.mean([agree(ours[i], ours[j]) for i in range(4) for j in range(i + 1, 4)])
+    ro = np.mean([agree(a, b) for a in refs for b in ours])
+    assert abs(ro - rr) < 0.1 and abs(oo - rr) < 0.1, (rr, oo, ro)
