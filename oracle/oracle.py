@@ -366,6 +366,12 @@ class Ref:
         X = np.ascontiguousarray(X, np.float32)
         self.L.ref_fit_soptics(self.h, _p(X), _i(self.n), _i(self.d), _f(eps), _i(minPts))
 
+    def test_sDbscan(self, X, eps, rangeEps, n_tests, minPts, prefix):
+        """The reference's index-once sweep; writes one labels file per eps."""
+        X = np.ascontiguousarray(X, np.float32)
+        self.L.ref_test_sdbscan(self.h, _p(X), _i(self.n), _i(self.d), _f(eps), _f(rangeEps), _i(n_tests),
+                                _i(minPts), str(prefix).encode())
+
     def set_sngParams(self, distance="Cosine", samplingProb=0.01, clusterNoise=0, verbose=False, n_threads=1,
                       random_seed=42):
         self.L.ref_set_sng_params(self.h, distance.encode(), _f(samplingProb), _i(clusterNoise),

@@ -34,6 +34,7 @@ public:
     int nPoints() const { return n_points; }
     const string& dist() const { return distance; }
     float kerSam() const { return ker_intervalSampling; }
+    void setOutput(const char* prefix) { output = prefix; }
 
     // Projection of every (already transformed) point exactly as
     // src/sDbscan.cpp:53-91 forms MATRIX_FHT, using the fitted bitHD3 / matrix_R
@@ -103,6 +104,14 @@ void ref_fit_sngdbscan(void* h, const float* X, int n, int d, float eps, int min
 void ref_fit_sngoptics(void* h, const float* X, int n, int d, float eps, int minPts) {
     Ref<const MatrixXf> ref(X, d, n);
     P(h)->fit_sngOptics(ref, eps, minPts);
+}
+// test_sDbscan (src/sDbscan.cpp:980-1039): index once, then one labels file
+// per eps = eps + i * rangeEps, named from the output prefix.
+void ref_test_sdbscan(void* h, const float* X, int n, int d, float eps, float rangeEps, int nTests, int minPts,
+                      const char* prefix) {
+    Ref<const MatrixXf> ref(X, d, n);
+    P(h)->setOutput(prefix);
+    P(h)->test_sDbscan(ref, eps, rangeEps, nTests, minPts);
 }
 void ref_clear(void* h) { P(h)->clear(); }
 

@@ -107,3 +107,24 @@ def test_noise_labelling_with_partial_core_sampling_same_law(port):
     oo = np.mean([agree(ours[i], ours[j]) for i in range(4) for j in range(i + 1, 4)])
     ro = np.mean([agree(a, b) for a in refs for b in ours])
     assert abs(ro - rr) < 0.1 and abs(oo - rr) < 0.1, (rr, oo, ro)
+
+
+def test_reference_sweep_files_equal_oracle_sweep(port, tmp_path):
+    """The reference's own test_sDbscan (src/sDbscan.cpp:980-1039): index once,
+    then for eps + i * rangeEps (computed in double, stored as float) one labels
+    file named <output>_<dist>_Eps_<round(1000 eps)>_MinPts_.._KerFeatures_..
+    _NumProj_.._TopM_.._TopK_..; every file equals the oracle's sweep."""
+    X = ds.cfg2_mnist_like(2500, 64, seed=41)[0]
+    n, d = X.shape
+    eps0, step, nt, minPts = 0.06, 0.03, 4, 10
+    r = Ref(n, d)
+    r.set_params(n_proj=256, topK=5, topM=20, distance="Cosine", n_threads=4, random_seed=6)
+    prefix = tmp_path / "ref"
+    r.test_sDbscan(X, eps0, step, nt, minPts, prefix)
+    eps = [np.float32(np.float64(np.float32(eps0)) + 1.0 * i * np.float64(np.float32(step))) for i in range(nt)]
+    labels, ncl, _ = port.fit_sdbscan_sweep(X, eps, minPts, n_proj=256, topK=5, topM=20, seed=6, threads=4)
+    for i, e in enumerate(eps):
+        f = (f"{prefix}_Cosine_Eps_{int(round(1000 * float(e)))}_MinPts_{minPts}_KerFeatures_{d}"
+             f"_NumProj_256_TopM_20_TopK_5")
+        np.testing.assert_array_equal(np.loadtxt(f, dtype=np.int32), labels[i])
+    assert len(set(map(int, ncl))) > 1  # the eps values give different clusterings
