@@ -103,12 +103,13 @@ def cfg3_aniso_l2(n: int = 1_000_000, d: int = 256, n_comp: int = 50, scale: flo
 
 
 def cfg4_dirichlet(n: int = 500_000, d: int = 512, n_comp: int = 30, alpha: float = 0.1, conc: float = 200.0,
-                   seed: int = 4007, chunk: int = 1 << 16) -> tuple[np.ndarray, np.ndarray]:
+                   seed: int = 4007, chunk: int = 1 << 16, zero_below: float = 1e-9) -> tuple[np.ndarray, np.ndarray]:
     """Config 4: nonnegative histograms.  30 prototypes ~ Dirichlet(alpha=0.1);
-    a point ~ Dirichlet(conc * prototype + alpha/10).  Entries below 1e-9 (less
-    than one count in a billion) are set to 0 and the row renormalised: the
-    Dirichlet's tiny shape parameters otherwise give entries near 1e-30 whose
-    pairwise products fall into float32's subnormal range."""
+    a point ~ Dirichlet(conc * prototype + alpha/10).  Entries below
+    zero_below (1e-9: less than one count in a billion) are set to 0 and the
+    row renormalised: the Dirichlet's tiny shape parameters otherwise give
+    entries near 1e-30 whose pairwise products fall into float32's subnormal
+    range.  zero_below = 0 keeps the raw law (tiny entries included)."""
     rng = np.random.default_rng(seed)
     protos = rng.dirichlet(np.full(d, alpha), n_comp)
     y = rng.integers(0, n_comp, n).astype(np.int32)
@@ -118,8 +119,9 @@ def cfg4_dirichlet(n: int = 500_000, d: int = 512, n_comp: int = 30, alpha: floa
         a = conc * protos[y[s:e]] + alpha / 10.0
         g = rng.standard_gamma(a)
         g /= g.sum(axis=1, keepdims=True)
-        g[g < 1e-9] = 0.0
-        g /= g.sum(axis=1, keepdims=True)
+        if zero_below > 0:
+            g[g < zero_below] = 0.0
+            g /= g.sum(axis=1, keepdims=True)
         X[s:e] = g.astype(np.float32)
     return X, y
 

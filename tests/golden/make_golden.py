@@ -36,7 +36,8 @@ def cases():
     X3, _ = ds.cfg2_mnist_like(2000, 196, seed=13)
     yield "cosine_mnistlike_2000x196", X3, dict(n_proj=256, topK=10, topM=30, distance="Cosine"), 0.25, 20, False
     yield "cosine_optics_2000x32", X1, dict(n_proj=256, topK=5, topM=20, distance="Cosine"), 0.2, 10, True
-    X4, _ = ds.cfg4_dirichlet(1500, 64, n_comp=5, seed=14)
+    # the raw Dirichlet law: entries down to ~1e-30, products in float32's subnormal range
+    X4, _ = ds.cfg4_dirichlet(1500, 64, n_comp=5, seed=14, zero_below=0.0)
     yield "chi2_ker512_1500x64", X4, dict(n_proj=256, topK=5, topM=20, distance="Chi2", ker_n_features=512), 0.3, 10, False
     yield "chi2_optics_ker1024_1500x64", X4, dict(n_proj=1024, topK=5, topM=20, distance="Chi2",
                                                    ker_n_features=1024), 0.3, 10, True
@@ -66,7 +67,8 @@ def cases():
     # rotation vectors longer than 2048 (the shared-memory projection path)
     X11, _ = ds.cfg1_cosine(600, 2100, seed=25)
     yield "cosine_d2100_fht4096_600", X11, dict(n_proj=256, topK=5, topM=20, distance="Cosine"), 0.15, 8, False
-    yield "chi2_ker4096_1500x64", X4, dict(n_proj=256, topK=5, topM=20, distance="Chi2", ker_n_features=4096), \
+    X4z, _ = ds.cfg4_dirichlet(1500, 64, n_comp=5, seed=14)  # entries below 1e-9 zeroed
+    yield "chi2_ker4096_1500x64", X4z, dict(n_proj=256, topK=5, topM=20, distance="Chi2", ker_n_features=4096), \
         0.3, 10, False
     X10, _ = ds.cfg4_dirichlet(1500, 64, n_comp=5, conc=10, seed=24)  # wider histograms: a third left as noise
     yield "chi2_noise1nn_1500x64", X10, dict(n_proj=256, topK=5, topM=20, distance="Chi2", ker_n_features=512,
@@ -88,7 +90,7 @@ def sng_cases():
     yield "sng_chi2_1500x64", X10, "Chi2", 0.2, 0.2, 15
 
 
-def main_sng(only=()):
+def main_sng(only=(), out_dir=HERE):
     for name, X, dist, prob, eps, minPts in sng_cases():
         if only and name not in only:
             continue
@@ -101,15 +103,15 @@ def main_sng(only=()):
                    core_degree=np.diff(off).astype(np.int32))
         meta = dict(distance=dist, samplingProb=prob, eps=eps, minPts=minPts, random_seed=7, n_threads=1)
         out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
-        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), **out)
         print(name, "n_clusters", r.n_clusters_, "cores", int(out["core"].sum()))
 
 
-def main(only=()):
-    """Writes every fixture, or only the named ones."""
+def main(only=(), out_dir=HERE):
+    """Writes every fixture, or only the named ones, into out_dir."""
     if build_ref() is None:
         sys.exit("the reference sources are not available here; fixtures cannot be regenerated")
-    main_sng(only)
+    main_sng(only, out_dir)
     for name, X, params, eps, minPts, optics in cases():
         if only and name not in only:
             continue
@@ -132,7 +134,7 @@ def main(only=()):
                        core_degree=np.diff(off).astype(np.int32))
         meta = dict(params, eps=eps, minPts=minPts, optics=optics, random_seed=7, n_threads=1)
         out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
-        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), **out)
         print(name, "n_clusters" if not optics else "ordering", r.n_clusters_ if not optics else len(r.ordering_),
               "cores", int(out["core"].sum()))
 

@@ -128,3 +128,25 @@ def test_reference_sweep_files_equal_oracle_sweep(port, tmp_path):
              f"_NumProj_256_TopM_20_TopK_5")
         np.testing.assert_array_equal(np.loadtxt(f, dtype=np.int32), labels[i])
     assert len(set(map(int, ncl))) > 1  # the eps values give different clusterings
+
+
+_FIXTURES = sorted(os.path.basename(p)[:-4] for p in
+                   __import__("glob").glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+@pytest.mark.parametrize("name", _FIXTURES)
+def test_golden_fixture_regenerates_bit_identically(name, tmp_path):
+    """tests/golden/make_golden.py, run again with the reference, writes the
+    committed fixture bit for bit (the fixtures are reproducible from the
+    committed script)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(os.path.dirname(__file__), "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    mg.main((name,), str(tmp_path))
+    new = np.load(tmp_path / f"{name}.npz")
+    old = np.load(os.path.join(os.path.dirname(__file__), "golden", f"{name}.npz"))
+    assert sorted(new.files) == sorted(old.files)
+    for k in old.files:
+        np.testing.assert_array_equal(new[k], old[k], err_msg=k)
