@@ -35,7 +35,7 @@ typedef enum {
     SDB_ERR_NEGATIVE = 3,   /* Chi2/JS input has a negative value (src/Utilities.h:308-312) */
     SDB_ERR_ZERO_POINT = 4, /* a point with zero sum (Chi2/JS, :318-325) or zero norm (Cosine) */
     SDB_ERR_STATE = 5,      /* output requested before the matching fit            */
-    SDB_ERR_NOMEM = 6,      /* device allocation failed                            */
+    SDB_ERR_NOMEM = 6,      /* device or host allocation failed                    */
     SDB_ERR_INTERNAL = 7    /* internal consistency check failed                   */
 } sdb_status;
 

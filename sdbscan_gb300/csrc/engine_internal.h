@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -12,6 +13,22 @@
 struct DevBuf {
     void* ptr = nullptr;
     size_t bytes = 0;
+};
+
+// Host staging kept across fits: grow-only, and its contents are not
+// initialised (each use overwrites what it reads).  get() may throw
+// std::bad_alloc.
+template <typename T>
+struct HostBuf {
+    std::unique_ptr<T[]> p;
+    size_t cap = 0;
+    T* get(size_t count) {
+        if (count > cap) {
+            p.reset(new T[count]);
+            cap = count;
+        }
+        return p.get();
+    }
 };
 
 // Eps sweep of one fit (the reference's test_sDbscan pattern): the index and
@@ -61,6 +78,12 @@ struct sdb_engine {
     bool lastSng = false;  // the last fit was sngDbscan / sngOptics (no index state)
     std::vector<int32_t> hostOrdering;
     std::vector<float> hostReach;
+    // the sOPTICS neighbour lists, core distances and core flags downloaded
+    // for the host ordering
+    HostBuf<int64_t> stageOff;
+    HostBuf<int32_t> stageIdx;
+    HostBuf<float> stageDist, stageCd;
+    HostBuf<uint8_t> stageCore;
     int32_t* hostErr = nullptr;
     unsigned long long* hostCounters = nullptr;
     int launchCount = 0;

@@ -11,7 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <queue>
+#include <new>
 #include <vector>
 
 #include "common.cuh"
@@ -142,25 +142,36 @@ sdb_status sdb_engine::optics_stage(const CoreArgs& ca, int& launches) {
 
 // Downloads the CSR neighbour lists (nbOff / nbIdx / nbDist), core flags and
 // core distances of the last fit and runs the ordering on the host.
+// The staging buffers are kept across fits and not zero-filled: a fresh,
+// zeroed buffer per fit costs a memset and first-touch page faults over the
+// whole list (hundreds of MB at 500K points) before the copy overwrites it.
 sdb_status sdb_engine::optics_order(int64_t total) {
     cudaStream_t st = stream;
     cudaError_t e;
-    std::vector<int64_t> hOff(n + 1);
-    std::vector<int32_t> hIdx(total);
-    std::vector<float> hDist(total), hCd(n);
-    std::vector<uint8_t> hCore(n);
-    e = cudaMemcpyAsync(hOff.data(), nbOff.ptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, st);
+    int64_t* hOff = nullptr;
+    int32_t* hIdx = nullptr;
+    float *hDist = nullptr, *hCd = nullptr;
+    uint8_t* hCore = nullptr;
+    try {
+        hOff = stageOff.get((size_t)n + 1);
+        hIdx = stageIdx.get((size_t)std::max<int64_t>(total, 1));
+        hDist = stageDist.get((size_t)std::max<int64_t>(total, 1));
+        hCd = stageCd.get((size_t)n);
+        hCore = stageCore.get((size_t)n);
+        hostOrdering.assign(n, 0);
+        hostReach.assign(n, 0.0f);
+    } catch (const std::bad_alloc&) {
+        return fail(SDB_ERR_NOMEM, "host memory for the sOPTICS neighbour lists");
+    }
+    e = cudaMemcpyAsync(hOff, nbOff.ptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess && total)
-        e = cudaMemcpyAsync(hIdx.data(), nbIdx.ptr, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, st);
+        e = cudaMemcpyAsync(hIdx, nbIdx.ptr, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess && total)
-        e = cudaMemcpyAsync(hDist.data(), nbDist.ptr, sizeof(float) * total, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(hCd.data(), coreDist.ptr, sizeof(float) * n, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(hCore.data(), core.ptr, n, cudaMemcpyDeviceToHost, st);
+        e = cudaMemcpyAsync(hDist, nbDist.ptr, sizeof(float) * total, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hCd, coreDist.ptr, sizeof(float) * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hCore, core.ptr, n, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "neighbour list download");
-    hostOrdering.assign(n, 0);
-    hostReach.assign(n, 0.0f);
-    form_optics(n, hCore.data(), hCd.data(), hOff.data(), hIdx.data(), hDist.data(), hostOrdering.data(),
-                hostReach.data());
+    form_optics(n, hCore, hCd, hOff, hIdx, hDist, hostOrdering.data(), hostReach.data());
     return SDB_OK;
 }
