@@ -56,6 +56,14 @@ def build_ref(quiet: bool = True) -> str | None:
     return REF_SO
 
 
+def _fit_error(code: int) -> str:
+    """Message for a negative return of the oracle's whole-fit entry points."""
+    return {1: "transformData: negative input value (Chi2/JS)",
+            2: "transformData: a point sums to zero (Chi2/JS)",
+            3: "ker_n_features must be >= n_features for Chi2/JS (the reference overruns its embedding)",
+            }.get(code, f"rejected (code {code})")
+
+
 def fht_dim(n_proj: int, ker: int) -> int:
     """fhtDim = 2^ceil(log2(max(n_proj, ker)))  (src/sDbscan.h:107)."""
     import math
@@ -196,7 +204,7 @@ class Port:
                                      _i(clusterNoise), _f(samplingProb), ctypes.c_uint32(seed & 0xFFFFFFFF),
                                      _p(labels), _p(core), _p(times))
         if ncl < 0:
-            raise ValueError(f"transform rejected the input (code {-ncl})")
+            raise ValueError(_fit_error(-ncl))
         return labels, ncl, core, times
 
     def fit_sngdbscan(self, X, eps, minPts, *, dist="Cosine", samplingProb=0.01, seed=42, threads=-1):
@@ -214,7 +222,7 @@ class Port:
         ncl = self.L.orc_fit_sngdbscan(_p(X), _i(n), _i(d), _i(DIST_CODES[dist]), _f(samplingProb), _i(seed),
                                        _f(eps), _i(minPts), _i(threads), _p(labels), _p(core), _p(deg), _p(times))
         if ncl < 0:
-            raise ValueError(f"transform rejected the input (code {-ncl})")
+            raise ValueError(_fit_error(-ncl))
         return labels, ncl, core, deg, times
 
     def fit_sngoptics(self, X, eps, minPts, *, dist="Cosine", samplingProb=0.01, seed=42, threads=-1):
@@ -232,7 +240,7 @@ class Port:
                                      _f(eps), _i(minPts), _i(threads), _p(ordering), _p(reach), _p(core), _p(cd),
                                      _p(deg), _p(times))
         if r < 0:
-            raise ValueError(f"transform rejected the input (code {-r})")
+            raise ValueError(_fit_error(-r))
         return ordering, reach, core, cd, deg, times
 
     def fit_sngdbscan_blocks(self, X, eps, minPts, *, dist="Cosine", samplingProb=0.01, seed=42, block_rows=32,
@@ -288,7 +296,7 @@ class Port:
                                          _i(ker), _f(L), _p(R), _p(bits), _i(fd), _p(eps), _i(len(eps)),
                                          _i(minPts), _i(threads), _p(labels), _p(ncl), _p(times))
         if r < 0:
-            raise ValueError(f"transform rejected the input (code {-r})")
+            raise ValueError(_fit_error(-r))
         return labels, ncl, times
 
     def label_noise(self, P, topK, core, labels, samplingProb, seed):
@@ -319,7 +327,7 @@ class Port:
                                     _i(ker), _f(L), _p(R), _p(bits), _i(fd), _f(eps), _i(minPts), _i(threads),
                                     _i(tie_mode), _p(order), _p(reach), _p(core), _p(cd), _p(times))
         if rc < 0:
-            raise ValueError(f"transform rejected the input (code {-rc})")
+            raise ValueError(_fit_error(-rc))
         return order, reach, core, cd, times
 
     def _R(self, dist, ker, d, sigma, seed):

@@ -228,6 +228,14 @@ void orc_cauchy(int rows, int cols, float x0, float gamma, int seed, float* out)
         for (int r = 0; r < rows; ++r) out[(size_t)c * rows + r] = cd(gen);
 }
 
+// embedChi2 / embedJS fill the first d slots of a ker-long vector
+// (src/Utilities.h:140-145), so the reference requires ker >= d
+// (src/sDbscan.cpp:54) and overruns the vector otherwise.  Returns 3 for such
+// parameters (the whole-fit entry points return -3), else 0.
+static int embed_precondition(int code, int ker, int d) {
+    return (code == D_CHI2 || code == D_JS) && ker < d ? 3 : 0;
+}
+
 // ---- transformData (src/Utilities.h:289-335) ---------------------------------
 // X: d x n column-major, modified in place.  Returns 0, or 1 (negative value)
 // / 2 (zero-sum column) where the reference prints an error and exits.
@@ -601,6 +609,7 @@ int orc_fit_sdbscan(const float* X, int n, int d, int code, int nproj, int k, in
                     int clusterNoise, float samplingProb, uint32_t seed, int32_t* labels, uint8_t* core,
                     double* times) {
     if (threads > 0) omp_set_num_threads(threads);
+    if (int e = embed_precondition(code, ker, d)) return -e;
     Timer tm, all;
     std::vector<float> Xc(X, X + (size_t)n * d);
     int err = orc_transform(Xc.data(), n, d, code);
@@ -635,6 +644,7 @@ int orc_fit_sdbscan_sweep(const float* X, int n, int d, int code, int nproj, int
                           const float* R, const uint8_t* bits, int fhtDim, const float* eps, int nEps, int minPts,
                           int threads, int32_t* labels, int32_t* ncl, double* times) {
     if (threads > 0) omp_set_num_threads(threads);
+    if (int e = embed_precondition(code, ker, d)) return -e;
     Timer tm, all;
     std::vector<float> Xc(X, X + (size_t)n * d);
     int err = orc_transform(Xc.data(), n, d, code);
@@ -669,6 +679,7 @@ int orc_fit_soptics(const float* X, int n, int d, int code, int nproj, int k, in
                     const float* R, const uint8_t* bits, int fhtDim, float eps, int minPts, int threads,
                     int tie_mode, int32_t* ordering, float* reach, uint8_t* core, float* coreDist, double* times) {
     if (threads > 0) omp_set_num_threads(threads);
+    if (int e = embed_precondition(code, ker, d)) return -e;
     Timer tm, all;
     std::vector<float> Xc(X, X + (size_t)n * d);
     int err = orc_transform(Xc.data(), n, d, code);

@@ -116,6 +116,10 @@ sdb_status sdb_engine::derive() {
     ker = p.distance == SDB_COSINE ? d : p.ker_n_features;  // src/sDbscan.h:102-104
     if (ker < 1) return fail(SDB_ERR_ARG, "ker_n_features must be >= 1");
     if ((p.distance == SDB_L1 || p.distance == SDB_L2) && ker % 2) return fail(SDB_ERR_ARG, "ker_n_features must be even for L1/L2");
+    // embedChi2 / embedJS fill the first d slots of a ker-long vector
+    // (src/Utilities.h:140-145): the reference requires ker >= d (src/sDbscan.cpp:54)
+    if ((p.distance == SDB_CHI2 || p.distance == SDB_JS) && ker < d)
+        return fail(SDB_ERR_ARG, "ker_n_features must be >= n_features for Chi2/JS");
     const int mx = std::max(p.n_proj, ker);
     fhtDim = 1 << (int)std::ceil(std::log2((double)mx));  // src/sDbscan.h:107
     if (fhtDim < 16) return fail(SDB_ERR_ARG, "max(n_proj, ker_n_features) must be >= 9");

@@ -161,6 +161,9 @@ def test_errors_follow_reference_checks():
     with pytest.raises(capi.SdbError) as e:
         eng2.labels()
     assert e.value.status == 5  # SDB_ERR_STATE
+    with pytest.raises(capi.SdbError) as e:  # embedChi2 fills n_features slots of ker_n_features
+        eng2.set_params(n_proj=64, topK=3, topM=10, distance="Chi2", ker_n_features=8)
+    assert e.value.status == 1  # SDB_ERR_ARG
 
 
 def test_pybind_dropin_matches_capi():

@@ -119,3 +119,18 @@ def test_whole_fit_noise_labelling_matches_reference(port, name):
                                             clusterNoise=1, samplingProb=meta["samplingProb"])
     np.testing.assert_array_equal(labels, z["labels"])
     assert ncl == int(z["n_clusters"])
+
+
+def test_oracle_rejects_chi2_js_with_fewer_kernel_features_than_dimensions(port):
+    """embedChi2 / embedJS fill n_features slots of a ker_n_features-long
+    vector (src/Utilities.h:140-145); with ker_n_features < n_features the
+    reference overruns it (undefined behaviour), so the oracle, like the
+    engine, refuses those parameters; ker_n_features = n_features runs."""
+    from sdbscan_gb300 import datasets as ds
+    X = ds.cfg4_dirichlet(300, 130, n_comp=3, seed=2)[0]
+    for dist in ("Chi2", "JS"):
+        with pytest.raises(ValueError, match="ker_n_features"):
+            port.fit_sdbscan(X, 0.3, 5, dist=dist, n_proj=64, topK=3, topM=10, ker=64, seed=1)
+        with pytest.raises(ValueError, match="ker_n_features"):
+            port.fit_soptics(X, 0.3, 5, dist=dist, n_proj=64, topK=3, topM=10, ker=64, seed=1)
+        port.fit_sdbscan(X, 0.3, 5, dist=dist, n_proj=64, topK=3, topM=10, ker=130, seed=1)
