@@ -150,3 +150,51 @@ def test_golden_fixture_regenerates_bit_identically(name, tmp_path):
     assert sorted(new.files) == sorted(old.files)
     for k in old.files:
         np.testing.assert_array_equal(new[k], old[k], err_msg=k)
+
+
+def _random_config(case):
+    """A seeded random parameter set: distance, sizes, n_proj, topK, topM,
+    ker_n_features, minPts, eps and fit, within the reference's preconditions."""
+    rng = np.random.default_rng(1000 + case)
+    dist = str(rng.choice(["Cosine", "L1", "L2", "Chi2", "JS"]))
+    n = int(rng.integers(50, 1200))
+    d = int(rng.choice([3, 8, 17, 32, 65, 130]))
+    n_proj = int(rng.choice([16, 64, 100, 256, 512]))
+    k = int(rng.integers(1, min(12, n_proj) + 1))
+    m = int(rng.integers(1, min(60, n) + 1))
+    ker = d if dist == "Cosine" else int(rng.choice([64, 128, 256, 512]))
+    if dist in ("Chi2", "JS") and ker < d:
+        ker = int(2 ** np.ceil(np.log2(d)))
+    minPts = int(rng.integers(2, 20))
+    seed = int(rng.integers(0, 1000))
+    if dist == "Cosine":
+        X, eps = ds.cfg1_cosine(n, d, seed=seed)[0], float(rng.uniform(0.02, 0.4))
+    elif dist in ("L1", "L2"):
+        X, eps = ds.cfg3_aniso_l2(n, d, n_comp=4, scale=0.1, seed=seed)[0], float(rng.uniform(0.2, 3.0))
+    else:
+        X, eps = ds.cfg4_dirichlet(n, d, n_comp=4, conc=10, seed=seed)[0], float(rng.uniform(0.05, 0.5))
+    return dist, X, n_proj, k, m, ker, minPts, eps, bool(rng.integers(0, 2)), seed
+
+
+@pytest.mark.parametrize("case", range(30))
+def test_random_configurations_match_reference(port, case):
+    """Seeded random configurations over every distance and both fits, one
+    thread: sDBSCAN labels, core flags and n_clusters_, or sOPTICS core flags
+    and core distances, equal the reference's."""
+    dist, X, n_proj, k, m, ker, minPts, eps, optics, seed = _random_config(case)
+    n, d = X.shape
+    r = Ref(n, d)
+    r.set_params(n_proj=n_proj, topK=k, topM=m, distance=dist, ker_n_features=ker, ker_sigma=0.7, n_threads=1,
+                 random_seed=seed)
+    kw = dict(dist=dist, n_proj=n_proj, topK=k, topM=m, ker=ker, sigma=0.7, seed=seed, threads=1)
+    if optics:
+        r.fit_sOptics(X, eps, minPts)
+        _, _, core, cd, _ = port.fit_soptics(X, eps, minPts, **kw)
+        np.testing.assert_array_equal(core, r.core())
+        np.testing.assert_array_equal(cd, r.core_dist())
+    else:
+        r.fit_sDbscan(X, eps, minPts)
+        labels, ncl, core, _ = port.fit_sdbscan(X, eps, minPts, **kw)
+        np.testing.assert_array_equal(core, r.core())
+        np.testing.assert_array_equal(labels, r.labels_)
+        assert ncl == r.n_clusters_
