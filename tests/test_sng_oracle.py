@@ -125,3 +125,32 @@ def test_block_rule_keeps_the_reference_statistics(port):
     assert abs(blk_o - ref_o) < 0.02 * ref_o, (blk_o, ref_o)
     assert abs(blk_d - ref_d) < 0.02 * ref_d, (blk_d, ref_d)
     assert shr_o < 0.95 * ref_o and shr_d < 0.95 * ref_d, (shr_o, shr_d, ref_o, ref_d)
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__file__), "..", "oracle", "_ref",
+                                                    "libsdbscan_ref.so")), reason="reference library not built here")
+@pytest.mark.parametrize("case", range(20))
+def test_random_sngdbscan_configurations_match_reference(port, case):
+    """Seeded random sngDbscan configurations (all distances, 2-900 points,
+    samplingProb from 0.001 to 1.5, i.e. sampled and exact): labels,
+    n_clusters_ and core flags equal the reference's, one thread."""
+    from oracle.oracle import Ref
+    from sdbscan_gb300 import datasets as ds
+    rng = np.random.default_rng(5000 + case)
+    dist = str(rng.choice(["Cosine", "L1", "L2", "Chi2", "JS"]))
+    n, d = int(rng.integers(2, 900)), int(rng.choice([3, 8, 17, 32, 65]))
+    prob = float(rng.choice([0.001, 0.01, 0.05, 0.3, 0.9, 1.0, 1.5]))
+    minPts, seed = int(rng.integers(2, 20)), int(rng.integers(0, 1000))
+    if dist == "Cosine":
+        X, eps = ds.cfg1_cosine(n, d, seed=seed)[0], float(rng.uniform(0.02, 0.4))
+    elif dist in ("L1", "L2"):
+        X, eps = ds.cfg3_aniso_l2(n, d, n_comp=4, scale=0.1, seed=seed)[0], float(rng.uniform(0.2, 3.0))
+    else:
+        X, eps = ds.cfg4_dirichlet(n, d, n_comp=4, conc=10, seed=seed)[0], float(rng.uniform(0.05, 0.5))
+    r = Ref(n, d)
+    r.set_sngParams(distance=dist, samplingProb=prob, n_threads=1, random_seed=seed)
+    r.fit_sngDbscan(X, eps, minPts)
+    labels, ncl, core, _, _ = port.fit_sngdbscan(X, eps, minPts, dist=dist, samplingProb=prob, seed=seed, threads=1)
+    np.testing.assert_array_equal(core, r.core())
+    np.testing.assert_array_equal(labels, r.labels_)
+    assert ncl == r.n_clusters_
