@@ -82,7 +82,7 @@ void sdb_engine_destroy(sdb_engine* e);
 
 /* set_params / set_kernel_params / set_topK / set_topM / set_threads /
  * set_clusterNoise  (src/sDbscan.h:79-124, :170-180).  Limits of this engine:
- * n_proj <= 2048, max(n_proj, ker_n_features) <= 16384 (d <= 16384 for
+ * n_proj <= 2048, 9 <= max(n_proj, ker_n_features) <= 16384 (d <= 16384 for
  * Cosine), 1 <= topK <= 31 and topK <= n_proj, topM <= n_points.  Chi2 and
  * JS need ker_n_features >= n_features, the reference's own precondition
  * (src/sDbscan.cpp:54; embedChi2 / embedJS write n_features slots of a
