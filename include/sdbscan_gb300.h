@@ -83,7 +83,8 @@ void sdb_engine_destroy(sdb_engine* e);
 /* set_params / set_kernel_params / set_topK / set_topM / set_threads /
  * set_clusterNoise  (src/sDbscan.h:79-124, :170-180).  Limits of this engine:
  * n_proj <= 2048, 9 <= max(n_proj, ker_n_features) <= 16384 (d <= 16384 for
- * Cosine), 1 <= topK <= 31 and topK <= n_proj, topM <= n_points.  Chi2 and
+ * Cosine), 1 <= topK <= 31 and topK <= n_proj, topM <= n_points, an even
+ * ker_n_features for L1 / L2.  Chi2 and
  * JS need ker_n_features >= n_features, the reference's own precondition
  * (src/sDbscan.cpp:54; embedChi2 / embedJS write n_features slots of a
  * ker_n_features-long vector, src/Utilities.h:140-145, and overrun it
