@@ -198,3 +198,37 @@ def test_random_configurations_match_reference(port, case):
         np.testing.assert_array_equal(core, r.core())
         np.testing.assert_array_equal(labels, r.labels_)
         assert ncl == r.n_clusters_
+
+
+@pytest.mark.parametrize("case", range(15))
+def test_random_noise_labelling_configurations_match_reference(port, case):
+    """sDbscan-1NN (clusterNoise = 1) with every core sampled, seeded random
+    configurations: labels equal the reference's.  Where there is no core
+    point the reference reads labels_[-1] (undefined); the oracle keeps every
+    point as noise."""
+    rng = np.random.default_rng(3000 + case)
+    dist = str(rng.choice(["Cosine", "L1", "L2", "Chi2", "JS"]))
+    n, d = int(rng.integers(50, 1500)), int(rng.choice([8, 17, 32, 65]))
+    n_proj = int(rng.choice([16, 64, 256]))
+    k, m = int(rng.integers(1, min(10, n_proj) + 1)), int(rng.integers(1, min(50, n) + 1))
+    ker = d if dist == "Cosine" else int(rng.choice([64, 128, 256]))
+    if dist in ("Chi2", "JS") and ker < d:
+        ker = 128
+    minPts, seed = int(rng.integers(2, 20)), int(rng.integers(0, 1000))
+    if dist == "Cosine":
+        X, eps = ds.cfg1_cosine(n, d, seed=seed)[0], float(rng.uniform(0.02, 0.3))
+    elif dist in ("L1", "L2"):
+        X, eps = ds.cfg3_aniso_l2(n, d, n_comp=4, scale=0.1, seed=seed)[0], float(rng.uniform(0.2, 2.0))
+    else:
+        X, eps = ds.cfg4_dirichlet(n, d, n_comp=4, conc=10, seed=seed)[0], float(rng.uniform(0.05, 0.4))
+    kw = dict(dist=dist, n_proj=n_proj, topK=k, topM=m, ker=ker, sigma=0.7, seed=seed, threads=1)
+    labels, ncl, core, _ = port.fit_sdbscan(X, eps, minPts, clusterNoise=1, samplingProb=1.0, **kw)
+    if core.sum() == 0:
+        assert (labels == -1).all() and ncl == 2
+        return
+    r = Ref(n, d)
+    r.set_params(n_proj=n_proj, topK=k, topM=m, distance=dist, ker_n_features=ker, ker_sigma=0.7, clusterNoise=1,
+                 samplingProb=1.0, n_threads=1, random_seed=seed)
+    r.fit_sDbscan(X, eps, minPts)
+    np.testing.assert_array_equal(labels, r.labels_)
+    assert ncl == r.n_clusters_
