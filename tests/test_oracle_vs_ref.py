@@ -232,3 +232,31 @@ def test_random_noise_labelling_configurations_match_reference(port, case):
     r.fit_sDbscan(X, eps, minPts)
     np.testing.assert_array_equal(labels, r.labels_)
     assert ncl == r.n_clusters_
+
+
+@pytest.mark.parametrize("case", [c for c in range(40) if _random_config(c)[8]][:15])
+def test_random_soptics_ordering_matches_reference(port, case):
+    """sOPTICS ordering and reachability on seeded random configurations, one
+    thread: the oracle's stages, with the neighbour lists in the reference's
+    own order and the reference's value-only heap ties (tie_mode 0), give the
+    reference's ordering_ and reachability_ bit for bit."""
+    from oracle.oracle import fht_dim
+    dist, X, n_proj, k, m, ker, minPts, eps, _, seed = _random_config(case)
+    n, d = X.shape
+    r = Ref(n, d)
+    r.set_params(n_proj=n_proj, topK=k, topM=m, distance=dist, ker_n_features=ker, ker_sigma=0.7, n_threads=1,
+                 random_seed=seed)
+    r.fit_sOptics(X, eps, minPts)
+    fd = fht_dim(n_proj, ker)
+    Xt, _ = port.transform(X, dist)
+    P = port.project(Xt, dist, ker, 0.4, port._R(dist, ker, d, 0.7, seed), port.hd3_bits(3 * fd, seed), fd, n_proj)
+    port.L.orc_set_threads(1)
+    try:
+        core, _, off, idx, dd = port.find_core(Xt, dist, port.topk(P, k), port.topm(P, m), eps, minPts,
+                                               with_dist=True, ref_order=True)
+    finally:
+        port.L.orc_set_threads(0)
+    order, reach = port.form_optics(core, port.core_dist(n, minPts, core), off, idx, dd, tie_mode=0)
+    port.graph_free()
+    np.testing.assert_array_equal(order, r.ordering_)
+    np.testing.assert_array_equal(reach, r.reachability_)
