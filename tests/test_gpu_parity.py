@@ -415,6 +415,6 @@ def test_noise_labelling_sampled_matches_oracle(port):
     assert (labels == -1).sum() == 0
     # no core point at all: nothing to join (the reference reads labels_[-1]
     # here, src/sDbscan.cpp:798-805); every point stays noise, as in the oracle
-    eng.fit_sdbscan(X, 1e-6, minPts)
+    eng.fit_sdbscan(X, -1.0, minPts)  # no pair is within a negative eps
     labels, ncl = eng.labels()
     assert eng.core()[0].sum() == 0 and (labels == -1).all() and ncl == 2
