@@ -152,9 +152,10 @@ def test_golden_fixture_regenerates_bit_identically(name, tmp_path):
         np.testing.assert_array_equal(new[k], old[k], err_msg=k)
 
 
-def _random_config(case):
-    """A seeded random parameter set: distance, sizes, n_proj, topK, topM,
-    ker_n_features, minPts, eps and fit, within the reference's preconditions."""
+def _random_params(case):
+    """A seeded random parameter set within the reference's preconditions:
+    distance, n, d, n_proj, topK, topM, ker_n_features, minPts, eps, fit
+    (True = sOPTICS) and seed.  Cheap: no data is drawn."""
     rng = np.random.default_rng(1000 + case)
     dist = str(rng.choice(["Cosine", "L1", "L2", "Chi2", "JS"]))
     n = int(rng.integers(50, 1200))
@@ -167,13 +168,21 @@ def _random_config(case):
         ker = int(2 ** np.ceil(np.log2(d)))
     minPts = int(rng.integers(2, 20))
     seed = int(rng.integers(0, 1000))
+    lo, hi = {"Cosine": (0.02, 0.4), "L1": (0.2, 3.0), "L2": (0.2, 3.0)}.get(dist, (0.05, 0.5))
+    eps = float(rng.uniform(lo, hi))
+    return dist, n, d, n_proj, k, m, ker, minPts, eps, bool(rng.integers(0, 2)), seed
+
+
+def _random_config(case):
+    """_random_params with the data drawn from the distance's law."""
+    dist, n, d, n_proj, k, m, ker, minPts, eps, optics, seed = _random_params(case)
     if dist == "Cosine":
-        X, eps = ds.cfg1_cosine(n, d, seed=seed)[0], float(rng.uniform(0.02, 0.4))
+        X = ds.cfg1_cosine(n, d, seed=seed)[0]
     elif dist in ("L1", "L2"):
-        X, eps = ds.cfg3_aniso_l2(n, d, n_comp=4, scale=0.1, seed=seed)[0], float(rng.uniform(0.2, 3.0))
+        X = ds.cfg3_aniso_l2(n, d, n_comp=4, scale=0.1, seed=seed)[0]
     else:
-        X, eps = ds.cfg4_dirichlet(n, d, n_comp=4, conc=10, seed=seed)[0], float(rng.uniform(0.05, 0.5))
-    return dist, X, n_proj, k, m, ker, minPts, eps, bool(rng.integers(0, 2)), seed
+        X = ds.cfg4_dirichlet(n, d, n_comp=4, conc=10, seed=seed)[0]
+    return dist, X, n_proj, k, m, ker, minPts, eps, optics, seed
 
 
 @pytest.mark.parametrize("case", range(30))
@@ -234,7 +243,7 @@ def test_random_noise_labelling_configurations_match_reference(port, case):
     assert ncl == r.n_clusters_
 
 
-@pytest.mark.parametrize("case", [c for c in range(40) if _random_config(c)[8]][:15])
+@pytest.mark.parametrize("case", [c for c in range(60) if _random_params(c)[9]][:15])
 def test_random_soptics_ordering_matches_reference(port, case):
     """sOPTICS ordering and reachability on seeded random configurations, one
     thread: the oracle's stages, with the neighbour lists in the reference's
