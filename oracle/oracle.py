@@ -338,6 +338,14 @@ class Port:
         return None
 
 
+def ref_load_txt(path, n: int, d: int, so: str = REF_SO) -> np.ndarray:
+    """The reference's own text loader (loadtxtData) on a file of n lines of d
+    numbers; (n, d) float32."""
+    out = np.zeros((n, d), np.float32)
+    ctypes.CDLL(so).ref_load_txt(str(path).encode(), _i(n), _i(d), _p(out))
+    return out
+
+
 class Ref:
     """The reference class itself (oracle/_ref), via oracle/ref_harness.cpp."""
 

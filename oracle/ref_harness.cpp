@@ -113,6 +113,13 @@ void ref_test_sdbscan(void* h, const float* X, int n, int d, float eps, float ra
     P(h)->setOutput(prefix);
     P(h)->test_sDbscan(ref, eps, rangeEps, nTests, minPts);
 }
+// loadtxtData (src/Utilities.cpp:60-95) with distance "L2", which leaves the
+// parsed values untransformed; out: n x d, one point per row.
+void ref_load_txt(const char* path, int n, int d, float* out) {
+    MatrixXf M;
+    loadtxtData(string(path), "L2", n, d, M);
+    std::memcpy(out, M.data(), sizeof(float) * (size_t)n * d);
+}
 void ref_clear(void* h) { P(h)->clear(); }
 
 int ref_n_clusters(void* h) { return P(h)->n_clusters_; }

@@ -269,3 +269,40 @@ def test_random_soptics_ordering_matches_reference(port, case):
     port.graph_free()
     np.testing.assert_array_equal(order, r.ordering_)
     np.testing.assert_array_equal(reach, r.reachability_)
+
+
+def test_text_loader_parses_like_the_reference(tmp_path):
+    """sdb_load_txt against the reference's own loadtxtData (fscanf "%f",
+    src/Utilities.cpp:60-95) on long decimal strings (near-halfway roundings),
+    exponents down to the subnormal range and past it, signs and odd spacing:
+    every float32 is the same."""
+    from oracle.oracle import ref_load_txt
+    from sdbscan_gb300 import capi
+    try:
+        capi.load()
+    except Exception as e:
+        pytest.skip(f"engine library not built here: {e}")
+    rng = np.random.default_rng(8)
+    n, d = 400, 9
+    toks = []
+    for i in range(n * d):
+        kind = i % 6
+        if kind == 0:
+            toks.append(f"{rng.standard_normal():.25f}")
+        elif kind == 1:
+            toks.append(f"{rng.standard_normal():.20e}")
+        elif kind == 2:
+            toks.append(f"{rng.random() * 1e-39:.30e}")  # subnormal float32 range
+        elif kind == 3:
+            toks.append(f"{rng.random() * 1e-47:.10e}")  # below the smallest subnormal
+        elif kind == 4:
+            toks.append(str(int(rng.integers(-10**6, 10**6))))
+        else:
+            toks.append(f"+{rng.random() * 10 ** int(rng.integers(-8, 8)):.17g}")
+    path = tmp_path / "data.txt"
+    with open(path, "w") as f:
+        for r in range(n):
+            f.write(("  " if r % 2 else "\t").join(toks[r * d:(r + 1) * d]) + (" \n" if r % 3 else "\n"))
+    want = ref_load_txt(path, n, d)
+    got = capi.load_txt(path, n, d)
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
