@@ -53,7 +53,7 @@ DIST_FLOPS = {"Cosine": 2, "L2": 3, "L1": 3, "Chi2": 4, "JS": 8}
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # nominal FP32 CUDA-core peak at max SM clock
 # DRAM bytes (read + write) of one k_dist<Cosine> launch on the 1M x 784
 # workload, from a one-pass ncu capture of
-# `python -m sdbscan_gb300.profile_fit 1000000 0` (profiles/k_dist_fp32_cfg2.md):
+# `python bench.py --single-fit 1000000 --precision 0` (profiles/k_dist_fp32_cfg2.md):
 # 23.29 GB read + 0.370 GB written (tiles run in point-chunk order).
 K_DIST_TRAFFIC_1M = 23.29e9 + 0.370e9
 # sngDBSCAN, the reference's sampling baseline that its benchmark loop runs
@@ -686,6 +686,37 @@ def run_ours(args, cfg):
     return 0
 
 
+def run_single_fit(args):
+    """One fit on the config-2 law at n = args.single_fit points, with the
+    engine's per-stage CUDA-event times and counters printed as one JSON
+    line: the small, self-contained case the ncu captures in profiles/ run.
+    --fit sdbscan (d, distance: Cosine, or L1 / L2 / Chi2 with ker 1024,
+    sigma 1) or sng (sngDbscan, Cosine, samplingProb --prob); eps 0.25,
+    minPts 50, seed 42."""
+    import torch
+
+    from sdbscan_gb300 import capi, datasets
+    n, d, dist = args.single_fit, args.d, args.distance
+    X, _ = datasets.cfg2_mnist_like_torch(n, d, seed=2007, device="cuda")
+    torch.cuda.synchronize()
+    eng = capi.Engine(n, d)
+    if args.fit == "sng":
+        eng.set_sng_params(distance=dist, samplingProb=args.prob, random_seed=42)
+        eng.set_precision(args.precision)
+        eng.fit_sngdbscan_device(X.data_ptr(), 0.25, 50)
+    else:
+        kw = dict(ker_n_features=1024, ker_sigma=1.0) if dist != "Cosine" else {}
+        eng.set_params(n_proj=1024, topK=10, topM=50, distance=dist, random_seed=42, precision=args.precision, **kw)
+        if args.fit == "soptics":
+            eng.fit_soptics_device(X.data_ptr(), 0.25, 50)
+        else:
+            eng.fit_sdbscan_device(X.data_ptr(), 0.25, 50)
+    print(json.dumps({"single_fit": args.fit, "n": n, "d": d, "distance": dist, "precision": args.precision,
+                      "stage_ms": eng.stage_ms(), "counters": eng.counters()}))
+    eng.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -700,7 +731,16 @@ def main():
     ap.add_argument("--batched-cpu", action="store_true", help="(reference arm) time the config-5 CPU baseline only")
     ap.add_argument("--no-sng", action="store_true")
     ap.add_argument("--sng-cpu", action="store_true", help="(reference arm) time the sngDbscan CPU baseline only")
+    ap.add_argument("--single-fit", type=int, default=0, metavar="N",
+                    help="one fit of N points of the config-2 law, stage times printed (for profilers)")
+    ap.add_argument("--fit", default="sdbscan", choices=["sdbscan", "soptics", "sng"])
+    ap.add_argument("--precision", type=int, default=0, help="0 = FP32, 1 = BF16 (with --single-fit)")
+    ap.add_argument("--d", type=int, default=784, help="dimensions (with --single-fit)")
+    ap.add_argument("--distance", default="Cosine", help="distance (with --single-fit)")
+    ap.add_argument("--prob", type=float, default=0.01, help="sngDbscan samplingProb (with --single-fit --fit sng)")
     args = ap.parse_args()
+    if args.single_fit:
+        return run_single_fit(args)
     cfg = WORKLOADS[args.config]
     if args.impl == "reference" and args.batched_cpu:
         print(json.dumps(_cpu_batched()))

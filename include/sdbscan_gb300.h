@@ -266,10 +266,17 @@ const char* sdb_batch_last_error(sdb_batch* b);
  *                 and content as sdb_get_topm
  *   stream      : cudaStream_t to run on (NULL = legacy default stream)
  * Limits: n_proj <= 1024, topM <= 64, topM <= n_points; larger sizes return
- * SDB_ERR_ARG.  Scratch is one fixed __device__ array (about 12 MiB) held by
- * every GPU that loads this library until it is unloaded.  The first call on
- * a device looks up that array's device address; make it before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race. */
+ * SDB_ERR_ARG.  When n_proj is a multiple of 4 the rows are read as 16-byte
+ * vectors, so proj_device must then be 16-byte aligned (SDB_ERR_ARG
+ * otherwise; an offset view into a larger buffer may not be).
+ * Scratch is one fixed __device__ array (about 12 MiB) held by every GPU that
+ * loads this library until it is unloaded.  With CUDA's lazy module loading
+ * (the default) the array is reserved on a device by the first call there,
+ * which also looks up its device address: make that first call before the
+ * caller's memory pool takes the device's memory, and before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race.
+ * The boundary-tie count and internal-error flag that a fit reports through
+ * sdb_get_counters / SDB_ERR_INTERNAL are not reported by this call. */
 sdb_status sdb_topm_noalloc(const float* proj_device, int32_t n_points, int32_t n_proj, int32_t topM,
                             int32_t* topM_device, void* stream);
 

@@ -45,7 +45,8 @@ def build_port(quiet: bool = True) -> str:
 
 def build_ref(quiet: bool = True) -> str | None:
     """Builds oracle/_ref when the reference sources are present; else None."""
-    src = os.environ.get("SDBSCAN_REF_SRC", "/root/reference/src")
+    # SDBSCAN_REF_SRC, else a checkout of the reference next to this repository
+    src = os.environ.get("SDBSCAN_REF_SRC") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference", "src")
     if not os.path.isfile(os.path.join(src, "sDbscan.cpp")):
         return None
     import platform

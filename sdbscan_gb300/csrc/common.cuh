@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #define SDB_DEV __device__ __forceinline__
 
 namespace sdb {
@@ -106,6 +108,26 @@ enum { DIST_COSINE = 0, DIST_L1 = 1, DIST_L2 = 2, DIST_CHI2 = 3, DIST_JS = 4 };
 // -------------------------------------------------------------------------
 namespace sdb {
 
+// Streaming multiprocessors of the current device, queried once per device;
+// grid sizes are multiples of it.
+inline int sm_count() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 1;
+    }
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v == 0) {
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+            cudaGetLastError();
+            v = 1;
+        }
+        cache[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
+}
+
 struct ProjectArgs {
     const float* X;      // input rows (n x d, row stride ldx)
     int ldx;
@@ -163,7 +185,6 @@ struct TopMArgs {
 int launch_topm_thresholds(const TopMArgs& a, cudaStream_t st);
 int launch_topm_collect(const TopMArgs& a, cudaStream_t st);
 int launch_topm_select(const TopMArgs& a, cudaStream_t st);
-int launch_topm_fallback(const TopMArgs& a, int list, uint32_t* hist, cudaStream_t st);
 
 // Exclusive scan of n int64 values (in place allowed); tmp needs
 // scan_tmp_elems(n) entries.

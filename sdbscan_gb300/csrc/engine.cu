@@ -199,7 +199,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     // top-m threshold chunks: a full wave of projection blocks (4 per SM) for
     // each upload segment, and at least 4m chunks so the chunk maxima bound
     // the m-th value
-    const int chunksWanted = std::max(152 * 4 * kUploadSegs, 4 * m);
+    const int chunksWanted = std::max(sm_count() * 4 * kUploadSegs, 4 * m);
     const int chunk = std::max(8, (n + chunksWanted - 1) / chunksWanted);
     const int G = (n + chunk - 1) / chunk;
     int cap = 256;
@@ -463,7 +463,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * ldb) || !ensure(queue, sizeof(uint64_t) * (size_t)qcap))
             return SDB_ERR_NOMEM;
         L_(launch_to_bf16(f32(Xt), ld, n, Xb.ptr, ldb, st));
-        const int grid = (int)std::min<int64_t>(maxTiles, 152 * 3);
+        const int grid = (int)std::min<int64_t>(maxTiles, (int64_t)sm_count() * 3);
         L_(launch_dist_tc(da, Xb.ptr, ldb, static_cast<uint64_t*>(queue.ptr), qcap, ctr + 4,
                           i32(errFlags) + 4, grid, st));
         L_(launch_recheck(da, static_cast<const uint64_t*>(queue.ptr), ctr + 4, qcap, st));

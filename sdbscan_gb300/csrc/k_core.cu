@@ -351,7 +351,7 @@ __global__ void k_core_dist(CoreArgs a, const int64_t* __restrict__ nbOff, const
 
 static int core_grid(int n, int warps) {
     const int blocks = (n + warps - 1) / warps;
-    return std::min(blocks, 152 * 8);
+    return std::min(blocks, sm_count() * 8);
 }
 
 int launch_slot_sigs(const int32_t* topM, int D, int m, const int64_t* hubOff, const int32_t* hubLists, void* sig,

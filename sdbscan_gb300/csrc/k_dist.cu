@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(TM) k_masks_from_rounds(DistArgs a) {
 }  // namespace
 
 int launch_pair_rounds(const DistArgs& a, uint8_t* rounds, cudaStream_t st) {
-    k_pair_rounds<<<152 * 16, 256, 0, st>>>(a.dists, a, reinterpret_cast<uint32_t*>(rounds));
+    k_pair_rounds<<<sm_count() * 16, 256, 0, st>>>(a.dists, a, reinterpret_cast<uint32_t*>(rounds));
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 

@@ -432,13 +432,13 @@ int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, uint64_t* queue, 
 }
 
 int launch_screen_reset(const DistArgs& a, cudaStream_t st) {
-    k_screen_reset<<<152 * 4, 256, 0, st>>>(a);
+    k_screen_reset<<<sm_count() * 4, 256, 0, st>>>(a);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
 int launch_recheck(const DistArgs& a, const uint64_t* queue, const unsigned long long* qcount, int64_t qcap,
                    cudaStream_t st) {
-    k_recheck<<<152 * 8, RC_WARPS * 32, 0, st>>>(a, queue, qcount, qcap);
+    k_recheck<<<sm_count() * 8, RC_WARPS * 32, 0, st>>>(a, queue, qcount, qcap);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 

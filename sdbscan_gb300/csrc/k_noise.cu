@@ -129,7 +129,7 @@ __global__ void k_noise_1nn(NoiseArgs a) {
 int launch_label_noise(const NoiseArgs& a, cudaStream_t st) {
     int launches = 0;
     if (cudaMemsetAsync(a.numCore, 0, sizeof(int32_t), st) != cudaSuccess) return -1;
-    k_count_cores<<<152 * 4, 256, 0, st>>>(a.core, a.n, a.numCore);
+    k_count_cores<<<sm_count() * 4, 256, 0, st>>>(a.core, a.n, a.numCore);
     k_noise_flags<<<(a.n + 1 + 255) / 256, 256, 0, st>>>(a);
     launches += 2;
     int r = launch_scan_i64(a.sampleFlag, a.sampleFlag, (size_t)a.n + 1, a.scanTmp, st);
@@ -141,7 +141,7 @@ int launch_label_noise(const NoiseArgs& a, cudaStream_t st) {
     k_noise_compact<<<(a.n + 255) / 256, 256, 0, st>>>(a);
     dim3 tg((a.sMax + 31) / 32, (a.nproj + 31) / 32);
     k_core_proj_t<<<tg, 256, 0, st>>>(a);
-    k_noise_1nn<<<152 * 8, 256, 0, st>>>(a);
+    k_noise_1nn<<<sm_count() * 8, 256, 0, st>>>(a);
     launches += 3;
     return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
 }

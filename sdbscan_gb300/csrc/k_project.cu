@@ -24,10 +24,6 @@
 namespace sdb {
 namespace {
 
-// Projection blocks per launch: one full wave of 4 blocks per SM; the blocks
-// walk the launch's chunks grid-stride.
-constexpr int kProjectBlocks = 152 * 4;
-
 __device__ __forceinline__ void cp_async16(float* dst, const float* src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
                  "l"(src));
@@ -552,7 +548,7 @@ int launch_project_smem(const ProjectArgs& a, const float* scale, cudaStream_t s
     if (cudaFuncSetAttribute(k_project_smem<EMB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
         cudaSuccess)
         return -1;
-    k_project_smem<EMB><<<std::min(G, 152 * 2), kBigThreads, sm, st>>>(a, scale);
+    k_project_smem<EMB><<<std::min(G, sm_count() * 2), kBigThreads, sm, st>>>(a, scale);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
@@ -597,7 +593,8 @@ int launch_project_nje(const ProjectArgs& a, const float* scale, cudaStream_t st
     const int warps = 4;
     const int G = (a.chunkEnd > 0 ? a.chunkEnd : (a.n + a.chunk - 1) / a.chunk) - a.chunkBase;
     if (G <= 0) return 0;
-    const int grid = std::min(G, kProjectBlocks);
+    // one full wave of 4 blocks per SM; the blocks walk the launch's chunks grid-stride
+    const int grid = std::min(G, sm_count() * 4);
     const int nsw = (3 * a.fhtDim + 31) / 32;
     const int rowLen = EMB == 2 ? ((a.d + 3) & ~3) + a.fhtDim : 0;
     const size_t xs = (size_t)((a.d + 3) & ~3);
@@ -655,7 +652,7 @@ int launch_transform(const ProjectArgs& a, cudaStream_t st) {
                                                                         a.err);
     if (cudaPeekAtLastError() != cudaSuccess) return -1;
     if (a.ld & 3) return -1;
-    const int grid = (int)std::min<int64_t>(((int64_t)a.n + 7) / 8, (int64_t)152 * 16);
+    const int grid = (int)std::min<int64_t>(((int64_t)a.n + 7) / 8, (int64_t)sm_count() * 16);
     k_transform_rows<<<grid, 256, 0, st>>>(a.X, a.ldx, a.n, a.d, a.ld, a.dist, a.scale, a.Xt);
     return cudaPeekAtLastError() == cudaSuccess ? 2 : -1;
 }

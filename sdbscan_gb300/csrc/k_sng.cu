@@ -331,7 +331,7 @@ int launch_block(const SngArgs& a, cudaStream_t st) {
 
 int grid_for(int64_t work, int threads) {
     const int64_t b = (work + threads - 1) / threads;
-    return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 8));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)sm_count() * 8));
 }
 
 }  // namespace

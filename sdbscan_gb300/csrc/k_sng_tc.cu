@@ -345,12 +345,12 @@ int launch_sng_tc(const SngArgs& a, const void* Xb, const void* Ub, int ldb, uin
         return -1;
     const int nbt = (a.nU + BN - 1) / BN;
     const int64_t tiles = (int64_t)((a.n + BM - 1) / BM) * nbt;
-    const int grid = (int)std::min<int64_t>(tiles, 152);
+    const int grid = (int)std::min<int64_t>(tiles, (int64_t)sm_count());
     k_sng_tc<<<grid, NT, sm, st>>>(tmX, tmU, a, ldb / BK, nbt, tiles, queue, qcap, qcount, gate);
     if (cudaPeekAtLastError() != cudaSuccess) return -1;
-    k_sng_recheck<<<152 * 8, RC_WARPS * 32, 0, st>>>(a, queue, qcount, qcap, gate);
+    k_sng_recheck<<<sm_count() * 8, RC_WARPS * 32, 0, st>>>(a, queue, qcount, qcap, gate);
     if (cudaPeekAtLastError() != cudaSuccess) return -1;
-    k_sng_reset<<<152 * 4, 256, 0, st>>>(a, gate);
+    k_sng_reset<<<sm_count() * 4, 256, 0, st>>>(a, gate);
     return cudaPeekAtLastError() == cudaSuccess ? 3 : -1;
 }
 

@@ -289,6 +289,4 @@ int launch_topm_select(const TopMArgs& a, cudaStream_t st) {
     return cudaPeekAtLastError() == cudaSuccess ? 2 : -1;
 }
 
-int launch_topm_fallback(const TopMArgs&, int, uint32_t*, cudaStream_t) { return 0; }
-
 }  // namespace sdb

@@ -15,9 +15,12 @@
 // as long as the library stays loaded.  All calls share it: two calls that
 // overlap on the GPU (different streams, or different host threads) race and
 // must not be issued.  Each call zeroes the counters it needs, so successive
-// calls do not see the previous call's state.
+// calls do not see the previous call's state.  The boundary-tie count and the
+// internal-error flag that a fit reports are kept in the array but not
+// returned by this entry point.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 
 #include "../../include/sdbscan_gb300.h"
@@ -70,6 +73,9 @@ extern "C" sdb_status sdb_topm_noalloc(const float* proj_device, int32_t n_point
                                        int32_t* topM_device, void* stream) {
     if (!proj_device || !topM_device || n_points < 1 || n_proj < 1 || topM < 1) return SDB_ERR_ARG;
     if (n_proj > kMaxProj || topM > kMaxTopM || topM > n_points) return SDB_ERR_ARG;
+    // rows of a multiple of 4 projections are read as float4: the base must be
+    // 16-byte aligned (an offset view of a larger buffer may not be)
+    if (n_proj % 4 == 0 && reinterpret_cast<uintptr_t>(proj_device) % 16 != 0) return SDB_ERR_ARG;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return SDB_ERR_CUDA;
     unsigned char* base = nullptr;

@@ -168,3 +168,12 @@ def test_no_cpu_fallback_without_a_gpu():
         pytest.skip(f"drop-in module not built here: {err}")
     with pytest.raises(RuntimeError):
         mod.sDbscan(10, 4)
+
+
+def test_topm_noalloc_rejects_misaligned_rows(lib):
+    """sdb_topm_noalloc reads rows of a multiple of 4 projections as 16-byte
+    vectors; a base that is not 16-byte aligned is refused on the host before
+    anything is launched (the pointer below is never dereferenced)."""
+    vp = ctypes.c_void_p
+    assert lib.sdb_topm_noalloc(vp(0x10004), 1000, 1024, 50, vp(0x20000), None) == 1
+    assert lib.sdb_topm_noalloc(vp(0x10008), 1000, 512, 50, vp(0x20000), None) == 1
