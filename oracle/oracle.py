@@ -89,6 +89,7 @@ class Port:
         L.orc_fit_sngdbscan.restype = _i
         L.orc_fit_sngoptics.restype = _i
         L.orc_distance.restype = _f
+        L.orc_core_cluster_lean.restype = _i
 
     def set_timing_mode(self, on: bool) -> None:
         """Cosine / L1 / L2 distances with vectorisable partial sums, at the
@@ -140,18 +141,59 @@ class Port:
         self.L.orc_topm(_p(np.ascontiguousarray(P)), _i(n), _i(nproj), _i(m), _p(out))
         return out
 
-    def find_core(self, Xt, dist, topK, topM, eps, minPts, with_dist=True, ref_order=False):
-        """Returns core (u8), degree (i32), CSR (off, idx, dist) of the
-        de-duplicated symmetric neighbourhoods of every point: sorted by id,
-        or (ref_order=True, run with one thread) in the reference's order."""
+    def topk_canon(self, P: np.ndarray, k: int) -> np.ndarray:
+        """Per-point top-k with ties at the boundary broken by the smallest
+        index (the engine's rule), rows in (value, index) order."""
+        n, nproj = P.shape
+        out = np.zeros((n, 2 * k), np.int32)
+        self.L.orc_topk_canon(_p(np.ascontiguousarray(P)), _i(n), _i(nproj), _i(k), _p(out))
+        return out
+
+    def topm_canon(self, P: np.ndarray, m: int) -> np.ndarray:
+        """Per-vector top-m with the engine's smallest-index tie rule."""
+        n, nproj = P.shape
+        out = np.zeros((nproj, 2 * m), np.int32)
+        self.L.orc_topm_canon(_p(np.ascontiguousarray(P)), _i(n), _i(nproj), _i(m), _p(out))
+        return out
+
+    def core_cluster_lean(self, Xt, dist, topK, topM, eps, minPts):
+        """Core flags, neighbourhood sizes, labels and n_clusters_ of
+        find_core + form_cluster, through the oracle's lock-free large-n
+        restatement.  Returns (core, degree, labels, n_clusters)."""
         n, d = Xt.shape
         k = topK.shape[1] // 2
         m = topM.shape[1] // 2
         core = np.zeros(n, np.uint8)
         deg = np.zeros(n, np.int32)
-        self.L.orc_find_core(_p(Xt), _i(n), _i(d), _i(DIST_CODES[dist]), _p(np.ascontiguousarray(topK)), _i(k),
-                             _p(np.ascontiguousarray(topM)), _i(m), _f(eps), _i(minPts), _i(1 if with_dist else 0),
-                             _i(1 if ref_order else 0), _p(core), _p(deg))
+        labels = np.zeros(n, np.int32)
+        ncl = self.L.orc_core_cluster_lean(_p(np.ascontiguousarray(Xt, np.float32)), _i(n), _i(d),
+                                           _i(DIST_CODES[dist]), _p(np.ascontiguousarray(topK, np.int32)), _i(k),
+                                           _p(np.ascontiguousarray(topM, np.int32)), _i(m), _f(eps), _i(minPts),
+                                           _p(core), _p(deg), _p(labels))
+        return core, deg, labels, int(ncl)
+
+    def find_core(self, Xt, dist, topK, topM, eps, minPts, with_dist=True, ref_order=False, lean=False):
+        """Returns core (u8), degree (i32), CSR (off, idx, dist) of the
+        de-duplicated symmetric neighbourhoods of every point: sorted by id,
+        or (ref_order=True, run with one thread) in the reference's order.
+        lean=True builds the same sorted graph through the large-n
+        construction (orc_find_core_lean)."""
+        n, d = Xt.shape
+        k = topK.shape[1] // 2
+        m = topM.shape[1] // 2
+        core = np.zeros(n, np.uint8)
+        deg = np.zeros(n, np.int32)
+        Xt = np.ascontiguousarray(Xt, np.float32)
+        if lean:
+            assert not ref_order
+            self.L.orc_find_core_lean(_p(Xt), _i(n), _i(d), _i(DIST_CODES[dist]),
+                                      _p(np.ascontiguousarray(topK, np.int32)), _i(k),
+                                      _p(np.ascontiguousarray(topM, np.int32)), _i(m), _f(eps), _i(minPts),
+                                      _i(1 if with_dist else 0), _p(core), _p(deg))
+        else:
+            self.L.orc_find_core(_p(Xt), _i(n), _i(d), _i(DIST_CODES[dist]), _p(np.ascontiguousarray(topK)), _i(k),
+                                 _p(np.ascontiguousarray(topM)), _i(m), _f(eps), _i(minPts), _i(1 if with_dist else 0),
+                                 _i(1 if ref_order else 0), _p(core), _p(deg))
         tot = self.L.orc_neighbors_total(_i(n))
         off = np.zeros(n + 1, np.int64)
         idx = np.zeros(tot, np.int32)

@@ -335,6 +335,68 @@ void orc_topm(const float* P, int n, int nproj, int m, int* topM) {
     }
 }
 
+// ---- canonical tie rule for the selections ----------------------------------
+// The reference's heaps (strict `>` replacement, src/sDbscan.cpp:115, :127,
+// :178, :190) keep, among values equal to the k-th, the ones that the heap's
+// internal order leaves in it.  The GPU engine keeps the smallest indices
+// instead.  These two selections state that rule: the k largest by (value
+// desc, index asc) (and the k smallest by (value asc, index asc) for the far
+// side).  Where no boundary tie occurs they equal orc_topk / orc_topm as
+// sets; where one does they are the engine's sets, so a whole fit can be
+// checked bit for bit through the tie.  Rows are written in (value, index)
+// order: row 0 is the most extreme.
+extern "C++" {
+namespace {
+// "a ranks above b" for the close side: larger value, then smaller index.
+inline bool ranks_above(float av, int ai, float bv, int bi) { return av > bv || (av == bv && ai < bi); }
+struct WorstOnTop {  // heap top = the lowest-ranked kept entry
+    bool operator()(const ValIdx& a, const ValIdx& b) const { return ranks_above(a.v, a.i, b.v, b.i); }
+};
+typedef std::priority_queue<ValIdx, std::vector<ValIdx>, WorstOnTop> CanonHeap;
+inline void canon_offer(CanonHeap& h, int k, int idx, float v) {
+    if ((int)h.size() < k) h.push({v, idx});
+    else if (ranks_above(v, idx, h.top().v, h.top().i)) {
+        h.pop();
+        h.push({v, idx});
+    }
+}
+inline void canon_drain(CanonHeap& h, int k, int* out) {
+    for (int j = k - 1; j >= 0; --j) {
+        out[j] = h.top().i;
+        h.pop();
+    }
+}
+}  // namespace
+}  // extern "C++"
+
+void orc_topk_canon(const float* P, int n, int nproj, int k, int* topK) {
+#pragma omp parallel for
+    for (int p = 0; p < n; ++p) {
+        CanonHeap close, far;
+        const float* v = P + (size_t)p * nproj;
+        for (int r = 0; r < nproj; ++r) {
+            canon_offer(close, k, r, v[r]);
+            canon_offer(far, k, r, -v[r]);
+        }
+        canon_drain(close, k, topK + (size_t)p * 2 * k);
+        canon_drain(far, k, topK + (size_t)p * 2 * k + k);
+    }
+}
+
+void orc_topm_canon(const float* P, int n, int nproj, int m, int* topM) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int r = 0; r < nproj; ++r) {
+        CanonHeap close, far;
+        for (int p = 0; p < n; ++p) {
+            const float v = P[(size_t)p * nproj + r];
+            canon_offer(close, m, p, v);
+            canon_offer(far, m, p, -v);
+        }
+        canon_drain(close, m, topM + (size_t)r * 2 * m);
+        canon_drain(far, m, topM + (size_t)r * 2 * m + m);
+    }
+}
+
 // ---- core points (src/sDbscan.cpp:217-408) -----------------------------------
 // Computes, for every point, its de-duplicated symmetric eps-neighbourhood
 // (own candidates within eps, plus every point that found it as a candidate
@@ -468,6 +530,309 @@ int orc_form_cluster(int n, const uint8_t* core, const int64_t* off, const int32
         ncl = id;
     }
     return ncl + 2;
+}
+
+// ---- core points + clusters for large n (src/sDbscan.cpp:217-408, 509-637) ---
+// The neighbourhood sizes, core flags, labels and n_clusters_ of orc_find_core
+// followed by orc_form_cluster, computed without the global lock and the
+// per-pair pushes of the reference's loop, so a million-point fit checks in a
+// minute or two of host time and a few GB of memory:
+//  - every candidate distance of point p through list (r, side) -- top-m
+//    member q of a random vector in p's top-k (:262-283) -- is evaluated list
+//    by list: the list's m rows are held transposed in cache and each of its
+//    member points is compared with all of them, leaving one pass bit per
+//    (p, slot, candidate) (dist <= eps, :286);
+//  - A(p): the distinct candidates of p whose bit is set, self skipped
+//    (:272-277), sorted.  A candidate met through two lists has the same
+//    distance both times, so evaluating it twice changes nothing;
+//  - B(q): every p with q in A(p), i.e. the reverse insertions of :293-294
+//    (a counted CSR: only top-m members ever receive one), sorted;
+//  - N(p) = A(p) u B(p): |N(p)| is the degree, core iff >= minPts - 1 (:382);
+//  - formCluster (:509-637): for p ascending, an unlabelled core point opens
+//    the next id and a flood through core points labels every point it
+//    reaches that is still -1.
+// Distances follow the numerical contract: each one is a sequential chain
+// over ascending dimension (fmaf for Cosine / L2, adds for L1 and Chi2); the
+// chains of a block of 16 candidates run side by side in SIMD lanes, which
+// changes no bits.  JS uses the scalar distance().  Returns n_clusters_.
+extern "C++" {
+namespace {
+constexpr int kLeanBlk = 16;
+// Eight lanes of float, GCC's generic vectors (SIMD on x86-64 and aarch64;
+// every lane op is the IEEE scalar op).
+typedef float f8 __attribute__((vector_size(32)));
+typedef int i8 __attribute__((vector_size(32)));
+template <int CODE>
+void block_dist(const float* x, const float* Ct, int d, float* out) {
+    if (CODE == D_COSINE || CODE == D_L2) {
+        float s[kLeanBlk];
+        for (int j = 0; j < kLeanBlk; ++j) s[j] = 0.0f;
+        for (int i = 0; i < d; ++i) {
+            const float a = x[i];
+            const float* c = Ct + (size_t)i * kLeanBlk;
+            for (int j = 0; j < kLeanBlk; ++j) {
+                if (CODE == D_COSINE) {
+                    s[j] = std::fma(a, c[j], s[j]);
+                } else {
+                    const float t = a - c[j];
+                    s[j] = std::fma(t, t, s[j]);
+                }
+            }
+        }
+        for (int j = 0; j < kLeanBlk; ++j) out[j] = CODE == D_COSINE ? 1 - s[j] : std::sqrt(s[j]);
+        return;
+    }
+    static_assert(kLeanBlk == 16, "two f8 lanes per block");
+    f8 s0 = {}, s1 = {};
+    const f8 zero = {};
+    for (int i = 0; i < d; ++i) {
+        const f8 a = zero + x[i];
+        f8 b0, b1;
+        std::memcpy(&b0, Ct + (size_t)i * kLeanBlk, sizeof(f8));
+        std::memcpy(&b1, Ct + (size_t)i * kLeanBlk + 8, sizeof(f8));
+        if (CODE == D_L1) {
+            const f8 t0 = a - b0, t1 = a - b1;
+            s0 = s0 + (t0 < zero ? -t0 : t0);  // |a - b|
+            s1 = s1 + (t1 < zero ? -t1 : t1);
+        } else {  // Chi2: only entries where both are > 0 contribute (Utilities.h:235-241)
+            const f8 q0 = (a * b0) / (a + b0), q1 = (a * b1) / (a + b1);
+            const i8 ok0 = (a > zero) & (b0 > zero), ok1 = (a > zero) & (b1 > zero);
+            s0 = ok0 ? s0 + q0 : s0;
+            s1 = ok1 ? s1 + q1 : s1;
+        }
+    }
+    for (int j = 0; j < 8; ++j) {
+        out[j] = CODE == D_L1 ? s0[j] : (float)(1.0 - 2.0 * (double)s0[j]);
+        out[j + 8] = CODE == D_L1 ? s1[j] : (float)(1.0 - 2.0 * (double)s1[j]);
+    }
+}
+}  // namespace
+}  // extern "C++"
+
+namespace {
+// A(p) (ids ascending, with distances when asked) and B as a CSR, as stated
+// above.
+struct LeanGraph {
+    std::vector<std::vector<int>> A;
+    std::vector<std::vector<float>> Ad;
+    std::vector<int64_t> roff;
+    std::vector<int32_t> B;
+    std::vector<float> Bd;
+};
+
+void lean_build(const float* X, int n, int d, int code, const int* topK, int k, const int* topM, int m, float eps,
+                bool withDist, LeanGraph& g) {
+    const int S = 2 * k, W = (m + 63) / 64;
+    int D = 0;  // number of random vectors: one past the largest list id in topK
+    for (size_t t = 0; t < (size_t)n * S; ++t) D = std::max(D, topK[t] + 1);
+    // members of each list (r, side): (point, slot) pairs, points ascending
+    std::vector<int64_t> loff((size_t)2 * D + 1, 0);
+    for (int p = 0; p < n; ++p)
+        for (int sl = 0; sl < S; ++sl) loff[(size_t)(sl >= k) * D + topK[(size_t)p * S + sl] + 1] += 1;
+    for (size_t l = 0; l < (size_t)2 * D; ++l) loff[l + 1] += loff[l];
+    std::vector<int64_t> lcur(loff.begin(), loff.end() - 1);
+    std::vector<int32_t> lmem((size_t)n * S);
+    for (int p = 0; p < n; ++p)
+        for (int sl = 0; sl < S; ++sl) lmem[lcur[(size_t)(sl >= k) * D + topK[(size_t)p * S + sl]]++] = p * S + sl;
+    std::vector<uint64_t> pass((size_t)n * S * W, 0ull);
+    std::vector<float> pdist(withDist ? (size_t)n * S * m : 0);
+    const int nb = (m + kLeanBlk - 1) / kLeanBlk;
+#pragma omp parallel
+    {
+        std::vector<float> Ct((size_t)nb * d * kLeanBlk);
+        std::vector<float> dd((size_t)nb * kLeanBlk);
+#pragma omp for schedule(dynamic, 1)
+        for (int l = 0; l < 2 * D; ++l) {
+            if (loff[l + 1] == loff[l]) continue;
+            const int side = l >= D, r = l - side * D;
+            const int* cand = topM + (size_t)r * 2 * m + side * m;
+            for (int b = 0; b < nb; ++b)  // candidates transposed, padded with copies of the first
+                for (int j = 0; j < kLeanBlk; ++j) {
+                    const int c = b * kLeanBlk + j < m ? cand[b * kLeanBlk + j] : cand[0];
+                    const float* y = X + (size_t)c * d;
+                    for (int i = 0; i < d; ++i) Ct[((size_t)b * d + i) * kLeanBlk + j] = y[i];
+                }
+            for (int64_t t = loff[l]; t < loff[l + 1]; ++t) {
+                const int ps = lmem[t], p = ps / S;
+                const float* xp = X + (size_t)p * d;
+                for (int b = 0; b < nb; ++b) {
+                    const float* cb = Ct.data() + (size_t)b * d * kLeanBlk;
+                    float* o = dd.data() + (size_t)b * kLeanBlk;
+                    if (code == D_COSINE) block_dist<D_COSINE>(xp, cb, d, o);
+                    else if (code == D_L2) block_dist<D_L2>(xp, cb, d, o);
+                    else if (code == D_L1) block_dist<D_L1>(xp, cb, d, o);
+                    else if (code == D_CHI2) block_dist<D_CHI2>(xp, cb, d, o);
+                    else
+                        for (int j = 0; j < kLeanBlk && b * kLeanBlk + j < m; ++j)
+                            o[j] = distance(xp, X + (size_t)cand[b * kLeanBlk + j] * d, d, code);
+                }
+                uint64_t* w = pass.data() + (size_t)ps * W;
+                for (int i = 0; i < m; ++i)
+                    if (dd[i] <= eps) w[i >> 6] |= 1ull << (i & 63);
+                if (withDist) std::memcpy(pdist.data() + (size_t)ps * m, dd.data(), sizeof(float) * m);
+            }
+        }
+    }
+    std::vector<int32_t>().swap(lmem);
+    g.A.assign(n, {});
+    g.Ad.assign(withDist ? n : 0, {});
+#pragma omp parallel
+    {
+        std::vector<uint64_t> seen(((size_t)n + 63) / 64, 0ull);
+        std::vector<std::pair<int, float>> tmp;
+#pragma omp for schedule(dynamic, 256)
+        for (int p = 0; p < n; ++p) {
+            tmp.clear();
+            for (int sl = 0; sl < S; ++sl) {
+                const int side = sl >= k, r = topK[(size_t)p * S + sl];
+                const int* cand = topM + (size_t)r * 2 * m + side * m;
+                const uint64_t* w = pass.data() + ((size_t)p * S + sl) * W;
+                for (int i = 0; i < m; ++i) {
+                    if (!(w[i >> 6] >> (i & 63) & 1)) continue;
+                    const int q = cand[i];
+                    if (q == p || (seen[q >> 6] >> (q & 63) & 1)) continue;
+                    seen[q >> 6] |= 1ull << (q & 63);
+                    tmp.push_back({q, withDist ? pdist[((size_t)p * S + sl) * m + i] : 0.0f});
+                }
+            }
+            for (const auto& e : tmp) seen[e.first >> 6] = 0ull;
+            std::sort(tmp.begin(), tmp.end(),
+                      [](const std::pair<int, float>& a, const std::pair<int, float>& b) { return a.first < b.first; });
+            g.A[p].resize(tmp.size());
+            for (size_t t = 0; t < tmp.size(); ++t) g.A[p][t] = tmp[t].first;
+            if (withDist) {
+                g.Ad[p].resize(tmp.size());
+                for (size_t t = 0; t < tmp.size(); ++t) g.Ad[p][t] = tmp[t].second;
+            }
+        }
+    }
+    std::vector<uint64_t>().swap(pass);
+    std::vector<float>().swap(pdist);
+    // B as a CSR, filled without atomics: thread t scatters the A lists of a
+    // fixed range of p into slots counted for it, so every B(q) comes out
+    // in ascending p
+    const int T = omp_get_max_threads();
+    std::vector<std::vector<int32_t>> cnt(T);
+    g.roff.assign((size_t)n + 1, 0);
+#pragma omp parallel num_threads(T)
+    {
+        const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+        const int p0 = (int)((int64_t)n * t / nt), p1 = (int)((int64_t)n * (t + 1) / nt);
+        std::vector<int32_t>& c = cnt[t];
+        c.assign(n, 0);
+        for (int p = p0; p < p1; ++p)
+            for (int q : g.A[p]) c[q] += 1;
+#pragma omp barrier
+#pragma omp single
+        {
+            for (int q = 0; q < n; ++q) {
+                int64_t o = g.roff[q];
+                for (int u = 0; u < nt; ++u) {
+                    const int32_t v = cnt[u][q];
+                    cnt[u][q] = (int32_t)(o - g.roff[q]);  // start of thread u's run inside B(q)
+                    o += v;
+                }
+                g.roff[q + 1] = o;
+            }
+            g.B.resize((size_t)g.roff[n]);
+            if (withDist) g.Bd.resize((size_t)g.roff[n]);
+        }
+        for (int p = p0; p < p1; ++p)
+            for (size_t t2 = 0; t2 < g.A[p].size(); ++t2) {
+                const int q = g.A[p][t2];
+                const int64_t slot = g.roff[q] + c[q]++;
+                g.B[slot] = p;
+                // dist(p, q) == dist(q, p) bit for bit: every formula is symmetric
+                if (withDist) g.Bd[slot] = g.Ad[p][t2];
+            }
+    }
+}
+
+// |A(q) u B(q)| for sorted A(q), B(q).
+int32_t lean_degree(const LeanGraph& g, int q) {
+    const std::vector<int>& a = g.A[q];
+    size_t i = 0, both = 0;
+    for (int64_t t = g.roff[q]; t < g.roff[q + 1]; ++t) {
+        while (i < a.size() && a[i] < g.B[t]) ++i;
+        if (i < a.size() && a[i] == g.B[t]) ++both;
+    }
+    return (int32_t)(a.size() + (size_t)(g.roff[q + 1] - g.roff[q]) - both);
+}
+}  // namespace
+
+int orc_core_cluster_lean(const float* X, int n, int d, int code, const int* topK, int k, const int* topM, int m,
+                          float eps, int minPts, uint8_t* core, int32_t* degree, int32_t* labels) {
+    LeanGraph g;
+    lean_build(X, n, d, code, topK, k, topM, m, eps, false, g);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int q = 0; q < n; ++q) {
+        degree[q] = lean_degree(g, q);
+        core[q] = degree[q] >= minPts - 1 ? 1 : 0;
+    }
+    std::fill(labels, labels + n, -1);
+    std::vector<uint8_t> conn(n, 0);
+    std::vector<int> touched, seeds;
+    int id = -1;
+    auto visit = [&](int y) {
+        if (conn[y]) return;
+        conn[y] = 1;
+        touched.push_back(y);
+        if (core[y] && labels[y] == -1) seeds.push_back(y);
+    };
+    for (int p = 0; p < n; ++p) {
+        if (!core[p] || labels[p] != -1) continue;
+        ++id;
+        seeds.assign(1, p);
+        touched.assign(1, p);
+        conn[p] = 1;
+        while (!seeds.empty()) {
+            const int x = seeds.back();
+            seeds.pop_back();
+            for (int y : g.A[x]) visit(y);
+            for (int64_t t = g.roff[x]; t < g.roff[x + 1]; ++t) visit(g.B[t]);
+        }
+        for (int y : touched) {
+            if (labels[y] == -1) labels[y] = id;
+            conn[y] = 0;
+        }
+    }
+    return id >= 0 ? id + 2 : 2;  // n_clusters_ = last id + 2, and 2 with no cluster (:633)
+}
+
+// orc_find_core (ref_order = 0) through the large-n construction: the same
+// core flags and sizes, and the same neighbour graph (ids ascending, with
+// distances when with_dist) for orc_core_dist / orc_neighbors_export.
+void orc_find_core_lean(const float* X, int n, int d, int code, const int* topK, int k, const int* topM, int m,
+                        float eps, int minPts, int with_dist, uint8_t* core, int32_t* degree) {
+    LeanGraph g;
+    lean_build(X, n, d, code, topK, k, topM, m, eps, with_dist != 0, g);
+    g_graph.nb.assign(n, {});
+    g_graph.nd.assign(n, {});
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int q = 0; q < n; ++q) {
+        const std::vector<int>& a = g.A[q];
+        std::vector<int>& o = g_graph.nb[q];
+        std::vector<float>& od = g_graph.nd[q];
+        size_t i = 0;
+        int64_t t = g.roff[q];
+        const int64_t te = g.roff[q + 1];
+        while (i < a.size() || t < te) {  // merge of two ascending lists, equal ids once
+            const bool takeA = t == te || (i < a.size() && a[i] <= g.B[t]);
+            if (takeA) {
+                const bool dup = t < te && a[i] == g.B[t];
+                o.push_back(a[i]);
+                if (with_dist) od.push_back(g.Ad[q][i]);
+                ++i;
+                if (dup) ++t;
+            } else {
+                o.push_back(g.B[t]);
+                if (with_dist) od.push_back(g.Bd[t]);
+                ++t;
+            }
+        }
+        degree[q] = (int32_t)o.size();
+        core[q] = (int)o.size() >= minPts - 1 ? 1 : 0;
+    }
 }
 
 // ---- core distance (src/sDbscan.cpp:1424-1460) -------------------------------

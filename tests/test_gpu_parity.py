@@ -50,8 +50,34 @@ def _rows_equal_as_sets(a, b):
 DBSCAN_FIXTURES = [p for p in GOLDEN if not _fixture(p)[1]["optics"]]
 
 
+def _oracle_canonical(port, X, meta):
+    """The oracle's fit of a fixture with the engine's tie rule at the top-k /
+    top-m boundaries (smallest index kept): top-k, top-m, core flags,
+    neighbourhood sizes, labels (with sDbscan-1NN when the fixture asks for
+    it) and n_clusters_."""
+    from oracle.oracle import fht_dim
+    n, d = X.shape
+    dist = meta["distance"]
+    ker = d if dist == "Cosine" else meta.get("ker_n_features", 1024)
+    fd = fht_dim(meta["n_proj"], ker)
+    bits = port.hd3_bits(3 * fd, meta["random_seed"])
+    R = port._R(dist, ker, d, meta.get("ker_sigma", 1.0), meta["random_seed"])
+    Xt, rc = port.transform(X, dist)
+    assert rc == 0
+    P = port.project(Xt, dist, ker, 0.4, R, bits, fd, meta["n_proj"])
+    tK, tM = port.topk_canon(P, meta["topK"]), port.topm_canon(P, meta["topM"])
+    core, deg, labels, ncl = port.core_cluster_lean(Xt, dist, tK, tM, meta["eps"], meta["minPts"])
+    if meta.get("clusterNoise", 0) == 1:
+        labels = port.label_noise(P, tK, core, labels, meta.get("samplingProb", 0.01), meta["random_seed"])
+    return tK, tM, core, deg, labels, ncl
+
+
+def _sorted_rows(a):
+    return np.sort(np.asarray(a), axis=1)
+
+
 @pytest.mark.parametrize("path", DBSCAN_FIXTURES, ids=[os.path.basename(p)[:-4] for p in DBSCAN_FIXTURES])
-def test_fit_sdbscan_matches_reference(path):
+def test_fit_sdbscan_matches_reference(port, path):
     z, meta = _fixture(path)
     X = z["X"]
     eng = _engine(X, meta)
@@ -76,6 +102,15 @@ def test_fit_sdbscan_matches_reference(path):
         assert _rows_equal_as_sets(topK, z["topK"])
     if exact and c["topm_ties"] == 0:
         assert _rows_equal_as_sets(topM, z["topM"])
+    if exact:
+        # bit-exact against the oracle with the engine's tie rule, ties or not
+        oK, oM, ocore, odeg, olabels, oncl = _oracle_canonical(port, X, meta)
+        np.testing.assert_array_equal(_sorted_rows(topK), _sorted_rows(oK))
+        np.testing.assert_array_equal(_sorted_rows(topM), _sorted_rows(oM))
+        np.testing.assert_array_equal(core, ocore)
+        np.testing.assert_array_equal(deg, odeg)
+        np.testing.assert_array_equal(labels, olabels)
+        assert ncl == oncl
     if exact and c["topk_ties"] == 0 and c["topm_ties"] == 0:
         np.testing.assert_array_equal(core, z["core"])
         np.testing.assert_array_equal(deg[core == 1], z["core_degree"][core == 1])
