@@ -264,6 +264,34 @@ def run_reference(args, cfg):
     return 0
 
 
+def run_cpu_full_fit(args, cfg):
+    """One fit of the whole workload (all n points) by the CPU restatement of
+    the reference (the reference arm's code, timing mode, all host threads):
+    the same-config CPU figure beside the sampled per-step rate.  The data is
+    the GPU arm's (the config's law drawn with torch, on the GPU when there is
+    one, then copied to the host).  Prints one JSON line."""
+    import torch
+    from sdbscan_gb300 import datasets
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    if cfg["workload"].startswith("cfg2"):
+        X, _ = datasets.cfg2_mnist_like_torch(cfg["n"], cfg["d"], seed=cfg["seed"], device=dev)
+        Xh = X.cpu().numpy()
+        del X
+    else:
+        Xh = _host_data(cfg, cfg["n"])
+    if dev == "cuda":
+        torch.cuda.empty_cache()
+    kp = _kernel_params(cfg, Xh) if cfg["distance"] not in ("L1", "L2") else {
+        "ker_n_features": cfg["ker_n_features"], "ker_sigma": _np_median_pair(Xh[:2000])}
+    rate, threads, dt = _cpu_sample_rate(Xh, cfg, cfg["n"], kp)
+    print(json.dumps({"impl": "reference", "cpu_full_fit": {
+        "workload": cfg["workload"], "n": cfg["n"], "seconds": dt, "value": rate, "unit": "points/s",
+        "cores": threads, "kind": "port",
+        "form": f"one full fit_{'sOptics' if cfg['fit'] == 'soptics' else 'sDbscan'} of the whole workload "
+                f"(oracle/ restatement of the reference's loop, vectorised distances, OpenMP)"}}))
+    return 0
+
+
 def run_batched(args, local, cpu=True):
     """Config 5: 64 vMF mixtures (n log-uniform 2K..200K, d in {64,128,256}),
     an 8-value eps sweep each (0.05 .. 0.40), minPts 20, D 1024, k 5, m 50.
@@ -707,6 +735,8 @@ def run_single_fit(args):
     else:
         kw = dict(ker_n_features=1024, ker_sigma=1.0) if dist != "Cosine" else {}
         eng.set_params(n_proj=1024, topK=10, topM=50, distance=dist, random_seed=42, precision=args.precision, **kw)
+        if args.tile_variant:
+            eng.set_tile_variant(args.tile_variant)
         if args.fit == "soptics":
             eng.fit_soptics_device(X.data_ptr(), 0.25, 50)
         else:
@@ -731,6 +761,8 @@ def main():
     ap.add_argument("--batched-cpu", action="store_true", help="(reference arm) time the config-5 CPU baseline only")
     ap.add_argument("--no-sng", action="store_true")
     ap.add_argument("--sng-cpu", action="store_true", help="(reference arm) time the sngDbscan CPU baseline only")
+    ap.add_argument("--cpu-full-fit", action="store_true",
+                    help="(reference arm) one CPU fit of the whole workload, timed (minutes at 1M points)")
     ap.add_argument("--single-fit", type=int, default=0, metavar="N",
                     help="one fit of N points of the config-2 law, stage times printed (for profilers)")
     ap.add_argument("--fit", default="sdbscan", choices=["sdbscan", "soptics", "sng"])
@@ -738,6 +770,7 @@ def main():
     ap.add_argument("--d", type=int, default=784, help="dimensions (with --single-fit)")
     ap.add_argument("--distance", default="Cosine", help="distance (with --single-fit)")
     ap.add_argument("--prob", type=float, default=0.01, help="sngDbscan samplingProb (with --single-fit --fit sng)")
+    ap.add_argument("--tile-variant", type=int, default=0, help="plain distance tile shape (with --single-fit)")
     args = ap.parse_args()
     if args.single_fit:
         return run_single_fit(args)
@@ -745,6 +778,8 @@ def main():
     if args.impl == "reference" and args.batched_cpu:
         print(json.dumps(_cpu_batched()))
         return 0
+    if args.impl == "reference" and args.cpu_full_fit:
+        return run_cpu_full_fit(args, cfg)
     if args.impl == "reference" and args.sng_cpu:
         print(json.dumps(_cpu_sng(cfg)))
         return 0

@@ -96,12 +96,35 @@ sdb_status sdb_set_params(sdb_engine* e, const sdb_params* p);
  * counterpart (the reference computes in FP32 only). */
 sdb_status sdb_set_precision(sdb_engine* e, int32_t precision);
 
+/* Test and diagnostic limits (no reference counterpart; each 0 = off, the
+ * default).  They let the failure paths run without a GPU fault:
+ *   stall_spins      > 0: each tensor-core kernel (BF16 distance screening,
+ *                    BF16 random-Fourier embedding, BF16 sngDbscan block) and
+ *                    the persistent plain distance kernel waits once per launch
+ *                    on a barrier that nothing completes, and gives up after
+ *                    this many polls; the kernel then takes its failure path:
+ *                    its roles stop, it waits for its own copies and MMAs, and
+ *                    it raises its flag.  The BF16 stages then run their FP32
+ *                    kernels (same results; sdb_get_counters out[5] counts
+ *                    them); the persistent plain kernel (sdb_set_tile_variant
+ *                    4, 5) fails the fit with SDB_ERR_INTERNAL.
+ *   queue_cap        > 0: the BF16 re-decision queues hold at most this many
+ *                    pairs; an overflow sends the stage to its FP32 kernel.
+ *   device_bytes_cap > 0: the engine's device memory stays below this; a fit
+ *                    that needs more returns SDB_ERR_NOMEM and the engine
+ *                    stays usable.
+ * Negative values return SDB_ERR_ARG. */
+sdb_status sdb_set_debug_limits(sdb_engine* e, int64_t stall_spins, int64_t queue_cap, int64_t device_bytes_cap);
+
 /* Tile shape of the plain FP32 distance kernel (a tuning control; no
  * reference counterpart): 0 = by topM and distance (default: for topM in
  * 41..50 shape 3 with Cosine, shape 2 otherwise; else 1), 1 = 128 x 64 tiles on 256 threads, 2 = 128 x 50 on 160 threads
  * (32 dimensions per stage, 2 stages), 3 = 128 x 50 with 16 dimensions per
- * stage in 4 stages (Cosine; shape 2 for the other distances).  The 50-column shapes apply when topM <= 50 (else shape
- * 1).  Any shape gives the same bits. */
+ * stage in 4 stages (Cosine; shape 2 for the other distances), 4 and 5 = the
+ * persistent warp-specialised kernel (a producer warp gathers the rows, the
+ * other warps compute; 4 stages and 3 CTAs per SM, or 6 stages and 2).  The
+ * 50-column shapes apply when topM <= 50 (else the 64-column ones).  Any shape
+ * gives the same bits. */
 sdb_status sdb_set_tile_variant(sdb_engine* e, int32_t variant);
 
 /* fit_sDbscan(const Ref<const MatrixXf>& X, float eps, int minPts)
@@ -149,13 +172,27 @@ sdb_status sdb_fit_sdbscan_sweep(sdb_engine* e, const float* X_host, const float
 sdb_status sdb_set_sng_params(sdb_engine* e, int32_t distance, float samplingProb, int32_t clusterNoise,
                               int32_t verbose, int32_t n_threads, int32_t random_seed);
 
+/* How fit_sngDbscan draws its samples (no reference counterpart; the
+ * reference's rule depends on the seed, src/sDbscan.cpp:437-440):
+ *   0 (default) by the seed: random_seed >= 0 -> 1, random_seed < 0 -> 2;
+ *   1 shared: every point draws the same sequence from random_seed, which is
+ *     the reference's own behaviour for a fixed seed (identical labels);
+ *   2 blocks: each block of 32 consecutive points draws its own S columns
+ *     (draw j of block b from splitmix64 of the seed, b and j), so that every
+ *     point has S forward and about S reverse draws, as when the reference's
+ *     points seed their generators apart (random_seed < 0); the seed is
+ *     random_seed, or the clock when < 0.  FP32 distances (BF16 precision
+ *     does not apply).  samplingProb >= 1 is exact DBSCAN in every mode. */
+sdb_status sdb_set_sng_sampling(sdb_engine* e, int32_t mode);
+
 /* fit_sngDbscan(X, eps, minPts)  (src/sDbscan.h:190, src/sDbscan.cpp:1131-1179):
  * each point's neighbourhood from ceil(n samplingProb) random draws (both
  * directions of every draw within eps), core points with >= minPts - 1
  * neighbours counted with repeats, clusters as fit_sDbscan; samplingProb >= 1
  * is exact DBSCAN.  With random_seed >= 0 the labels equal the reference's
- * (every point's generator is seeded alike); with random_seed < 0 one clock
- * seed is shared by all points.  Switches clusterNoise to 0 (src/sDbscan.cpp:1157).
+ * (every point's generator is seeded alike); with random_seed < 0 the sample
+ * is drawn per block of points (sdb_set_sng_sampling).  Switches clusterNoise
+ * to 0 (src/sDbscan.cpp:1157).
  * Results: sdb_get_labels, sdb_get_core (neighbourhood sizes with repeats). */
 sdb_status sdb_fit_sngdbscan(sdb_engine* e, const float* X_host, float eps, int32_t minPts);
 /* (With SDB_PREC_BF16 and Cosine the distance block is screened on the tensor

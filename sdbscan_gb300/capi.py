@@ -27,7 +27,7 @@ EXPORTS = ["sdb_params_default", "sdb_engine_create", "sdb_engine_destroy", "sdb
            "sdb_batch_destroy", "sdb_batch_last_error", "sdb_load_txt",
            "sdb_batch_tile_variant", "sdb_set_sng_params", "sdb_fit_sngdbscan", "sdb_fit_sngdbscan_device",
            "sdb_fit_sngdbscan_sweep", "sdb_fit_sngoptics", "sdb_fit_sngoptics_device", "sdb_set_precision",
-           "sdb_set_tile_variant"]
+           "sdb_set_tile_variant", "sdb_set_debug_limits", "sdb_set_sng_sampling"]
 
 
 class SdbParams(ctypes.Structure):
@@ -82,6 +82,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.sdb_set_sng_params.argtypes = [vp, i32, f32, i32, i32, i32, i32]
     L.sdb_set_precision.argtypes = [vp, i32]
     L.sdb_set_tile_variant.argtypes = [vp, i32]
+    L.sdb_set_debug_limits.argtypes = [vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]
+    L.sdb_set_sng_sampling.argtypes = [vp, i32]
     L.sdb_batch_create.argtypes = [i32, vp, vp, vp, ctypes.POINTER(SdbParams), vp, i32, i32, i32,
                                    ctypes.POINTER(vp)]
     L.sdb_batch_run.argtypes = [vp, ctypes.POINTER(f32)]
@@ -189,6 +191,14 @@ class Engine:
     def set_tile_variant(self, variant: int):
         """Tile shape of the plain FP32 distance kernel (0 = by topM; see the header)."""
         self._check(self.L.sdb_set_tile_variant(self.h, variant))
+
+    def set_sng_sampling(self, mode: int):
+        """sdb_set_sng_sampling: 0 by seed, 1 shared sample, 2 per-block samples."""
+        self._check(self.L.sdb_set_sng_sampling(self.h, mode))
+
+    def set_debug_limits(self, stall_spins: int = 0, queue_cap: int = 0, device_bytes_cap: int = 0):
+        """sdb_set_debug_limits: the failure-path test controls (0 = off)."""
+        self._check(self.L.sdb_set_debug_limits(self.h, stall_spins, queue_cap, device_bytes_cap))
 
     def fit_sngdbscan(self, X: np.ndarray, eps: float, minPts: int):
         X = self._host(X)

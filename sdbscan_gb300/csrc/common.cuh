@@ -163,7 +163,9 @@ int launch_rff(const float* Xt, int ld, int n, int d, const float* R, int h, flo
 // BF16 mode: the same embedding on the tensor cores from split-BF16 copies
 // ([hi | lo] per row) of the points (n x 2 ldb) and of R (h x 2 ldb); err set
 // on a timed-out wait.
-int launch_rff_tc(const void* Xb, const void* Rb, int n, int h, int ldb, float* E, int32_t* err, cudaStream_t st);
+// stallSpins > 0: the stall test (sdb_set_debug_limits).
+int launch_rff_tc(const void* Xb, const void* Rb, int n, int h, int ldb, float* E, int32_t* err, long long stallSpins,
+                  cudaStream_t st);
 
 struct TopMArgs {
     const float* P;
@@ -220,6 +222,12 @@ int launch_index_count(const IndexArgs& a, cudaStream_t st);
 int launch_index_scatter(const IndexArgs& a, cudaStream_t st);
 // tilePerm: the tiles sorted by the chunk of their first member.
 int launch_tile_order(const IndexArgs& a, cudaStream_t st);
+// tilePerm for the tensor-core distance kernel: tiles by (super-chunk of
+// superChunk point chunks, list); keys: total tiles, keyOff:
+// tile_order_list_keys() entries (scanTmp must cover that many).
+size_t tile_order_list_keys(const IndexArgs& a, int superChunk);
+int launch_tile_order_list(const IndexArgs& a, int superChunk, int32_t* keys, int64_t* keyOff, int32_t* perm,
+                           cudaStream_t st);
 // Tile id of the b-th launched tile (identity without a permutation).
 __device__ __forceinline__ int64_t tile_at(const int32_t* perm, int64_t b) { return perm != nullptr ? perm[b] : b; }
 int launch_tiles(const IndexArgs& a, int64_t total_tiles, cudaStream_t st);
@@ -250,11 +258,15 @@ struct DistArgs {
     unsigned long long* pairs;  // pass counter
     const int32_t* topKmat;     // n x 2k (the re-decision kernel maps slots back to lists)
     const int32_t* gate;        // optional: k_dist runs only if *gate != 0 (screening failed)
+    int32_t* waitErr;           // set by the persistent plain kernel when a bounded wait ran out
+    long long stallSpins;       // > 0: the stall test (sdb_set_debug_limits)
     int nSweep;                 // BF16 sweep: eps values whose margins are re-decided exactly
     float sweepEps[16];
 };
 constexpr int kMaxScreenedSweep = 16;
 int launch_dist(const DistArgs& a, cudaStream_t st);
+// The persistent warp-specialised plain kernel (k_dist_ws.cu): variant 4 or 5.
+int launch_dist_ws(const DistArgs& a, int variant, cudaStream_t st);
 int launch_masks_from_dists(const DistArgs& a, cudaStream_t st);
 // Eps sweeps: each pair's round (index of the first of the nSweep ascending
 // sweepEps values >= its distance; nSweep when none; 255 for the point's own
@@ -263,8 +275,10 @@ int launch_pair_rounds(const DistArgs& a, uint8_t* rounds, cudaStream_t st);
 int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream_t st);
 int launch_to_bf16_split(const float* Xt, int ld, int n, void* Xs, int ldb, cudaStream_t st);
 int launch_screen_reset(const DistArgs& a, cudaStream_t st);
-int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, uint64_t* queue, int64_t qcap,
-                   unsigned long long* qcount, int32_t* err, int grid, cudaStream_t st);
+// BF16 screening: Cb (dist_tc_cand_bytes) receives the lists' candidate rows.
+size_t dist_tc_cand_bytes(const DistArgs& a, int ldb);
+int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, void* Cb, uint64_t* queue, int64_t qcap,
+                   unsigned long long* qcount, int32_t* err, cudaStream_t st);
 int launch_recheck(const DistArgs& a, const uint64_t* queue, const unsigned long long* qcount, int64_t qcap,
                    cudaStream_t st);
 
@@ -362,6 +376,7 @@ struct SngArgs {
     float* nbDist;
     int32_t* err;          // set when a list would overflow its slots
     const uint64_t* heavy; // nct words: bit set for the columns drawn more than once (null: none)
+    long long stallSpins;  // > 0: the stall test of k_sng_tc (sdb_set_debug_limits)
 };
 // First block pass: pass bits (mask may be null), row degrees, column counts.
 int launch_sng_block(const SngArgs& a, cudaStream_t st);
@@ -384,6 +399,38 @@ int launch_sng_degree(const SngArgs& a, int exact, int optics, int minPts, int32
 int launch_sng_union(const SngArgs& a, const uint8_t* core, int32_t* parent, cudaStream_t st);
 int launch_sng_border(const SngArgs& a, const uint8_t* core, const int32_t* parent, int32_t* border,
                       cudaStream_t st);
+
+// sngDbscan with independent samples per block of sng_block_rows() points
+// (k_sng_blocks.cu): draw j of block b is the point
+// floor(hi32(splitmix64(key + b S + j)) n / 2^32), key = splitmix64(seed).
+struct SngBlockArgs {
+    const float* Xt;
+    int ld, d, dist, n;
+    int64_t S;             // draws per block
+    uint64_t key;
+    float eps;
+    uint32_t* words;       // blocks x S pass words (bit i: point 32 b + i)
+    int32_t* degree;       // n, zeroed by the caller: passes with repeats, both sides
+    unsigned long long* pairs;
+    // sngOptics: per-point open-addressing tables of distinct neighbours
+    const int64_t* hashOff;  // n + 1
+    int32_t* hashId;         // -1 = empty
+    float* hashDist;
+    int32_t* err;            // set if a table overflows (cannot happen by construction)
+};
+int sng_block_rows();
+// pass words, degrees and core flags
+int launch_sngb_pass(const SngBlockArgs& a, int minPts, uint8_t* core, cudaStream_t st);
+int launch_sngb_union(const SngBlockArgs& a, const uint8_t* core, int32_t* parent, cudaStream_t st);
+int launch_sngb_border(const SngBlockArgs& a, const uint8_t* core, const int32_t* parent, int32_t* border,
+                       cudaStream_t st);
+// sngOptics under the same rule: table sizes (n + 1 entries into cap) from
+// the pass's degrees, the emitting pass, distinct counts + core flags, and the
+// tables compacted into CSR lists.
+int launch_sngb_caps(const SngBlockArgs& a, int64_t* cap, cudaStream_t st);
+int launch_sngb_emit(const SngBlockArgs& a, cudaStream_t st);
+int launch_sngb_distinct(const SngBlockArgs& a, int minPts, int32_t* distinct, uint8_t* core, cudaStream_t st);
+int launch_sngb_compact(const SngBlockArgs& a, const int64_t* nbOff, int32_t* nbIdx, float* nbDist, cudaStream_t st);
 
 // sDbscan-1NN noise labelling (clusterNoise = 1), after the cluster labels.
 struct NoiseArgs {

@@ -40,6 +40,14 @@ using namespace sdb;
 
 namespace {
 
+// Point chunks per super-chunk of the tensor-core distance kernel's tile order
+// (launch_tile_order_list), and the key count of that order's counting sort.
+constexpr int kSuperChunk = 8;
+size_t kTcKeys(int n, int L) {
+    const int nChunks = (n + 4095) / 4096;
+    return (size_t)((nChunks + kSuperChunk - 1) / kSuperChunk) * L + 1;
+}
+
 const char* dist_name(int d) {
     switch (d) {
         case SDB_COSINE: return "Cosine";
@@ -59,7 +67,13 @@ const char* dist_name(int d) {
 bool sdb_engine::ensure(DevBuf& b, size_t bytes) {
     if (bytes == 0) bytes = 16;
     if (b.bytes >= bytes) return true;
+    if (dbgDeviceCap > 0 && devBytes - b.bytes + bytes > dbgDeviceCap) {
+        fail(SDB_ERR_NOMEM, std::string("device allocation of ") + std::to_string(bytes) +
+                                " bytes is over the engine's device memory cap of " + std::to_string(dbgDeviceCap));
+        return false;
+    }
     if (b.ptr) cudaFree(b.ptr);
+    devBytes -= b.bytes;
     b.ptr = nullptr;
     b.bytes = 0;
     cudaError_t e = cudaMalloc(&b.ptr, bytes);
@@ -70,6 +84,7 @@ bool sdb_engine::ensure(DevBuf& b, size_t bytes) {
         return false;
     }
     b.bytes = bytes;
+    devBytes += bytes;
     return true;
 }
 
@@ -89,6 +104,7 @@ void sdb_engine::free_all() {
             b->ptr = nullptr;
             b->bytes = 0;
         }
+    devBytes = 0;
 }
 
 std::vector<DevBuf*> sdb_engine::all_bufs() {
@@ -98,7 +114,8 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
             &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig, &Rb, &newMasks, &coreEps, &sampleFlag,
             &noiseFlag, &noiseCores, &noisePts, &PcT, &numCore, &pairRound, &sngCols, &sngMult, &sngColOf, &sngExtras,
-            &sngExtraPass, &sngMask, &rowDeg, &colCnt, &sngUb, &sngHeavy, &chunkOff, &tileKey, &keyOff, &tilePerm};
+            &sngExtraPass, &sngMask, &rowDeg, &colCnt, &sngUb, &sngHeavy, &chunkOff, &tileKey, &keyOff, &tilePerm, &Cb, &tileKeyTc, &keyOffTc, &tilePermTc, &sngWords, &hashOffB, &hashIdB,
+            &hashDistB};
 }
 
 // ---------------------------------------------------------------------------
@@ -196,10 +213,10 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     const int nct = (m + TNc - 1) / TNc;
     const int W = (m + 63) / 64;
     const int L = 2 * D;
-    // top-m threshold chunks: a full wave of projection blocks (4 per SM) for
-    // each upload segment, and at least 4m chunks so the chunk maxima bound
-    // the m-th value
-    const int chunksWanted = std::max(sm_count() * 4 * kUploadSegs, 4 * m);
+    // top-m threshold chunks: eight full waves of projection blocks (4 per
+    // SM; half a wave per upload segment), and at least 4m chunks so the
+    // chunk maxima bound the m-th value
+    const int chunksWanted = std::max(sm_count() * 4 * 8, 4 * m);
     const int chunk = std::max(8, (n + chunksWanted - 1) / chunksWanted);
     const int G = (n + chunk - 1) / chunk;
     int cap = 256;
@@ -226,8 +243,9 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
           ensure(parent, sizeof(int32_t) * n) && ensure(border, sizeof(int32_t) * n) &&
           ensure(rootFlag, sizeof(int64_t) * (n + 1)) && ensure(labels, sizeof(int32_t) * n) &&
           ensure(nClusters, sizeof(int32_t) * 4) &&
-          ensure(scanTmp, sizeof(int64_t) * scan_tmp_elems((size_t)std::max(n + 1, L + 1))) &&
-          ensure(errFlags, sizeof(int32_t) * 8) && ensure(counters, sizeof(unsigned long long) * 8) &&
+          ensure(scanTmp, sizeof(int64_t) * scan_tmp_elems(std::max<size_t>((size_t)std::max(n + 1, L + 1),
+                                                                             kTcKeys(n, L)))) &&
+          ensure(errFlags, sizeof(int32_t) * kErrSlots) && ensure(counters, sizeof(unsigned long long) * 8) &&
           ensure(signs, sizeof(uint32_t) * hostSigns.size()) &&
           ensure(compCosh, sizeof(double) * std::max<size_t>(1, hostCosh.size()));
     const int chunkPts = 4096, nChunks = (n + chunkPts - 1) / chunkPts;
@@ -272,7 +290,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
             SDB_CK(cudaMemcpyAsync(compCosh.ptr, hostCosh.data(), sizeof(double) * hostCosh.size(),
                                    cudaMemcpyHostToDevice, st));
     }
-    SDB_CK(cudaMemsetAsync(errFlags.ptr, 0, sizeof(int32_t) * 8, st));
+    SDB_CK(cudaMemsetAsync(errFlags.ptr, 0, sizeof(int32_t) * kErrSlots, st));
     SDB_CK(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long) * 8, st));
     unsigned long long* ctr = static_cast<unsigned long long*>(counters.ptr);
 
@@ -318,7 +336,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
                 return SDB_ERR_NOMEM;
             L_(launch_to_bf16_split(f32(Xt), ld, n, Xb.ptr, ldb, st));
             L_(launch_to_bf16_split(f32(Rt), ld, h, Rb.ptr, ldb, st));
-            tcr = launch_rff_tc(Xb.ptr, Rb.ptr, n, h, ldb, f32(E), i32(errFlags) + 5, st);
+            tcr = launch_rff_tc(Xb.ptr, Rb.ptr, n, h, ldb, f32(E), i32(errFlags) + 5, dbgStallSpins, st);
             if (tcr > 0) launches += tcr;
         }
         L_(launch_rff(f32(Xt), ld, n, d, f32(Rt), h, f32(E), st, tcr > 0 ? i32(errFlags) + 5 : nullptr));
@@ -331,12 +349,14 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         const int segs = std::min(kUploadSegs, G);
         SDB_CK(cudaEventRecord(segEv[kUploadSegs], st));  // Xin is free once the stream got here
         SDB_CK(cudaStreamWaitEvent(copyStream, segEv[kUploadSegs], 0));
+        SDB_CK(cudaStreamWaitEvent(copyStream2, segEv[kUploadSegs], 0));
         for (int sgi = 0; sgi < segs; ++sgi) {
             const int cb = (int)((int64_t)G * sgi / segs), ce = (int)((int64_t)G * (sgi + 1) / segs);
             const size_t pb = (size_t)cb * chunk, pe = std::min<size_t>((size_t)n, (size_t)ce * chunk);
+            cudaStream_t cs = (sgi & 1) ? copyStream2 : copyStream;  // one cudaMemcpyAsync per segment
             SDB_CK(cudaMemcpyAsync(static_cast<float*>(Xin.ptr) + pb * d, X + pb * d, sizeof(float) * (pe - pb) * d,
-                                   cudaMemcpyHostToDevice, copyStream));
-            SDB_CK(cudaEventRecord(segEv[sgi], copyStream));
+                                   cudaMemcpyHostToDevice, cs));
+            SDB_CK(cudaEventRecord(segEv[sgi], cs));
             SDB_CK(cudaStreamWaitEvent(st, segEv[sgi], 0));
             pa.chunkBase = cb;
             pa.chunkEnd = ce;
@@ -445,6 +465,8 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     da.pairs = ctr + 3;
     da.topKmat = i32(topK);
     da.variant = distVariant;
+    da.waitErr = i32(errFlags) + 8;
+    da.stallSpins = dbgStallSpins;
     SDB_CK(cudaMemsetAsync(inRaw.ptr, 0, sizeof(int32_t) * n, st));
     // BF16 tensor-core screening + exact FP32 re-decision near eps (Cosine
     // sDBSCAN fits and eps sweeps of up to kMaxScreenedSweep values).  The
@@ -459,13 +481,22 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
             std::sort(da.sweepEps, da.sweepEps + sw->nEps);
         }
         const int ldb = (d + 63) / 64 * 64;
-        const int64_t qcap = std::max<int64_t>(1 << 20, (int64_t)n * 2 * k * m / 8);
-        if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * ldb) || !ensure(queue, sizeof(uint64_t) * (size_t)qcap))
+        const int64_t qcap = dbgQueueCap > 0 ? dbgQueueCap : std::max<int64_t>(1 << 20, (int64_t)n * 2 * k * m / 8);
+        if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * ldb) || !ensure(queue, sizeof(uint64_t) * (size_t)qcap) ||
+            !ensure(Cb, dist_tc_cand_bytes(da, ldb)))
             return SDB_ERR_NOMEM;
         L_(launch_to_bf16(f32(Xt), ld, n, Xb.ptr, ldb, st));
-        const int grid = (int)std::min<int64_t>(maxTiles, (int64_t)sm_count() * 3);
-        L_(launch_dist_tc(da, Xb.ptr, ldb, static_cast<uint64_t*>(queue.ptr), qcap, ctr + 4,
-                          i32(errFlags) + 4, grid, st));
+        // the tensor-core kernel takes the tiles by (super-chunk, list): the
+        // rows of 8 point chunks stay in L2 while every list passes over them
+        const size_t nKeys = tile_order_list_keys(ia, kSuperChunk);
+        if (!ensure(tileKeyTc, sizeof(int32_t) * (size_t)maxTiles) || !ensure(keyOffTc, sizeof(int64_t) * nKeys) ||
+            !ensure(tilePermTc, sizeof(int32_t) * (size_t)maxTiles))
+            return SDB_ERR_NOMEM;
+        L_(launch_tile_order_list(ia, kSuperChunk, i32(tileKeyTc), i64(keyOffTc), i32(tilePermTc), st));
+        DistArgs dtc = da;
+        dtc.tilePerm = i32(tilePermTc);
+        L_(launch_dist_tc(dtc, Xb.ptr, ldb, Cb.ptr, static_cast<uint64_t*>(queue.ptr), qcap, ctr + 4,
+                          i32(errFlags) + 4, st));
         L_(launch_recheck(da, static_cast<const uint64_t*>(queue.ptr), ctr + 4, qcap, st));
         da.gate = i32(errFlags) + 4;
         L_(launch_screen_reset(da, st));
@@ -615,7 +646,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     }
     }  // eps rounds
     if (!capture) SDB_CK(cudaEventRecord(ev[7], st));
-    SDB_CK(cudaMemcpyAsync(hostErr, errFlags.ptr, sizeof(int32_t) * 8, cudaMemcpyDeviceToHost, st));
+    SDB_CK(cudaMemcpyAsync(hostErr, errFlags.ptr, sizeof(int32_t) * kErrSlots, cudaMemcpyDeviceToHost, st));
     SDB_CK(cudaMemcpyAsync(hostCounters, counters.ptr, sizeof(unsigned long long) * 8, cudaMemcpyDeviceToHost, st));
     launchCount = launches;
     if (capture) return SDB_OK;  // flags are read by check_flags() after the graph has run
@@ -661,6 +692,7 @@ sdb_status sdb_engine::check_flags() {
                                                                    : "X has a point of zero sum (Chi2/JS)");
     if (hostErr[2]) return fail(SDB_ERR_ARG, "X has a non-finite value");
     if (hostErr[3]) return fail(SDB_ERR_INTERNAL, "top-m selection found fewer candidates than topM");
+    if (hostErr[8]) return fail(SDB_ERR_INTERNAL, "a bounded wait of the distance kernel ran out");
     return SDB_OK;
 }
 
@@ -703,7 +735,8 @@ sdb_status sdb_engine_create(int32_t n_points, int32_t n_features, int32_t devic
     e->device = device;
     sdb_params_default(&e->prm);
     if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&e->copyStream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamCreateWithFlags(&e->copyStream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&e->copyStream2, cudaStreamNonBlocking) != cudaSuccess) {
         sdb_engine_destroy(e);
         return SDB_ERR_CUDA;
     }
@@ -717,7 +750,7 @@ sdb_status sdb_engine_create(int32_t n_points, int32_t n_features, int32_t devic
             sdb_engine_destroy(e);
             return SDB_ERR_CUDA;
         }
-    if (cudaMallocHost(&e->hostErr, sizeof(int32_t) * 8) != cudaSuccess ||
+    if (cudaMallocHost(&e->hostErr, sizeof(int32_t) * kErrSlots) != cudaSuccess ||
         cudaMallocHost(&e->hostCounters, sizeof(unsigned long long) * 8) != cudaSuccess) {
         sdb_engine_destroy(e);
         return SDB_ERR_CUDA;
@@ -731,12 +764,14 @@ void sdb_engine_destroy(sdb_engine* e) {
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     if (e->copyStream) cudaStreamSynchronize(e->copyStream);
+    if (e->copyStream2) cudaStreamSynchronize(e->copyStream2);
     e->free_all();
     for (int i = 0; i < 9; ++i)
         if (e->ev[i]) cudaEventDestroy(e->ev[i]);
     for (int i = 0; i <= sdb_engine::kUploadSegs; ++i)
         if (e->segEv[i]) cudaEventDestroy(e->segEv[i]);
     if (e->copyStream) cudaStreamDestroy(e->copyStream);
+    if (e->copyStream2) cudaStreamDestroy(e->copyStream2);
     if (e->hostErr) cudaFreeHost(e->hostErr);
     if (e->hostCounters) cudaFreeHost(e->hostCounters);
     if (e->stream) cudaStreamDestroy(e->stream);
@@ -754,8 +789,18 @@ sdb_status sdb_set_params(sdb_engine* e, const sdb_params* p) {
 
 sdb_status sdb_set_tile_variant(sdb_engine* e, int32_t variant) {
     if (!e) return SDB_ERR_ARG;
-    if (variant < 0 || variant > 3) return e->fail(SDB_ERR_ARG, "tile variant must be 0..3");
+    if (variant < 0 || variant > 5) return e->fail(SDB_ERR_ARG, "tile variant must be 0..5");
     e->distVariant = variant;
+    return SDB_OK;
+}
+
+sdb_status sdb_set_debug_limits(sdb_engine* e, int64_t stall_spins, int64_t queue_cap, int64_t device_bytes_cap) {
+    if (!e) return SDB_ERR_ARG;
+    if (stall_spins < 0 || queue_cap < 0 || device_bytes_cap < 0)
+        return e->fail(SDB_ERR_ARG, "debug limits must be >= 0 (0 = off)");
+    e->dbgStallSpins = stall_spins;
+    e->dbgQueueCap = queue_cap;
+    e->dbgDeviceCap = (size_t)device_bytes_cap;
     return SDB_OK;
 }
 

@@ -44,6 +44,13 @@ struct SweepSpec {
     bool capture = false;
 };
 
+// Device error / status flags of a fit (int32 each):
+//   [0] negative Chi2/JS input   [1] zero point   [2] non-finite value
+//   [3] top-m internal error     [4] BF16 distance screening failed (plain path redoes it)
+//   [5] tensor-core embedding failed (FP32 redoes it)   [6] sngOptics list overflow
+//   [7] sng BF16 block failed (FP32 redoes it)   [8] a bounded wait of the plain distance kernel ran out
+constexpr int kErrSlots = 16;
+
 struct sdb_engine {
     int n = 0, d = 0, device = 0;
     sdb_params prm{};
@@ -51,10 +58,11 @@ struct sdb_engine {
     bool sngParamsSet = false;  // set_sngParams (enough for the sng fits)
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[9] = {};
-    // host input is uploaded in segments on a second stream, each segment's
-    // projection starting as soon as its rows have landed
-    static constexpr int kUploadSegs = 8;
-    cudaStream_t copyStream = nullptr;
+    // host input is uploaded in segments on two copy streams (alternating, so
+    // two copies are in flight), each segment's projection starting as soon
+    // as its rows have landed
+    static constexpr int kUploadSegs = 16;
+    cudaStream_t copyStream = nullptr, copyStream2 = nullptr;
     cudaEvent_t segEv[kUploadSegs + 1] = {};
     std::string err;
 
@@ -71,7 +79,8 @@ struct sdb_engine {
         rootFlag, labels, nClusters, scanTmp, errFlags, counters, E, Rt, signs, compCosh, dists, coreDist, nbOff,
         nbIdx, nbDist, nbFill, hubIdx, kMask, firstMasks, Xb, queue, sweepLabels, sweepNcl, sig, Rb, newMasks,
         coreEps, sampleFlag, noiseFlag, noiseCores, noisePts, PcT, numCore, pairRound, sngCols, sngMult, sngColOf,
-        sngExtras, sngExtraPass, sngMask, rowDeg, colCnt, sngUb, sngHeavy, chunkOff, tileKey, keyOff, tilePerm;
+        sngExtras, sngExtraPass, sngMask, rowDeg, colCnt, sngUb, sngHeavy, chunkOff, tileKey, keyOff, tilePerm, Cb, tileKeyTc, keyOffTc, tilePermTc, sngWords, hashOffB,
+        hashIdB, hashDistB;
 
     // results
     bool haveLabels = false, haveOptics = false, haveFit = false, lastOptics = false;
@@ -90,6 +99,12 @@ struct sdb_engine {
     int64_t fallbacks = 0;  // BF16 screening fits redone on the plain path
     int sngColsLast = 0, sngExtraLast = 0;  // sampled columns and extra draws of the last sng fit
     int distVariant = 0;    // plain distance tile shape (DistArgs::variant), set by the batch's autotuner
+    int sngSampling = 0;    // sngDbscan sample: 0 = by seed (shared when >= 0, blocks when < 0), 1 = shared, 2 = blocks
+    // test and diagnostic limits (sdb_set_debug_limits), 0 = off
+    long long dbgStallSpins = 0;  // each tensor-core / persistent distance kernel takes its failure path once
+    int64_t dbgQueueCap = 0;      // cap of the BF16 re-decision queues
+    size_t dbgDeviceCap = 0;      // cap of the engine's device memory
+    size_t devBytes = 0;          // device memory the engine holds now
     float stageMs[9] = {};
 
     bool ensure(DevBuf& b, size_t bytes);
@@ -108,6 +123,9 @@ struct sdb_engine {
     // labelsOut + i n when given) or sngOptics (one eps)
     sdb_status fit_sng(const float* X, bool xOnDevice, const float* epsList, int nEps, int minPts, bool optics,
                        int32_t* labelsOut = nullptr, int32_t* nclOut = nullptr);
+    // sngDbscan with independent samples per block of points (k_sng_blocks.cu)
+    sdb_status fit_sng_blocks(const float* X, bool xOnDevice, const float* epsList, int nEps, int minPts, bool optics,
+                              int32_t* labelsOut, int32_t* nclOut);
 
     static float* f32(DevBuf& b) { return static_cast<float*>(b.ptr); }
     static int32_t* i32(DevBuf& b) { return static_cast<int32_t*>(b.ptr); }

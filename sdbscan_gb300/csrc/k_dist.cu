@@ -155,6 +155,7 @@ template <int DIST, int TX, int CN, int KT = TK, int NST = STAGES> int launch_di
 // shapes need m <= 50.
 template <int DIST> int launch_dist_t(const DistArgs& a, cudaStream_t st) {
     const bool fits50 = a.m <= 50;
+    if (a.variant == 4 || a.variant == 5) return launch_dist_ws(a, a.variant, st);
     switch (a.variant) {
         case 2: if (fits50) return launch_dist_v<DIST, 10, 5>(a, st); break;
         case 3:  // the 4-stage shape is built for the FMA-bound Cosine tile only (Chi2: 2.5 % slower)

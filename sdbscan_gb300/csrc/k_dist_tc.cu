@@ -1,30 +1,48 @@
 // Stage 4, BF16 screening mode: candidate dot products on the tcgen05 tensor
 // cores, with an exact FP32 re-decision of every pair near eps.
 //
-// Same grouped, gathered formulation as k_dist (tile = list l, 128 member rows,
-// 64 candidate columns), but the operands are BF16 copies of the unit-norm
-// rows and the products accumulate in FP32 in tensor memory:
-//   - operands are staged by cp.async into shared memory in the 128-byte
-//     swizzled K-major layout the MMA reads (8-row x 128-byte atoms, 16-byte
-//     chunk c of row r stored at chunk c ^ (r & 7)), 3 stages of 64 dimensions
-//     (73 KB, so three CTAs share an SM);
-//   - one thread issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=64,
-//     K=16) into a 128 x 64 FP32 accumulator in TMEM, and tcgen05.commit
-//     arrives on the stage's mbarrier when the MMAs have read it;
-//   - the epilogue reads the accumulator with tcgen05.ld (thread t = row t).
+// Same grouped, gathered formulation as k_dist (tile = list l, 128 member
+// rows, 64 candidate columns), with BF16 copies of the unit-norm rows as
+// operands and FP32 accumulation in tensor memory.  Persistent and
+// warp-specialised, one CTA per SM, 256 threads:
+//   warps 0-1  gather the tile's 128 member rows (A), 64 dimensions per stage,
+//              with cp.async into the 128-byte-swizzled K-major layout the MMA
+//              reads (8-row x 128-byte atoms, 16-byte chunk c of row r at
+//              chunk c ^ (r & 7)); each lane's copies arrive on the stage's
+//              "full" mbarrier (cp.async.mbarrier.arrive.noinc) as they land;
+//   warp 2     loads the list's 64 candidate rows (B) with one TMA tile load
+//              (cp.async.bulk.tensor) per stage from the candidate matrix Cb,
+//              the BF16 rows of every list's top-m points gathered once per
+//              fit (k_gather_cand), completing bytes on the same barrier;
+//   warp 3     issues tcgen05.mma.cta_group::1.kind::f16 (M = 128, N = 64,
+//              K = 16) into one of two 128 x 64 FP32 accumulators in tensor
+//              memory and commits each stage back to its "empty" barrier, so
+//              the loaders refill it while later stages compute;
+//   warps 4-7  epilogue: tcgen05.ld of the other accumulator (warp w reads
+//              TMEM lanes 32 (w % 4)..), the eps decisions as bit words, the
+//              queue of pairs near eps, the column counts; it runs under the
+//              next tile's MMAs.
+// An 8-stage ring (24 KB per stage) runs ahead across tiles.  The CTA takes
+// the launch order's tiles b, b + grid, ..., so the tiles in flight stay in
+// one window of point chunks (L2 reuse of the gathered rows).
 //
 // Decision rule.  For unit vectors x, y and their BF16 roundings x', y'
 // (relative error <= 2^-8 each), |x'.y' - x.y| <= (2^-7 + 2^-16) * sum|x_i y_i|
-// <= 0.00783; FP32 accumulation of 784 exact products adds < 2^-10, and the
+// <= 0.00783; FP32 accumulation of the exact products adds < 2^-10, and the
 // FP32 reference's own rounding < 5e-5, 0.00886 in all.  A pair whose screened
 // distance is farther than kMargin = 0.009 from eps is therefore on the same
 // side of eps as the reference's FP32 distance; every other pair goes to a
 // queue and is recomputed by k_recheck with the plain path's exact sequential
 // FP32 dot.  The resulting masks are identical to the plain FP32 path's.
 //
-// Every wait on an mbarrier is bounded; on timeout the CTA records an error,
-// stops issuing work, drains its own copies, frees its TMEM and returns.
+// Every wait on an mbarrier is bounded.  A wait that runs out stops every
+// role (a shared abort flag) and raises the error flag, after which the plain
+// FP32 kernel redoes the stage; before freeing its tensor memory the CTA waits
+// for its own copies and MMAs.
+#include <cuda.h>
 #include <cuda_bf16.h>
+
+#include <algorithm>
 
 #include "common.cuh"
 #include "dist_tile.cuh"
@@ -34,28 +52,31 @@ namespace sdb {
 namespace {
 
 constexpr int TM = 128, TN = 64, TKB = 64;  // rows, candidate columns, bf16 per stage row (128 B)
-constexpr int STAGES = 3, NT = 128;
+constexpr int STAGES = 8;
 constexpr int A_BYTES = TM * 128, B_BYTES = TN * 128, STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int NT = 256, EPI0 = 4;               // warps 0-1 A, 2 B, 3 MMA, 4-7 epilogue
+constexpr int A_LANES = 64;                     // threads gathering A
 constexpr float kMargin = 0.009f;
-constexpr uint32_t kTmemCols = 64;
+constexpr uint32_t kTmemCols = 2 * TN;          // two accumulators
+constexpr uint32_t kIdesc = tc::idesc_bf16(TM, TN);
 
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0));
 }
-
-using tc::mbar_init;
-using tc::mbar_wait;
-using tc::smem_desc;
-using tc::smem_u32;
-using tc::tmem_ld16;
-using tc::mma_commit;
-
-// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
-// K-major, M = 128, N = 64.
-constexpr uint32_t kIdesc = tc::idesc_bf16(TM, TN);
-
-__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
-    tc::mma_bf16(dtmem, adesc, bdesc, kIdesc, accumulate);
+__device__ __forceinline__ void cp_async_arrive_noinc(uint32_t bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];\n" ::"r"(bar) : "memory");
+}
+// Named barrier 2 over the four epilogue warps; the OR form returns the same
+// value to all of them.
+__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 2, 128;\n" ::: "memory"); }
+__device__ __forceinline__ bool epi_or(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.or.pred p, 2, 128, q;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v)
+        : "memory");
+    return r != 0;
 }
 
 // Swizzled byte offset of 16-byte chunk c (0..7) of row r in an operand tile.
@@ -63,31 +84,63 @@ __device__ __forceinline__ uint32_t sw128(int r, int c) {
     return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
 }
 
+struct TileIds {
+    int64_t mbeg, mend;
+    int l, ct;
+};
+__device__ __forceinline__ TileIds tile_ids(const DistArgs& a, int64_t b) {
+    const int64_t t = tile_at(a.tilePerm, b);
+    TileIds r;
+    r.l = a.tileList[t];
+    const int64_t ti = t - a.tileOff[r.l];
+    const int mt = (int)(ti / a.nct);
+    r.ct = (int)(ti % a.nct);
+    r.mbeg = a.listOff[r.l] + (int64_t)mt * TM;
+    r.mend = a.listOff[r.l + 1];
+    return r;
+}
+
 // SWEEP: store the screened distance of every pair and queue the pairs near
 // any of the sweep's eps values (masks follow per eps from the distances);
 // otherwise decide against eps and write the masks.
 template <bool SWEEP>
-__global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat16* __restrict__ Xb, int ldb,
+__global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUtensorMap tmC, DistArgs a,
+                                                  const __nv_bfloat16* __restrict__ Xb, int ldb,
                                                   uint64_t* __restrict__ queue, int64_t qcap,
                                                   unsigned long long* __restrict__ qcount, int32_t* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smraw[];
-    __shared__ uint64_t bars[STAGES];
+    __shared__ uint64_t fullA[STAGES], fullB[STAGES], emptyBar[STAGES], tfullBar[2], temptyBar[2], doneBar, neverBar;
     __shared__ uint32_t tmemBase;
-    // tile ids: the next tile's are loaded under this tile's epilogue, which
-    // by then holds its own row's ids in registers (column ids by tile
-    // parity); kept small so three CTAs still share an SM's shared memory
-    __shared__ int rowPoints[TM], colPoints[2][TN], colCount[TN];
-    __shared__ uint8_t rowSlots[TM];
+    __shared__ int colPoints[2][TN], colCount[2][TN];
+    __shared__ volatile int abortFlag;
+    __shared__ volatile long long bIssued, bUsed;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t base = (smem_u32(smraw) + 1023u) & ~1023u;  // 1024-aligned operand tiles
+    const uint32_t base = (tc::smem_u32(smraw) + 1023u) & ~1023u;  // 1024-aligned operand tiles
+    const int nk = ldb / TKB;
+    const int64_t total = *a.tileTotal;
 
     if (tid == 0) {
-        for (int s = 0; s < STAGES; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        for (int s = 0; s < STAGES; ++s) {
+            tc::mbar_init(tc::smem_u32(&fullA[s]), A_LANES);  // one noinc arrival per A lane
+            tc::mbar_init(tc::smem_u32(&fullB[s]), 1);        // the B loader's expect_tx (+ the TMA bytes)
+            tc::mbar_init(tc::smem_u32(&emptyBar[s]), 1);     // the MMA commit
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(tc::smem_u32(&tfullBar[b]), 1);
+            tc::mbar_init(tc::smem_u32(&temptyBar[b]), 4);
+        }
+        tc::mbar_init(tc::smem_u32(&doneBar), 1);
+        tc::mbar_init(tc::smem_u32(&neverBar), 1);  // the stall test's barrier: nothing arrives on it
+        abortFlag = 0;
+        bIssued = 0;
+        bUsed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
+    for (int i = tid; i < 2 * TN; i += NT) colCount[i / TN][i % TN] = 0;
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmemBase)),
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         tc::smem_u32(&tmemBase)),
                      "r"(kTmemCols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
     }
@@ -95,227 +148,296 @@ __global__ void __launch_bounds__(NT, 3) k_dist_tc(DistArgs a, const __nv_bfloat
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = tmemBase;
-    uint32_t phaseBits = 0;  // bit s: parity of the next completion of stage s's barrier
-    bool timedOut = false;
-    const int nk = ldb / TKB;
-    const int64_t total = *a.tileTotal;
+    auto stop = [&]() {
+        abortFlag = 1;
+        atomicExch(err, 1);
+    };
 
-    // The next tile's ids and first STAGES - 1 stages are loaded before the
-    // current tile's epilogue (its MMAs are done by then), so the gathers
-    // overlap the epilogue.
-    auto load_meta = [&](int64_t tb, int b) {  // tb: launch index, mapped to a tile id
-        const int64_t t = tile_at(a.tilePerm, tb);
-        const int l = a.tileList[t];
-        const int64_t ti = t - a.tileOff[l];
-        const int mt = (int)(ti / a.nct), ct = (int)(ti % a.nct);
-        const int64_t mbeg = a.listOff[l] + (int64_t)mt * TM, mend = a.listOff[l + 1];
-        const int r = l % a.nproj, side = l / a.nproj;
-        const int32_t* cand = a.topM + (size_t)r * 2 * a.m + side * a.m;
-        for (int i = tid; i < TM; i += NT) {
-            const int64_t q = mbeg + i;
-            if (q < mend) {
-                const int2 mb = a.members[q];
-                rowPoints[i] = mb.x;
-                rowSlots[i] = (uint8_t)mb.y;
-            } else {
-                rowPoints[i] = -1;
-                rowSlots[i] = 0;
+    if (warp < 2) {
+        // ---------------- A: member rows, gathered ----------------
+        long long it = 0;
+        for (int64_t b = blockIdx.x; b < total && !abortFlag; b += gridDim.x) {
+            const TileIds ti = tile_ids(a, b);
+            // copy u of this lane: chunk tid % 8 of row 8 u + tid / 8, so the
+            // eight lanes of a row read its 128 contiguous bytes together
+            const int c = tid & 7;
+            const __nv_bfloat16* src[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                const int64_t q = ti.mbeg + 8 * u + (tid >> 3);
+                src[u] = q < ti.mend ? Xb + (size_t)__ldg(&a.members[q].x) * ldb + c * 8 : nullptr;
+            }
+            bool bad = false;
+            for (int kc = 0; kc < nk; ++kc, ++it) {
+                const int s = (int)(it % STAGES);
+                if (it >= STAGES && !tc::mbar_wait_or(tc::smem_u32(&emptyBar[s]),
+                                                      (uint32_t)(((it / STAGES) - 1) & 1), &abortFlag)) {
+                    bad = true;
+                    break;
+                }
+                if (abortFlag) break;
+                const uint32_t sA = base + s * STAGE_BYTES;
+#pragma unroll
+                for (int u = 0; u < 16; ++u) {
+                    const int row = 8 * u + (tid >> 3);
+                    cp_async16(sA + sw128(row, c), src[u] != nullptr ? src[u] + kc * TKB : Xb, src[u] != nullptr);
+                }
+                cp_async_arrive_noinc(tc::smem_u32(&fullA[s]));
+            }
+            if (bad) {
+                stop();
+                break;
             }
         }
-        for (int j = tid; j < TN; j += NT) {
-            const int c = ct * TN + j;
-            colPoints[b][j] = c < a.m ? cand[c] : -1;
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+    } else if (warp == 2) {
+        // ---------------- B: the list's candidate rows, one TMA tile per stage ----------------
+        if (lane == 0) {
+            long long it = 0;
+            for (int64_t b = blockIdx.x; b < total && !abortFlag; b += gridDim.x) {
+                const TileIds ti = tile_ids(a, b);
+                const int y0 = (ti.l * a.nct + ti.ct) * TN;
+                bool bad = false;
+                for (int kc = 0; kc < nk; ++kc, ++it) {
+                    const int s = (int)(it % STAGES);
+                    if (it >= STAGES && !tc::mbar_wait_or(tc::smem_u32(&emptyBar[s]),
+                                                          (uint32_t)(((it / STAGES) - 1) & 1), &abortFlag)) {
+                        bad = true;
+                        break;
+                    }
+                    if (abortFlag) break;
+                    const uint32_t bar = tc::smem_u32(&fullB[s]);
+                    tc::mbar_expect_tx(bar, B_BYTES);
+                    tc::tma_load_2d(base + s * STAGE_BYTES + A_BYTES, &tmC, kc * TKB, y0, bar);
+                    bIssued = it + 1;
+                }
+                if (bad) {
+                    stop();
+                    break;
+                }
+            }
         }
-    };
-    auto load_stage = [&](int b, int stage, int kc) {
-        const uint32_t sA = base + stage * STAGE_BYTES, sB = sA + A_BYTES;
-        const int k0 = kc * TKB;
-#pragma unroll
-        for (int it = 0; it < (TM * 8) / NT; ++it) {  // 8 per thread
-            const int idx = tid + it * NT, row = idx >> 3, c = idx & 7;
-            const int p = rowPoints[row];
-            const bool ok = p >= 0;
-            cp_async16(sA + sw128(row, c), ok ? Xb + (size_t)p * ldb + k0 + c * 8 : Xb, ok);
-        }
-#pragma unroll
-        for (int it = 0; it < (TN * 8) / NT; ++it) {  // 4 per thread
-            const int idx = tid + it * NT, row = idx >> 3, c = idx & 7;
-            const int p = colPoints[b][row];
-            const bool ok = p >= 0;
-            cp_async16(sB + sw128(row, c), ok ? Xb + (size_t)p * ldb + k0 + c * 8 : Xb, ok);
-        }
-    };
-    auto prologue = [&](int b) {
-        for (int s = 0; s < STAGES - 1; ++s) {
-            if (s < nk) load_stage(b, s, s);
-            asm volatile("cp.async.commit_group;\n" ::);
-        }
-    };
-    for (int j = tid; j < TN; j += NT) colCount[j] = 0;  // re-zeroed after each tile's use
-    if ((int64_t)blockIdx.x < total) {
-        load_meta(blockIdx.x, 0);
-        __syncthreads();
-        prologue(0);
-    }
-
-    int tb = 0;  // parity of the current tile's buffers
-    for (int64_t t = blockIdx.x; t < total; t += gridDim.x, tb ^= 1) {
-        const int64_t tileId = tile_at(a.tilePerm, t);
-        const int ct = (int)((tileId - a.tileOff[a.tileList[tileId]]) % a.nct);
-        const int* colPoint = colPoints[tb];
-        for (int kc = 0; kc < nk; ++kc) {
-            const int stage = kc % STAGES;
-            asm volatile("cp.async.wait_group %0;\n" ::"n"(STAGES - 2));
-            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // cp.async data -> async proxy
-            __syncthreads();
-            if (tid == 0) {
+    } else if (warp == 3) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            long long it = 0;
+            int i = 0;
+            for (int64_t b = blockIdx.x; b < total && !abortFlag; b += gridDim.x, ++i) {
+                const int buf = i & 1;
+                if (i >= 2 && !tc::mbar_wait_or(tc::smem_u32(&temptyBar[buf]), (uint32_t)(((i >> 1) - 1) & 1),
+                                                &abortFlag)) {
+                    stop();
+                    break;
+                }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                const uint32_t sA = base + stage * STAGE_BYTES, sB = sA + A_BYTES;
+                const uint32_t acc = tmem + (uint32_t)(buf * TN);
+                // the stall test: a producer that never delivers, with copies and loads in flight
+                bool bad = i == 0 && a.stallSpins > 0 && !tc::stall_wait(tc::smem_u32(&neverBar), a.stallSpins);
+                for (int kc = 0; kc < nk && !bad; ++kc, ++it) {
+                    const int s = (int)(it % STAGES);
+                    if (!tc::mbar_wait_or(tc::smem_u32(&fullB[s]), (uint32_t)((it / STAGES) & 1), &abortFlag)) {
+                        bad = true;
+                        break;
+                    }
+                    bUsed = it + 1;
+                    if (!tc::mbar_wait_or(tc::smem_u32(&fullA[s]), (uint32_t)((it / STAGES) & 1), &abortFlag)) {
+                        bad = true;
+                        break;
+                    }
+                    // cp.async writes to shared memory (generic proxy) before the MMA reads them (async proxy)
+                    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    const uint32_t sA = base + s * STAGE_BYTES, sB = sA + A_BYTES;
 #pragma unroll
-                for (int k = 0; k < TKB / 16; ++k)
-                    mma_bf16(tmem, smem_desc(sA + k * 32), smem_desc(sB + k * 32), (kc > 0 || k > 0) ? 1u : 0u);
-                mma_commit(smem_u32(&bars[stage]));
-            }
-            const int nxt = kc + STAGES - 1;
-            if (nxt < nk) {
-                const int ns = nxt % STAGES;
-                if (kc >= 1) {  // stage ns was read by the MMAs of chunk kc - 1
-                    if (!mbar_wait(smem_u32(&bars[ns]), (phaseBits >> ns) & 1u)) timedOut = true;
-                    phaseBits ^= 1u << ns;
+                    for (int k = 0; k < TKB / 16; ++k)
+                        tc::mma_bf16(acc, tc::smem_desc(sA + k * 32), tc::smem_desc(sB + k * 32), kIdesc,
+                                     (kc > 0 || k > 0) ? 1u : 0u);
+                    tc::mma_commit(tc::smem_u32(&emptyBar[s]));
                 }
-                load_stage(tb, ns, nxt);
+                if (bad) {
+                    stop();
+                    break;
+                }
+                tc::mma_commit(tc::smem_u32(&tfullBar[buf]));
             }
-            asm volatile("cp.async.commit_group;\n" ::);
+            tc::mma_commit(tc::smem_u32(&doneBar));  // arrives once every MMA issued above has completed
         }
-        // chunks [0, nk - STAGES) were waited on inside the loop; wait for the rest
-        for (int c = (nk > STAGES ? nk - STAGES : 0); c < nk; ++c) {
-            const int s = c % STAGES;
-            if (!mbar_wait(smem_u32(&bars[s]), (phaseBits >> s) & 1u)) timedOut = true;
-            phaseBits ^= 1u << s;
-        }
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        // epilogue: thread tid owns row tid
-        const int row = tid;
-        const int p = rowPoints[row];
-        const int mySlot = rowSlots[row];
-        const int64_t tn = t + gridDim.x;
-        if (tn < total) {  // the next tile's gathers start now, under this tile's epilogue
-            __syncthreads();  // every thread holds its row's ids
-            load_meta(tn, tb ^ 1);
-            __syncthreads();
-            prologue(tb ^ 1);
-        }
-        uint64_t bits = 0;
-        int nPass = 0;
-        if constexpr (SWEEP) {
+    } else {
+        // ---------------- epilogue: thread et owns row et of the tile ----------------
+        const int et = tid - EPI0 * 32, quarter = warp & 3;
+        int i = 0;
+        for (int64_t b = blockIdx.x; b < total; b += gridDim.x, ++i) {
+            const int buf = i & 1;
+            const TileIds ti = tile_ids(a, b);
+            const int row = quarter * 32 + lane;  // TMEM lane = tile row
+            const int64_t q = ti.mbeg + row;
+            int p = -1, mySlot = 0;
+            if (q < ti.mend) {
+                const int2 mm = a.members[q];
+                p = mm.x;
+                mySlot = mm.y;
+            }
+            if (et < TN) {
+                const int side = ti.l / a.nproj, r = ti.l % a.nproj;
+                const int c = ti.ct * TN + et;
+                colPoints[buf][et] = c < a.m ? a.topM[(size_t)r * 2 * a.m + side * a.m + c] : -1;
+            }
+            // the column ids are in, the previous use of colCount[buf] is flushed,
+            // and every epilogue warp sees the same stop decision
+            if (epi_or(abortFlag != 0)) break;
+            const int* colPoint = colPoints[buf];
+            if (!tc::mbar_wait_or(tc::smem_u32(&tfullBar[buf]), (uint32_t)((i >> 1) & 1), &abortFlag)) {
+                stop();  // the next tile's epi_or ends every epilogue warp
+                if (!SWEEP) epi_sync();
+                continue;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t tacc = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * TN);
+            const int ct = ti.ct;
+            uint64_t bits = 0;
+            int nPass = 0;
+            if constexpr (SWEEP) {
 #pragma unroll 1
-        for (int c16 = 0; c16 < TN / 16; ++c16) {
-            float v[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c16 * 16), v);
+                for (int c16 = 0; c16 < TN / 16; ++c16) {
+                    float v[16];
+                    tc::tmem_ld16(tacc + (uint32_t)(c16 * 16), v);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int col = c16 * 16 + j;
-                const int q = colPoint[col];
-                bool unsure = false;
-                if (p >= 0 && q >= 0) {  // keep the screened distance, re-decide near any eps
-                    const float dist = 1.0f - v[j];
-                    a.dists[((size_t)p * 2 * a.k + mySlot) * a.m + ct * TN + col] = dist;
-                    if (p != q)
-                        for (int e = 0; e < a.nSweep; ++e) unsure |= fabsf(dist - a.sweepEps[e]) <= kMargin;
+                    for (int j = 0; j < 16; ++j) {
+                        const int col = c16 * 16 + j;
+                        const int qq = colPoint[col];
+                        bool unsure = false;
+                        if (p >= 0 && qq >= 0) {  // keep the screened distance, re-decide near any eps
+                            const float dist = 1.0f - v[j];
+                            a.dists[((size_t)p * 2 * a.k + mySlot) * a.m + ct * TN + col] = dist;
+                            if (p != qq)
+                                for (int e = 0; e < a.nSweep; ++e) unsure |= fabsf(dist - a.sweepEps[e]) <= kMargin;
+                        }
+                        const unsigned um = __ballot_sync(0xffffffffu, unsure);
+                        if (um) {
+                            const int leader = __ffs(um) - 1;
+                            unsigned long long at0 = 0;
+                            if (lane == leader) at0 = atomicAdd(qcount, (unsigned long long)__popc(um));
+                            at0 = __shfl_sync(0xffffffffu, at0, leader);
+                            if (unsure) {
+                                const unsigned long long at = at0 + __popc(um & ((1u << lane) - 1u));
+                                if ((int64_t)at < qcap)
+                                    queue[at] = ((uint64_t)(uint32_t)p << 32) | ((uint32_t)mySlot << 16) |
+                                                (uint32_t)(ct * TN + col);
+                                else
+                                    atomicExch(err, 2);
+                            }
+                        }
+                    }
                 }
-                const unsigned um = __ballot_sync(0xffffffffu, unsure);
-                if (um) {
-                    const int leader = __ffs(um) - 1;
-                    unsigned long long at0 = 0;
-                    if (lane == leader) at0 = atomicAdd(qcount, (unsigned long long)__popc(um));
-                    at0 = __shfl_sync(0xffffffffu, at0, leader);
-                    if (unsure) {
-                        const unsigned long long at = at0 + __popc(um & ((1u << lane) - 1u));
-                        if ((int64_t)at < qcap)
-                            queue[at] = ((uint64_t)(uint32_t)p << 32) | ((uint32_t)mySlot << 16) |
-                                        (uint32_t)(ct * TN + col);
-                        else
-                            atomicExch(err, 2);
+                asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(tc::smem_u32(&temptyBar[buf]));
+            } else {
+                // The row's 64 decisions as bit words: pass (screened distance
+                // below eps - margin), unsure (within the margin), near zero (the
+                // only place the point itself can be among the candidates); then
+                // the columns that do not exist, the row's own point and empty
+                // rows are masked out.
+                uint64_t uw = 0, zw = 0;
+                const float lo = a.eps - kMargin, hi = a.eps + kMargin;
+#pragma unroll
+                for (int c16 = 0; c16 < TN / 16; ++c16) {
+                    float v[16];
+                    tc::tmem_ld16(tacc + (uint32_t)(c16 * 16), v);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const float dist = 1.0f - v[j];
+                        const bool pass = dist <= lo;
+                        bits |= (uint64_t)pass << (c16 * 16 + j);
+                        uw |= (uint64_t)(!pass && dist <= hi) << (c16 * 16 + j);
+                        zw |= (uint64_t)(dist <= kMargin) << (c16 * 16 + j);
+                    }
+                }
+                // the accumulator is in registers: the MMAs may reuse it
+                asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(tc::smem_u32(&temptyBar[buf]));
+                const int nvalid = a.m - ct * TN;
+                uint64_t keep = p < 0 ? 0ull : (nvalid >= 64 ? ~0ull : (1ull << nvalid) - 1ull);
+                for (uint64_t z = zw & keep & (bits | uw); z; z &= z - 1) {  // rare: is the row's point a candidate?
+                    const int col = __ffsll((long long)z) - 1;
+                    if (colPoint[col] == p) keep &= ~(1ull << col);
+                }
+                bits &= keep;
+                uw &= keep;
+                if (__any_sync(0xffffffffu, uw != 0)) {  // pairs within the margin go to the queue
+                    const int cnt = __popcll(uw);
+                    if (cnt) {
+                        unsigned long long at = atomicAdd(qcount, (unsigned long long)cnt);
+                        for (uint64_t u = uw; u; u &= u - 1, ++at) {
+                            const int col = __ffsll((long long)u) - 1;
+                            if ((int64_t)at < qcap)
+                                queue[at] = ((uint64_t)(uint32_t)p << 32) | ((uint32_t)mySlot << 16) |
+                                            (uint32_t)(ct * TN + col);
+                            else
+                                atomicExch(err, 2);
+                        }
+                    }
+                }
+                nPass = __popcll(bits);
+                int cc0 = 0, cc1 = 0;  // passes of columns lane and lane + 32
+#pragma unroll
+                for (int col = 0; col < TN; ++col) {
+                    const int pc = __popc(__ballot_sync(0xffffffffu, (bits >> col) & 1ull));
+                    if (lane == (col & 31)) {
+                        if (col < 32) cc0 += pc;
+                        else cc1 += pc;
+                    }
+                }
+                if (cc0) atomicAdd(&colCount[buf][lane], cc0);
+                if (cc1) atomicAdd(&colCount[buf][lane + 32], cc1);
+                if (p >= 0) a.masks[((size_t)p * 2 * a.k + mySlot) * a.W + ct] = bits;
+            }
+            const int wp = warp_sum(nPass);
+            if (lane == 0 && wp) atomicAdd(a.pairs, (unsigned long long)wp);
+            if constexpr (!SWEEP) {
+                epi_sync();  // every warp's column counts for this tile are in
+                if (et < TN) {
+                    const int cnt = colCount[buf][et];
+                    if (cnt) {
+                        atomicAdd(a.inRaw + colPoint[et], cnt);
+                        colCount[buf][et] = 0;
                     }
                 }
             }
         }
-        } else {
-        // The row's 64 decisions as bit words: pass (screened distance below
-        // eps - margin), unsure (within the margin), near zero (the only place
-        // the point itself can be among the candidates); then the columns
-        // that do not exist, the row's own point and empty rows are masked out.
-        uint64_t uw = 0, zw = 0;
-        const float lo = a.eps - kMargin, hi = a.eps + kMargin;
-#pragma unroll
-        for (int c16 = 0; c16 < TN / 16; ++c16) {
-            float v[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c16 * 16), v);
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const float dist = 1.0f - v[j];
-                const bool pass = dist <= lo;
-                bits |= (uint64_t)pass << (c16 * 16 + j);
-                uw |= (uint64_t)(!pass && dist <= hi) << (c16 * 16 + j);
-                zw |= (uint64_t)(dist <= kMargin) << (c16 * 16 + j);
-            }
-        }
-        const int nvalid = a.m - ct * TN;
-        uint64_t keep = p < 0 ? 0ull : (nvalid >= 64 ? ~0ull : (1ull << nvalid) - 1ull);
-        for (uint64_t z = zw & keep & (bits | uw); z; z &= z - 1) {  // rare: is the row's point a candidate?
-            const int col = __ffsll((long long)z) - 1;
-            if (colPoint[col] == p) keep &= ~(1ull << col);
-        }
-        bits &= keep;
-        uw &= keep;
-        if (__any_sync(0xffffffffu, uw != 0)) {  // pairs within the margin go to the queue
-            const int cnt = __popcll(uw);
-            if (cnt) {
-                unsigned long long at = atomicAdd(qcount, (unsigned long long)cnt);
-                for (uint64_t u = uw; u; u &= u - 1, ++at) {
-                    const int col = __ffsll((long long)u) - 1;
-                    if ((int64_t)at < qcap)
-                        queue[at] = ((uint64_t)(uint32_t)p << 32) | ((uint32_t)mySlot << 16) |
-                                    (uint32_t)(ct * TN + col);
-                    else
-                        atomicExch(err, 2);
-                }
-            }
-        }
-        nPass = __popcll(bits);
-        int cc0 = 0, cc1 = 0;  // passes of columns lane and lane + 32
-#pragma unroll
-        for (int col = 0; col < TN; ++col) {
-            const int pc = __popc(__ballot_sync(0xffffffffu, (bits >> col) & 1ull));
-            if (lane == (col & 31)) {
-                if (col < 32) cc0 += pc;
-                else cc1 += pc;
-            }
-        }
-        if (cc0) atomicAdd(&colCount[lane], cc0);
-        if (cc1) atomicAdd(&colCount[lane + 32], cc1);
-        }
-        if (!SWEEP && p >= 0) a.masks[((size_t)p * 2 * a.k + mySlot) * a.W + ct] = bits;
-        const int wp = warp_sum(nPass);
-        if (lane == 0 && wp) atomicAdd(a.pairs, (unsigned long long)wp);
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        __syncthreads();
-        for (int j = tid; j < TN; j += NT)
-            if (colCount[j]) {
-                atomicAdd(a.inRaw + colPoint[j], colCount[j]);
-                colCount[j] = 0;
-            }
-        // a timed-out wait anywhere in the CTA ends the CTA's work (uniformly)
-        if (__syncthreads_or(timedOut ? 1 : 0)) {
-            if (tid == 0) atomicExch(err, 1);
-            break;
-        }
     }
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+        // a stopped CTA may still have TMA loads in flight into its shared memory
+        for (long long it = bUsed; it < bIssued; ++it)
+            tc::mbar_wait(tc::smem_u32(&fullB[it % STAGES]), (uint32_t)((it / STAGES) & 1));
+        if (!tc::mbar_wait(tc::smem_u32(&doneBar), 0u)) atomicExch(err, 1);
+    }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
+}
+
+// Cb: the BF16 rows of every list's candidates, list-major, nct * 64 rows per
+// list (row ct * 64 + j = candidate ct * 64 + j of the list, zero past m), the
+// B operand of k_dist_tc as plain tiles.
+__global__ void k_gather_cand(const DistArgs a, const __nv_bfloat16* __restrict__ Xb, int ldb,
+                              __nv_bfloat16* __restrict__ Cb) {
+    const int rowsPerList = a.nct * TN, per = ldb / 8;
+    const size_t total = (size_t)2 * a.nproj * rowsPerList * per;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = i / per;
+        const int c8 = (int)(i % per) * 8;
+        const int l = (int)(row / rowsPerList), j = (int)(row % rowsPerList);
+        const int r = l % a.nproj, side = l / a.nproj;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (j < a.m) {
+            const int q = __ldg(a.topM + (size_t)r * 2 * a.m + side * a.m + j);
+            v = __ldg(reinterpret_cast<const uint4*>(Xb + (size_t)q * ldb + c8));
+        }
+        *reinterpret_cast<uint4*>(Cb + row * ldb + c8) = v;
+    }
 }
 
 // Exact re-decision of the queued pairs: a warp takes 32 queue entries, one
@@ -421,14 +543,26 @@ int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
-int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, uint64_t* queue, int64_t qcap,
-                   unsigned long long* qcount, int32_t* err, int grid, cudaStream_t st) {
+size_t dist_tc_cand_bytes(const DistArgs& a, int ldb) {
+    return sizeof(uint16_t) * (size_t)2 * a.nproj * a.nct * TN * ldb;
+}
+
+int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, void* Cb, uint64_t* queue, int64_t qcap,
+                   unsigned long long* qcount, int32_t* err, cudaStream_t st) {
+    if (ldb % TKB != 0 || (reinterpret_cast<uintptr_t>(Xb) & 15) || (reinterpret_cast<uintptr_t>(Cb) & 15)) return -1;
+    const int rows = 2 * a.nproj * a.nct * TN;
+    k_gather_cand<<<sm_count() * 8, 256, 0, st>>>(a, static_cast<const __nv_bfloat16*>(Xb), ldb,
+                                                  static_cast<__nv_bfloat16*>(Cb));
+    if (cudaPeekAtLastError() != cudaSuccess) return -1;
+    CUtensorMap tmC;
+    if (!tc::encode_bf16_2d(&tmC, Cb, rows, ldb, TKB, TN)) return -1;
     const size_t sm = (size_t)STAGES * STAGE_BYTES + 1024;
     auto kern = a.dists != nullptr ? k_dist_tc<true> : k_dist_tc<false>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return -1;
-    kern<<<grid, NT, sm, st>>>(a, static_cast<const __nv_bfloat16*>(Xb), ldb, queue, qcap, qcount, err);
-    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(a.nTiles, (int64_t)sm_count()));
+    kern<<<grid, NT, sm, st>>>(tmC, a, static_cast<const __nv_bfloat16*>(Xb), ldb, queue, qcap, qcount, err);
+    return cudaPeekAtLastError() == cudaSuccess ? 2 : -1;
 }
 
 int launch_screen_reset(const DistArgs& a, cudaStream_t st) {

@@ -91,6 +91,29 @@ __global__ void k_tile_keys(IndexArgs a) {
     atomicAdd(reinterpret_cast<unsigned long long*>(a.keyOff) + key, 1ull);
 }
 
+// The tensor-core distance kernel's order: tiles by (super-chunk of their
+// first member, list), a super-chunk being superChunk consecutive point
+// chunks.  The rows of a super-chunk stay in L2 while every list passes over
+// them, and the few tiles a list has there run back to back, so its candidate
+// rows are read once per super-chunk.
+__global__ void k_tile_keys_list(IndexArgs a, int superChunk, int32_t* keys, int64_t* keyOff) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.tileOff[2 * a.nproj]) return;
+    const int l = a.tileList[t];
+    const int mt = (int)((t - a.tileOff[l]) / a.nct);
+    const int sc = a.members[a.listOff[l] + (int64_t)mt * a.TM].x / a.chunkPts / superChunk;
+    const int key = sc * 2 * a.nproj + l;
+    keys[t] = key;
+    atomicAdd(reinterpret_cast<unsigned long long*>(keyOff) + key, 1ull);
+}
+
+__global__ void k_tile_perm_keys(IndexArgs a, const int32_t* keys, int64_t* keyOff, int32_t* perm) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.tileOff[2 * a.nproj]) return;
+    const unsigned long long pos = atomicAdd(reinterpret_cast<unsigned long long*>(keyOff) + keys[t], 1ull);
+    perm[pos] = (int32_t)t;
+}
+
 __global__ void k_tile_perm(IndexArgs a) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.tileOff[2 * a.nproj]) return;
@@ -249,6 +272,24 @@ int launch_tile_order(const IndexArgs& a, cudaStream_t st) {
     const int r = launch_scan_i64(a.keyOff, a.keyOff, (size_t)a.nChunks + 1, a.scanTmp, st);
     if (r < 0) return -1;
     k_tile_perm<<<g, 256, 0, st>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? r + 2 : -1;
+}
+
+size_t tile_order_list_keys(const IndexArgs& a, int superChunk) {
+    return (size_t)((a.nChunks + superChunk - 1) / superChunk) * 2 * a.nproj + 1;
+}
+
+int launch_tile_order_list(const IndexArgs& a, int superChunk, int32_t* keys, int64_t* keyOff, int32_t* perm,
+                           cudaStream_t st) {
+    if (a.maxTiles <= 0) return 0;
+    const size_t nk = tile_order_list_keys(a, superChunk);
+    if (cudaMemsetAsync(keyOff, 0, sizeof(int64_t) * nk, st) != cudaSuccess) return -1;
+    const unsigned g = (unsigned)((a.maxTiles + 255) / 256);
+    k_tile_keys_list<<<g, 256, 0, st>>>(a, superChunk, keys, keyOff);
+    if (cudaPeekAtLastError() != cudaSuccess) return -1;
+    const int r = launch_scan_i64(keyOff, keyOff, nk, a.scanTmp, st);
+    if (r < 0) return -1;
+    k_tile_perm_keys<<<g, 256, 0, st>>>(a, keys, keyOff, perm);
     return cudaPeekAtLastError() == cudaSuccess ? r + 2 : -1;
 }
 

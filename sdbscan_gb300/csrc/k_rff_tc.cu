@@ -40,9 +40,10 @@ constexpr uint32_t kIdesc = tc::idesc_bf16(BM, BN);
 
 __global__ void __launch_bounds__(NT, 2) k_rff_tc(const __grid_constant__ CUtensorMap tmX,
                                                  const __grid_constant__ CUtensorMap tmR, int n, int h, int nk,
-                                                 float* __restrict__ E, int32_t* __restrict__ err) {
+                                                 float* __restrict__ E, int32_t* __restrict__ err,
+                                                 long long stallSpins) {
     extern __shared__ __align__(1024) unsigned char smraw[];
-    __shared__ uint64_t fullBar[STAGES], freeBar[STAGES], doneBar;
+    __shared__ uint64_t fullBar[STAGES], freeBar[STAGES], doneBar, neverBar;
     __shared__ uint32_t tmemBase;
     const int tid = threadIdx.x, warp = tid >> 5;
     const uint32_t base = (tc::smem_u32(smraw) + 1023u) & ~1023u;  // 1024-aligned operand tiles
@@ -54,6 +55,7 @@ __global__ void __launch_bounds__(NT, 2) k_rff_tc(const __grid_constant__ CUtens
             tc::mbar_init(tc::smem_u32(&freeBar[s]), 1);
         }
         tc::mbar_init(tc::smem_u32(&doneBar), 1);
+        tc::mbar_init(tc::smem_u32(&neverBar), 1);  // the stall test's barrier: nothing arrives on it
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     if (warp == 0) {
@@ -83,7 +85,9 @@ __global__ void __launch_bounds__(NT, 2) k_rff_tc(const __grid_constant__ CUtens
         const int nkAll = 3 * nk;
         for (int kc = 0; kc < nkAll && kc < STAGES; ++kc) load(kc);
         int committed = 0;
-        for (int kc = 0; kc < nkAll; ++kc) {
+        // the stall test: a producer that never delivers, with loads in flight
+        if (stallSpins > 0 && !tc::stall_wait(tc::smem_u32(&neverBar), stallSpins)) failed = 1;
+        for (int kc = 0; kc < nkAll && !failed; ++kc) {
             const int s = kc % STAGES;
             if (!tc::mbar_wait(tc::smem_u32(&fullBar[s]), (uint32_t)(landed[s] & 1))) {
                 failed = 1;
@@ -164,7 +168,8 @@ __global__ void __launch_bounds__(NT, 2) k_rff_tc(const __grid_constant__ CUtens
 // Xs: n x 2 ldb BF16 points ([hi | lo] per row), Rs: h x 2 ldb BF16 rows of R
 // likewise (ldb a multiple of 64, zero padded past d, 16-byte aligned);
 // E: n x 2h FP32.
-int launch_rff_tc(const void* Xs, const void* Rs, int n, int h, int ldb, float* E, int32_t* err, cudaStream_t st) {
+int launch_rff_tc(const void* Xs, const void* Rs, int n, int h, int ldb, float* E, int32_t* err, long long stallSpins,
+                  cudaStream_t st) {
     if (ldb % BK != 0 || (reinterpret_cast<uintptr_t>(Xs) & 15) || (reinterpret_cast<uintptr_t>(Rs) & 15)) return -1;
     CUtensorMap tmX, tmR;
     if (!tc::encode_bf16_2d(&tmX, Xs, n, 2 * ldb, BK, BM) || !tc::encode_bf16_2d(&tmR, Rs, h, 2 * ldb, BK, BN))
@@ -173,7 +178,7 @@ int launch_rff_tc(const void* Xs, const void* Rs, int n, int h, int ldb, float* 
     if (cudaFuncSetAttribute(k_rff_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return -1;
     dim3 grid((n + BM - 1) / BM, (h + BN - 1) / BN);
-    k_rff_tc<<<grid, NT, sm, st>>>(tmX, tmR, n, h, ldb / BK, E, err);
+    k_rff_tc<<<grid, NT, sm, st>>>(tmX, tmR, n, h, ldb / BK, E, err, stallSpins);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 

@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(NT, 1) k_sng_tc(const __grid_constant__ CUtens
                                                  int64_t tiles, uint64_t* __restrict__ queue, int64_t qcap,
                                                  unsigned long long* __restrict__ qcount, int32_t* __restrict__ gate) {
     extern __shared__ __align__(1024) unsigned char smraw[];
-    __shared__ uint64_t fullBar[STAGES], emptyBar[STAGES], tfullBar[2], temptyBar[2], epiBar[2], doneBar;
+    __shared__ uint64_t fullBar[STAGES], emptyBar[STAGES], tfullBar[2], temptyBar[2], epiBar[2], doneBar, neverBar;
     __shared__ uint32_t tmemBase;
     __shared__ int colCount[2][BN];
     __shared__ volatile int abortFlag;
@@ -75,6 +75,7 @@ __global__ void __launch_bounds__(NT, 1) k_sng_tc(const __grid_constant__ CUtens
             tc::mbar_init(tc::smem_u32(&epiBar[b]), EPI_WARPS);
         }
         tc::mbar_init(tc::smem_u32(&doneBar), 1);
+        tc::mbar_init(tc::smem_u32(&neverBar), 1);  // the stall test's barrier: nothing arrives on it
         abortFlag = 0;
         loadsIssued = 0;
         loadsUsed = 0;
@@ -103,8 +104,8 @@ __global__ void __launch_bounds__(NT, 1) k_sng_tc(const __grid_constant__ CUtens
                 const int m0 = (int)(t / nbt) * BM, n0 = (int)(t % nbt) * BN;
                 for (int kc = 0; kc < nk; ++kc, ++it) {
                     const int s = (int)(it % STAGES);
-                    if (it >= STAGES &&
-                        !tc::mbar_wait(tc::smem_u32(&emptyBar[s]), (uint32_t)(((it / STAGES) - 1) & 1))) {
+                    if (it >= STAGES && !tc::mbar_wait_or(tc::smem_u32(&emptyBar[s]),
+                                                          (uint32_t)(((it / STAGES) - 1) & 1), &abortFlag)) {
                         stop();
                         break;
                     }
@@ -123,16 +124,18 @@ __global__ void __launch_bounds__(NT, 1) k_sng_tc(const __grid_constant__ CUtens
             int i = 0;
             for (int64_t t = blockIdx.x; t < tiles && !abortFlag; t += gridDim.x, ++i) {
                 const int buf = i & 1;
-                if (i >= 2 && !tc::mbar_wait(tc::smem_u32(&temptyBar[buf]), (uint32_t)(((i >> 1) - 1) & 1))) {
+                if (i >= 2 && !tc::mbar_wait_or(tc::smem_u32(&temptyBar[buf]), (uint32_t)(((i >> 1) - 1) & 1),
+                                                &abortFlag)) {
                     stop();
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                 const uint32_t acc = tmem + (uint32_t)(buf * BN);
-                bool bad = false;
-                for (int kc = 0; kc < nk; ++kc, ++it) {
+                // the stall test: a producer that never delivers, with loads in flight
+                bool bad = i == 0 && a.stallSpins > 0 && !tc::stall_wait(tc::smem_u32(&neverBar), a.stallSpins);
+                for (int kc = 0; kc < nk && !bad; ++kc, ++it) {
                     const int s = (int)(it % STAGES);
-                    if (!tc::mbar_wait(tc::smem_u32(&fullBar[s]), (uint32_t)((it / STAGES) & 1))) {
+                    if (!tc::mbar_wait_or(tc::smem_u32(&fullBar[s]), (uint32_t)((it / STAGES) & 1), &abortFlag)) {
                         bad = true;
                         break;
                     }
@@ -159,7 +162,7 @@ __global__ void __launch_bounds__(NT, 1) k_sng_tc(const __grid_constant__ CUtens
         for (int64_t t = blockIdx.x; t < tiles && !abortFlag; t += gridDim.x, ++i) {
             const int buf = i & 1;
             const int m0 = (int)(t / nbt) * BM, n0 = (int)(t % nbt) * BN, bt = (int)(t % nbt);
-            if (!tc::mbar_wait(tc::smem_u32(&tfullBar[buf]), (uint32_t)((i >> 1) & 1))) {
+            if (!tc::mbar_wait_or(tc::smem_u32(&tfullBar[buf]), (uint32_t)((i >> 1) & 1), &abortFlag)) {
                 stop();
                 break;
             }
@@ -232,7 +235,7 @@ __global__ void __launch_bounds__(NT, 1) k_sng_tc(const __grid_constant__ CUtens
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(tc::smem_u32(&epiBar[buf]));
             if (ew == 0) {  // every epilogue warp is done with this tile: flush its column counts
-                if (!tc::mbar_wait(tc::smem_u32(&epiBar[buf]), (uint32_t)((i >> 1) & 1))) {
+                if (!tc::mbar_wait_or(tc::smem_u32(&epiBar[buf]), (uint32_t)((i >> 1) & 1), &abortFlag)) {
                     stop();
                     break;
                 }

@@ -116,6 +116,14 @@ sdb_status sdb_engine::fit_sng(const float* X, bool xOnDevice, const float* epsL
     cudaError_t ce = cudaSetDevice(device);
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
 
+    // independent samples per block of points: the reference's law when its
+    // points draw apart (random_seed < 0), or when asked for
+    // (sngOptics: the reference draws every point's sample from its own
+    // std::random_device, so blocks unless a shared sample is asked for)
+    if (optics ? sngSampling != 1
+               : p.samplingProb < 1.0 && (sngSampling == 2 || (sngSampling == 0 && p.random_seed < 0)))
+        return fit_sng_blocks(X, xOnDevice, epsList, nEps, minPts, optics, labelsOut, nclOut);
+
     SngSample smp;
     sng_sample(n, p.samplingProb, (unsigned)seedUsed, optics, smp);
     const int nU = (int)smp.cols.size();
@@ -127,7 +135,7 @@ sdb_status sdb_engine::fit_sng(const float* X, bool xOnDevice, const float* epsL
     bool ok = true;
     if (!xOnDevice) ok &= ensure(Xin, sizeof(float) * (size_t)n * d);
     ok &= ensure(Xt, sizeof(float) * (size_t)n * ld) && ensure(scale, sizeof(float) * n) &&
-          ensure(errFlags, sizeof(int32_t) * 8) && ensure(counters, sizeof(unsigned long long) * 8) &&
+          ensure(errFlags, sizeof(int32_t) * kErrSlots) && ensure(counters, sizeof(unsigned long long) * 8) &&
           ensure(sngCols, sizeof(int32_t) * std::max(nU, 1)) && ensure(sngMult, sizeof(int32_t) * std::max(nU, 1)) &&
           ensure(sngColOf, sizeof(int32_t) * n) && ensure(sngExtras, sizeof(int2) * std::max(nExtra, 1)) &&
           ensure(sngExtraPass, std::max(nExtra, 1)) && ensure(rowDeg, sizeof(int32_t) * n) &&
@@ -162,7 +170,7 @@ sdb_status sdb_engine::fit_sng(const float* X, bool xOnDevice, const float* epsL
         SDB_CK(cudaMemcpyAsync(Xin.ptr, X, sizeof(float) * (size_t)n * d, cudaMemcpyHostToDevice, st));
     }
     SDB_CK(cudaEventRecord(ev[1], st));
-    SDB_CK(cudaMemsetAsync(errFlags.ptr, 0, sizeof(int32_t) * 8, st));
+    SDB_CK(cudaMemsetAsync(errFlags.ptr, 0, sizeof(int32_t) * kErrSlots, st));
     SDB_CK(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long) * 8, st));
     unsigned long long* ctr = static_cast<unsigned long long*>(counters.ptr);
     ProjectArgs pa{};
@@ -205,6 +213,7 @@ sdb_status sdb_engine::fit_sng(const float* X, bool xOnDevice, const float* epsL
     sa.extraPass = static_cast<uint8_t*>(sngExtraPass.ptr);
     sa.nExtra = nExtra;
     sa.err = i32(errFlags) + 6;
+    sa.stallSpins = dbgStallSpins;
     L_(launch_sng_col_of(sa, i32(sngColOf), st));
     // BF16 screening of the block (Cosine sngDbscan): BF16 copies of every
     // row and of the sampled rows, a queue for the pairs near eps
@@ -214,6 +223,7 @@ sdb_status sdb_engine::fit_sng(const float* X, bool xOnDevice, const float* epsL
     std::vector<uint64_t> heavy;  // per 64-column word: the columns drawn more than once
     if (screen) {
         qcap = std::min<int64_t>((int64_t)1 << 31, std::max<int64_t>((int64_t)1 << 22, (int64_t)n * nU / 16));
+        if (dbgQueueCap > 0) qcap = dbgQueueCap;
         if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * ldb) || !ensure(sngUb, sizeof(uint16_t) * (size_t)nU * ldb) ||
             !ensure(queue, sizeof(uint64_t) * (size_t)qcap) || !ensure(sngHeavy, sizeof(uint64_t) * nct))
             return SDB_ERR_NOMEM;
@@ -301,14 +311,14 @@ sdb_status sdb_engine::fit_sng(const float* X, bool xOnDevice, const float* epsL
         ca.coreDist = f32(coreDist);
         L_(launch_core_dist(ca, i64(nbOff), f32(nbDist), st));
         if (!ok) return fail(SDB_ERR_CUDA, "neighbour list launch failed");
-        SDB_CK(cudaMemcpyAsync(hostErr, errFlags.ptr, sizeof(int32_t) * 8, cudaMemcpyDeviceToHost, st));
+        SDB_CK(cudaMemcpyAsync(hostErr, errFlags.ptr, sizeof(int32_t) * kErrSlots, cudaMemcpyDeviceToHost, st));
         SDB_CK(cudaStreamSynchronize(st));
         if (hostErr[6]) return fail(SDB_ERR_INTERNAL, "sngOptics neighbour list overflow");
         sdb_status s = optics_order(total);
         if (s != SDB_OK) return s;
     }
     SDB_CK(cudaEventRecord(ev[7], st));
-    SDB_CK(cudaMemcpyAsync(hostErr, errFlags.ptr, sizeof(int32_t) * 8, cudaMemcpyDeviceToHost, st));
+    SDB_CK(cudaMemcpyAsync(hostErr, errFlags.ptr, sizeof(int32_t) * kErrSlots, cudaMemcpyDeviceToHost, st));
     SDB_CK(cudaMemcpyAsync(hostCounters, counters.ptr, sizeof(unsigned long long) * 8, cudaMemcpyDeviceToHost, st));
     SDB_CK(cudaEventRecord(ev[8], st));
     SDB_CK(cudaStreamSynchronize(st));
@@ -340,10 +350,198 @@ sdb_status sdb_engine::fit_sng(const float* X, bool xOnDevice, const float* epsL
     return SDB_OK;
 }
 
+// sngDbscan with independent samples per block of sng_block_rows() points
+// (k_sng_blocks.cu): transform, then per eps the pass words, degrees and core
+// flags, the union-find over the core-core passes, border minima and labels.
+sdb_status sdb_engine::fit_sng_blocks(const float* X, bool xOnDevice, const float* epsList, int nEps, int minPts,
+                                      bool optics, int32_t* labelsOut, int32_t* nclOut) {
+    const sdb_params& p = prm;
+    const int BR = sng_block_rows();
+    // draws per point: ceil(1.0 n prob) in double (src/sDbscan.cpp:432), for
+    // sngOptics ceil(prob n) in float (:1490)
+    const int64_t S = optics ? (int64_t)std::ceil(p.samplingProb * (float)n)
+                             : (int64_t)std::ceil(1.0 * n * p.samplingProb);
+    const int64_t nb = (n + BR - 1) / BR;
+    sngColsLast = 0;
+    sngExtraLast = 0;
+    bool ok = true;
+    if (!xOnDevice) ok &= ensure(Xin, sizeof(float) * (size_t)n * d);
+    ok &= ensure(Xt, sizeof(float) * (size_t)n * ld) && ensure(scale, sizeof(float) * n) &&
+          ensure(errFlags, sizeof(int32_t) * kErrSlots) && ensure(counters, sizeof(unsigned long long) * 8) &&
+          ensure(degree, sizeof(int32_t) * n) && ensure(core, n) && ensure(parent, sizeof(int32_t) * n) &&
+          ensure(border, sizeof(int32_t) * n) && ensure(rootFlag, sizeof(int64_t) * (n + 1)) &&
+          ensure(labels, sizeof(int32_t) * n) && ensure(nClusters, sizeof(int32_t) * 4) &&
+          ensure(scanTmp, sizeof(int64_t) * scan_tmp_elems((size_t)n + 1)) &&
+          ensure(sngWords, sizeof(uint32_t) * std::max<size_t>(1, (size_t)nb * (size_t)std::max<int64_t>(S, 0)));
+    if (optics)
+        ok &= ensure(nbOff, sizeof(int64_t) * (n + 1)) && ensure(coreDist, sizeof(float) * n) &&
+              ensure(hashOffB, sizeof(int64_t) * (n + 1));
+    if (!ok) return SDB_ERR_NOMEM;
+    cudaStream_t st = stream;
+    int launches = 0;
+    auto L_ = [&](int r) {
+        if (r < 0) ok = false;
+        else launches += r;
+    };
+#define SDB_CK(call)                                        \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+    SDB_CK(cudaEventRecord(ev[0], st));
+    const float* Xd = X;
+    if (!xOnDevice) {
+        Xd = static_cast<const float*>(Xin.ptr);
+        SDB_CK(cudaMemcpyAsync(Xin.ptr, X, sizeof(float) * (size_t)n * d, cudaMemcpyHostToDevice, st));
+    }
+    SDB_CK(cudaEventRecord(ev[1], st));
+    SDB_CK(cudaMemsetAsync(errFlags.ptr, 0, sizeof(int32_t) * kErrSlots, st));
+    SDB_CK(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long) * 8, st));
+    unsigned long long* ctr = static_cast<unsigned long long*>(counters.ptr);
+    ProjectArgs pa{};
+    pa.X = Xd;
+    pa.ldx = d;
+    pa.Xt = f32(Xt);
+    pa.ld = ld;
+    pa.n = n;
+    pa.d = d;
+    pa.dist = p.distance;
+    pa.scale = f32(scale);
+    pa.err = i32(errFlags);
+    L_(launch_transform(pa, st));
+    SDB_CK(cudaEventRecord(ev[2], st));
+    SDB_CK(cudaEventRecord(ev[3], st));
+    SDB_CK(cudaEventRecord(ev[4], st));
+    // splitmix64 of the seed, the key of every block's draws
+    uint64_t key = (uint64_t)(uint32_t)seedUsed + 0x9E3779B97F4A7C15ull;
+    key = (key ^ (key >> 30)) * 0xBF58476D1CE4E5B9ull;
+    key = (key ^ (key >> 27)) * 0x94D049BB133111EBull;
+    key ^= key >> 31;
+    SngBlockArgs ba{};
+    ba.Xt = f32(Xt);
+    ba.ld = ld;
+    ba.d = d;
+    ba.dist = p.distance;
+    ba.n = n;
+    ba.S = std::max<int64_t>(S, 0);
+    ba.key = key;
+    ba.words = static_cast<uint32_t*>(sngWords.ptr);
+    ba.degree = i32(degree);
+    ba.pairs = ctr + 3;
+    ba.err = i32(errFlags) + 6;
+    if (optics) {
+        // passes with repeats -> table sizes -> the emitting pass into the
+        // tables -> distinct lists, core flags and core distances -> ordering
+        ba.eps = epsList[0];
+        SDB_CK(cudaMemsetAsync(degree.ptr, 0, sizeof(int32_t) * n, st));
+        L_(launch_sngb_pass(ba, minPts, static_cast<uint8_t*>(core.ptr), st));
+        L_(launch_sngb_caps(ba, i64(hashOffB), st));
+        L_(launch_scan_i64(i64(hashOffB), i64(hashOffB), (size_t)n + 1, i64(scanTmp), st));
+        if (!ok) return fail(SDB_ERR_CUDA, "sampled-block launch failed");
+        int64_t slots = 0;
+        SDB_CK(cudaMemcpyAsync(&slots, i64(hashOffB) + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        SDB_CK(cudaStreamSynchronize(st));
+        if (!ensure(hashIdB, sizeof(int32_t) * std::max<int64_t>(slots, 1)) ||
+            !ensure(hashDistB, sizeof(float) * std::max<int64_t>(slots, 1)))
+            return SDB_ERR_NOMEM;
+        SDB_CK(cudaMemsetAsync(hashIdB.ptr, 0xFF, sizeof(int32_t) * std::max<int64_t>(slots, 1), st));
+        ba.hashOff = i64(hashOffB);
+        ba.hashId = i32(hashIdB);
+        ba.hashDist = f32(hashDistB);
+        L_(launch_sngb_emit(ba, st));
+        SDB_CK(cudaEventRecord(ev[5], st));
+        L_(launch_sngb_distinct(ba, minPts, i32(degree), static_cast<uint8_t*>(core.ptr), st));
+        SDB_CK(cudaMemsetAsync(nbOff.ptr, 0, sizeof(int64_t) * (n + 1), st));
+        L_(launch_i32_to_i64(i32(degree), i64(nbOff), n, st));
+        L_(launch_scan_i64(i64(nbOff), i64(nbOff), (size_t)n + 1, i64(scanTmp), st));
+        if (!ok) return fail(SDB_ERR_CUDA, "sampled-block launch failed");
+        int64_t total = 0;
+        SDB_CK(cudaMemcpyAsync(&total, i64(nbOff) + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        SDB_CK(cudaStreamSynchronize(st));
+        if (!ensure(nbIdx, sizeof(int32_t) * std::max<int64_t>(total, 1)) ||
+            !ensure(nbDist, sizeof(float) * std::max<int64_t>(total, 1)))
+            return SDB_ERR_NOMEM;
+        L_(launch_sngb_compact(ba, i64(nbOff), i32(nbIdx), f32(nbDist), st));
+        CoreArgs ca{};
+        ca.n = n;
+        ca.minPts = minPts;
+        ca.core = static_cast<uint8_t*>(core.ptr);
+        ca.coreDist = f32(coreDist);
+        L_(launch_core_dist(ca, i64(nbOff), f32(nbDist), st));
+        SDB_CK(cudaEventRecord(ev[6], st));
+        if (!ok) return fail(SDB_ERR_CUDA, "sampled-block launch failed");
+        SDB_CK(cudaMemcpyAsync(hostErr, errFlags.ptr, sizeof(int32_t) * kErrSlots, cudaMemcpyDeviceToHost, st));
+        SDB_CK(cudaStreamSynchronize(st));
+        if (hostErr[6]) return fail(SDB_ERR_INTERNAL, "sngOptics neighbour table overflow");
+        sdb_status so = optics_order(total);
+        if (so != SDB_OK) return so;
+    }
+    for (int ei = 0; ei < nEps && !optics; ++ei) {
+        ba.eps = epsList[ei];
+        SDB_CK(cudaMemsetAsync(degree.ptr, 0, sizeof(int32_t) * n, st));
+        L_(launch_sngb_pass(ba, minPts, static_cast<uint8_t*>(core.ptr), st));
+        if (ei == 0) SDB_CK(cudaEventRecord(ev[5], st));
+        if (ei == 0) SDB_CK(cudaEventRecord(ev[6], st));
+        ClusterArgs ka{};
+        ka.n = n;
+        ka.core = static_cast<const uint8_t*>(core.ptr);
+        ka.parent = i32(parent);
+        ka.border = i32(border);
+        ka.rootFlag = i64(rootFlag);
+        ka.scanTmp = i64(scanTmp);
+        ka.labels = i32(labels);
+        ka.nClusters = i32(nClusters);
+        L_(launch_uf_init(i32(parent), i32(border), n, st));
+        if (ba.S > 0) L_(launch_sngb_union(ba, ka.core, i32(parent), st));
+        L_(launch_uf_compress(ka, st));
+        if (ba.S > 0) L_(launch_sngb_border(ba, ka.core, i32(parent), i32(border), st));
+        L_(launch_cluster_labels(ka, st));
+        if (!ok) return fail(SDB_ERR_CUDA, "sampled-block launch failed");
+        if (labelsOut) {
+            SDB_CK(cudaMemcpyAsync(labelsOut + (size_t)ei * n, labels.ptr, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                                   st));
+            SDB_CK(cudaMemcpyAsync(nclOut + ei, nClusters.ptr, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        }
+    }
+    SDB_CK(cudaEventRecord(ev[7], st));
+    SDB_CK(cudaMemcpyAsync(hostErr, errFlags.ptr, sizeof(int32_t) * kErrSlots, cudaMemcpyDeviceToHost, st));
+    SDB_CK(cudaMemcpyAsync(hostCounters, counters.ptr, sizeof(unsigned long long) * 8, cudaMemcpyDeviceToHost, st));
+    SDB_CK(cudaEventRecord(ev[8], st));
+    SDB_CK(cudaStreamSynchronize(st));
+#undef SDB_CK
+    launchCount = launches;
+    for (int i = 0; i < 8; ++i) cudaEventElapsedTime(&stageMs[i], ev[i], ev[i + 1]);
+    cudaEventElapsedTime(&stageMs[8], ev[0], ev[8]);
+    sdb_status s = check_flags();
+    if (s != SDB_OK) return s;
+    haveFit = true;
+    if (optics) haveOptics = true;
+    else haveLabels = true;
+    lastOptics = optics;
+    lastSng = true;
+    if (p.verbose) {
+        std::printf("sdbscan_gb300 %s fit (independent samples per %d-point block): n=%d d=%d dist=%s "
+                    "samplingProb=%g draws=%lld eps=%g minPts=%d\n",
+                    optics ? "sngOPTICS" : "sngDBSCAN", BR, n, d, dist_label(p.distance), p.samplingProb,
+                    (long long)ba.S, epsList[0], minPts);
+        const char* names[9] = {"upload", "transform", "-", "-", "distances", "-", "cluster", "readback", "total"};
+        for (int i = 0; i < 9; ++i) std::printf("  %-14s %9.3f ms\n", names[i], stageMs[i]);
+    }
+    err.clear();
+    return SDB_OK;
+}
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
 extern "C" {
+
+sdb_status sdb_set_sng_sampling(sdb_engine* e, int32_t mode) {
+    if (!e) return SDB_ERR_ARG;
+    if (mode < 0 || mode > 2) return e->fail(SDB_ERR_ARG, "sng sampling must be 0 (by seed), 1 (shared) or 2 (blocks)");
+    e->sngSampling = mode;
+    return SDB_OK;
+}
 
 sdb_status sdb_set_sng_params(sdb_engine* e, int32_t distance, float samplingProb, int32_t clusterNoise,
                               int32_t verbose, int32_t n_threads, int32_t random_seed) {

@@ -36,6 +36,28 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
+// Bounded wait of one role of a CTA whose other roles may stop: gives up as
+// soon as *abortFlag is set, or after `limit` polls.  Returns false then.
+// (Drains -- waits for the CTA's own copies and MMAs before it frees shared
+// or tensor memory -- use mbar_wait: they always complete.)
+__device__ __forceinline__ bool mbar_wait_or(uint32_t bar, uint32_t parity, const volatile int* abortFlag,
+                                             long long limit = kWaitLimit) {
+    for (long long it = 0; it < limit; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 31) == 31 && *abortFlag) return false;
+    }
+    return false;
+}
+
+// The stall test (sdb_set_debug_limits): a wait on a barrier that nothing
+// arrives on, bounded by `spins` polls; always returns false.  It stands in
+// for a producer that stopped, so that the caller's failure path runs.
+__device__ __forceinline__ bool stall_wait(uint32_t neverBar, long long spins) {
+    for (long long it = 0; it < spins; ++it)
+        if (mbar_try_wait(neverBar, 0u)) return true;
+    return false;
+}
+
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
 }

@@ -52,6 +52,7 @@ def test_null_engine_is_rejected(lib):
     assert lib.sdb_set_params(None, None) == 1
     assert lib.sdb_fit_sdbscan(None, None, ctypes.c_float(0.1), 5) == 1
     assert lib.sdb_last_error(None) == b"null engine"
+    assert lib.sdb_set_debug_limits(None, 0, 0, 0) == 1
 
 
 def test_load_txt_parses_like_fscanf(tmp_path):

@@ -453,3 +453,41 @@ def test_noise_labelling_sampled_matches_oracle(port):
     eng.fit_sdbscan(X, -1.0, minPts)  # no pair is within a negative eps
     labels, ncl = eng.labels()
     assert eng.core()[0].sum() == 0 and (labels == -1).all() and ncl == 2
+
+
+@pytest.mark.parametrize("dist,m,optics", [("Cosine", 50, False), ("Cosine", 70, False), ("L2", 50, False),
+                                           ("Chi2", 50, True)])
+def test_every_distance_tile_shape_gives_the_same_bits(dist, m, optics):
+    """The plain distance kernel's tile shapes (sdb_set_tile_variant 1-5:
+    one CTA per tile with 64 or 50 columns, and the persistent
+    warp-specialised kernel with 4 or 6 stages) compute the same sequential
+    fmaf chains, so neighbourhood sizes, core flags and labels -- and for
+    sOPTICS every stored distance, hence the ordering and reachability -- are
+    identical to the default shape's."""
+    from sdbscan_gb300 import capi, datasets
+    if dist == "Chi2":
+        X = datasets.cfg4_dirichlet(8000, 96, seed=61)[0]
+        eps, minPts, kw = 0.3, 10, dict(ker_n_features=1024)
+    elif dist == "L2":
+        X = datasets.cfg3_aniso_l2(8000, 32, n_comp=8, scale=0.1, seed=62)[0]
+        eps, minPts, kw = 0.9, 10, dict(ker_n_features=256, ker_sigma=1.5)
+    else:
+        X = datasets.cfg1_cosine(12000, 64, seed=63)[0]
+        eps, minPts, kw = 0.15, 15, {}
+    eng = capi.Engine(*X.shape)
+    eng.set_params(n_proj=512, topK=6, topM=m, distance=dist, random_seed=8, **kw)
+    ref = None
+    for v in range(6):
+        eng.set_tile_variant(v)
+        if optics:
+            eng.fit_soptics(X, eps, minPts)
+            out = eng.optics() + eng.core() + (eng.core_dist(),)
+        else:
+            eng.fit_sdbscan(X, eps, minPts)
+            out = eng.labels() + eng.core()
+        assert eng.counters()["pairs"] > 0
+        if ref is None:
+            ref = out
+            continue
+        for a_, b_ in zip(out, ref):
+            np.testing.assert_array_equal(np.asarray(a_), np.asarray(b_), err_msg=f"variant {v}")

@@ -5,8 +5,9 @@ Parity bar: bit-exact.  sngDbscan with a seed >= 0 must give the reference's
 labels, n_clusters_, core flags and core neighbourhood sizes (golden
 fixtures made by the reference itself) and the oracle's neighbourhood sizes
 for every point; sngOptics must give the oracle's ordering, reachability,
-core flags, core distances and neighbourhood sizes (the same shared seeded
-sample; the reference's own sample comes from std::random_device).
+core flags, core distances and neighbourhood sizes under the same sampling
+rule (per 32-point block by default, as the reference's per-point
+std::random_device samples are independent; or one shared seeded sample).
 """
 import glob
 import json
@@ -138,17 +139,30 @@ OPTICS = [
 ]
 
 
+@pytest.mark.parametrize("mode", ["blocks", "shared"])
 @pytest.mark.parametrize("case", OPTICS, ids=[c[0] for c in OPTICS])
-def test_fit_sngoptics_matches_oracle(port, case):
+def test_fit_sngoptics_matches_oracle(port, case, mode):
+    """sngOptics under both sampling rules: per 32-point block (the default:
+    the reference samples every point independently) against the oracle's
+    orc_fit_sngoptics_blocks, and one shared sample (sdb_set_sng_sampling 1)
+    against orc_fit_sngoptics -- neighbourhood sizes, core flags, core
+    distances, ordering and reachability bit for bit."""
     _, distance, prob, eps, minPts, seed = case
     X = _data(distance, 2000)
     eng = _sng_engine(X, distance, prob, seed)
+    if mode == "shared":
+        eng.set_sng_sampling(1)
     eng.fit_sngoptics(X, eps, minPts)
     ordering, reach = eng.optics()
     core, deg = eng.core()
     cd = eng.core_dist()
-    o2, r2, c2, cd2, d2, _ = port.fit_sngoptics(X, eps, minPts, dist=distance, samplingProb=prob, seed=seed,
-                                                threads=8)
+    if mode == "shared":
+        o2, r2, c2, cd2, d2, _ = port.fit_sngoptics(X, eps, minPts, dist=distance, samplingProb=prob, seed=seed,
+                                                    threads=8)
+    else:
+        o2, r2, c2, cd2, d2 = port.fit_sngoptics_blocks(X, eps, minPts, dist=distance, samplingProb=prob,
+                                                        seed=seed, block_rows=32, threads=8)
+    assert c2.sum() > 0
     np.testing.assert_array_equal(deg, d2)
     np.testing.assert_array_equal(core, c2)
     np.testing.assert_array_equal(cd, cd2)
@@ -227,3 +241,62 @@ def test_pybind_sng_dropin(tmp_path):
     np.testing.assert_array_equal(np.asarray(dbs.ordering_), o)
     np.testing.assert_array_equal(np.asarray(dbs.reachability_, dtype=np.float32), r)
     eng.close()
+
+
+BLOCKS = [
+    ("cosine_p05", "Cosine", 0.05, 0.2, 10, 7),
+    ("l2_p10", "L2", 0.1, 0.6, 10, 8),
+    ("chi2_p05", "Chi2", 0.05, 0.25, 6, 9),
+    ("js_p02", "JS", 0.02, 0.3, 4, 10),
+    ("cosine_p0", "Cosine", 0.0, 0.2, 5, 11),
+]
+
+
+@pytest.mark.parametrize("case", BLOCKS, ids=[c[0] for c in BLOCKS])
+def test_fit_sngdbscan_blocks_matches_oracle(port, case):
+    """Independent samples per 32-point block (sdb_set_sng_sampling 2, the
+    rule of random_seed < 0): neighbourhood sizes with repeats, core flags,
+    labels and n_clusters_ equal the oracle's restatement of the rule
+    (orc_fit_sngdbscan_blocks) for the same seed, bit for bit."""
+    _, distance, prob, eps, minPts, seed = case
+    X = _data(distance, 3000)
+    eng = _sng_engine(X, distance, prob, seed)
+    eng.set_sng_sampling(2)
+    eng.fit_sngdbscan(X, eps, minPts)
+    labels, ncl = eng.labels()
+    core, deg = eng.core()
+    l2, n2, c2, d2 = port.fit_sngdbscan_blocks(X, eps, minPts, dist=distance, samplingProb=prob, seed=seed,
+                                               block_rows=32, threads=8)
+    np.testing.assert_array_equal(deg, d2)
+    np.testing.assert_array_equal(core, c2)
+    np.testing.assert_array_equal(labels, l2)
+    assert ncl == n2
+    if prob > 0:
+        assert core.sum() > 0
+    # sweeps: every eps equals a separate fit
+    lab_sw, ncl_sw = eng.fit_sngdbscan_sweep(X, [eps, 0.8 * eps], minPts)
+    np.testing.assert_array_equal(lab_sw[0], l2)
+    l3, n3, _, _ = port.fit_sngdbscan_blocks(X, 0.8 * np.float32(eps), minPts, dist=distance, samplingProb=prob,
+                                             seed=seed, block_rows=32, threads=8)
+    np.testing.assert_array_equal(lab_sw[1], l3)
+    eng.close()
+
+
+def test_unseeded_sngdbscan_draws_per_block():
+    """random_seed < 0 takes the block rule (independent samples, the
+    reference's law for clock-seeded points): about S forward and S reverse
+    draws per point, so the mean neighbourhood size (repeats counted) is
+    about twice the forward passes -- far above one shared sample's, where
+    only the sampled points get reverse draws."""
+    from sdbscan_gb300 import capi, datasets
+    X = datasets.cfg2_mnist_like(4000, 64, seed=12)[0]
+    degs = {}
+    for mode in (1, 0):
+        eng = capi.Engine(*X.shape)
+        eng.set_sng_params(distance="Cosine", samplingProb=0.05, random_seed=-1)
+        eng.set_sng_sampling(mode)
+        eng.fit_sngdbscan(X, 0.2, 10)
+        degs[mode] = eng.core()
+        eng.close()
+    # same law of forward passes; the block rule adds the reverse ones for every point
+    assert degs[0][0].sum() > 1.05 * degs[1][0].sum()
