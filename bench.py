@@ -718,9 +718,10 @@ def run_single_fit(args):
     """One fit on the config-2 law at n = args.single_fit points, with the
     engine's per-stage CUDA-event times and counters printed as one JSON
     line: the small, self-contained case the ncu captures in profiles/ run.
-    --fit sdbscan (d, distance: Cosine, or L1 / L2 / Chi2 with ker 1024,
-    sigma 1) or sng (sngDbscan, Cosine, samplingProb --prob); eps 0.25,
-    minPts 50, seed 42."""
+    --fit sdbscan / soptics / sweep (d, distance: Cosine, or L1 / L2 / Chi2
+    with ker 1024, sigma 1; --noise 1 for sDbscan-1NN), or sng / sngoptics
+    (Cosine, samplingProb --prob, --sng-sampling); eps 0.25, minPts 50,
+    seed 42."""
     import torch
 
     from sdbscan_gb300 import capi, datasets
@@ -728,17 +729,25 @@ def run_single_fit(args):
     X, _ = datasets.cfg2_mnist_like_torch(n, d, seed=2007, device="cuda")
     torch.cuda.synchronize()
     eng = capi.Engine(n, d)
-    if args.fit == "sng":
+    if args.fit in ("sng", "sngoptics"):
         eng.set_sng_params(distance=dist, samplingProb=args.prob, random_seed=42)
         eng.set_precision(args.precision)
-        eng.fit_sngdbscan_device(X.data_ptr(), 0.25, 50)
+        if args.sng_sampling:
+            eng.set_sng_sampling(args.sng_sampling)
+        if args.fit == "sngoptics":
+            eng.fit_sngoptics_device(X.data_ptr(), 0.25, 50)
+        else:
+            eng.fit_sngdbscan_device(X.data_ptr(), 0.25, 50)
     else:
         kw = dict(ker_n_features=1024, ker_sigma=1.0) if dist != "Cosine" else {}
-        eng.set_params(n_proj=1024, topK=10, topM=50, distance=dist, random_seed=42, precision=args.precision, **kw)
+        eng.set_params(n_proj=1024, topK=10, topM=50, distance=dist, random_seed=42, precision=args.precision,
+                       clusterNoise=args.noise, samplingProb=0.01, **kw)
         if args.tile_variant:
             eng.set_tile_variant(args.tile_variant)
         if args.fit == "soptics":
             eng.fit_soptics_device(X.data_ptr(), 0.25, 50)
+        elif args.fit == "sweep":  # test_sDbscan: 8 eps values, the index once (pinned host copy of X)
+            eng.fit_sdbscan_sweep(X.cpu().numpy(), [0.1, 0.125, 0.15, 0.175, 0.2, 0.225, 0.25, 0.275], 50)
         else:
             eng.fit_sdbscan_device(X.data_ptr(), 0.25, 50)
     print(json.dumps({"single_fit": args.fit, "n": n, "d": d, "distance": dist, "precision": args.precision,
@@ -765,7 +774,9 @@ def main():
                     help="(reference arm) one CPU fit of the whole workload, timed (minutes at 1M points)")
     ap.add_argument("--single-fit", type=int, default=0, metavar="N",
                     help="one fit of N points of the config-2 law, stage times printed (for profilers)")
-    ap.add_argument("--fit", default="sdbscan", choices=["sdbscan", "soptics", "sng"])
+    ap.add_argument("--fit", default="sdbscan", choices=["sdbscan", "soptics", "sweep", "sng", "sngoptics"])
+    ap.add_argument("--noise", type=int, default=0, help="clusterNoise (with --single-fit)")
+    ap.add_argument("--sng-sampling", type=int, default=0, help="0 by seed, 1 shared, 2 blocks (with --single-fit)")
     ap.add_argument("--precision", type=int, default=0, help="0 = FP32, 1 = BF16 (with --single-fit)")
     ap.add_argument("--d", type=int, default=784, help="dimensions (with --single-fit)")
     ap.add_argument("--distance", default="Cosine", help="distance (with --single-fit)")
