@@ -4,7 +4,7 @@
 // Same grouped, gathered formulation as k_dist (tile = list l, 128 member
 // rows, 64 candidate columns), with BF16 copies of the unit-norm rows as
 // operands and FP32 accumulation in tensor memory.  Persistent and
-// warp-specialised, one CTA per SM, 256 threads:
+// warp-specialised, one CTA per SM, 384 threads:
 //   warps 0-1  gather the tile's 128 member rows (A), 64 dimensions per stage,
 //              with cp.async into the 128-byte-swizzled K-major layout the MMA
 //              reads (8-row x 128-byte atoms, 16-byte chunk c of row r at
@@ -18,10 +18,12 @@
 //              K = 16) into one of two 128 x 64 FP32 accumulators in tensor
 //              memory and commits each stage back to its "empty" barrier, so
 //              the loaders refill it while later stages compute;
-//   warps 4-7  epilogue: tcgen05.ld of the other accumulator (warp w reads
-//              TMEM lanes 32 (w % 4)..), the eps decisions as bit words, the
-//              queue of pairs near eps, the column counts; it runs under the
-//              next tile's MMAs.
+//   warps 4-11 epilogue: tcgen05.ld of the other accumulator (warp w reads
+//              TMEM lanes 32 (w % 4).. and one half of the 64 columns), the
+//              eps decisions as bit words, the queue of pairs near eps, the
+//              column counts; the eight warps work independently (each writes
+//              its half of a row's mask word) and fetch the next tile's ids
+//              while this tile's MMAs run.
 // An 8-stage ring (24 KB per stage) runs ahead across tiles.  The CTA takes
 // the launch order's tiles b, b + grid, ..., so the tiles in flight stay in
 // one window of point chunks (L2 reuse of the gathered rows).
@@ -54,7 +56,7 @@ namespace {
 constexpr int TM = 128, TN = 64, TKB = 64;  // rows, candidate columns, bf16 per stage row (128 B)
 constexpr int STAGES = 8;
 constexpr int A_BYTES = TM * 128, B_BYTES = TN * 128, STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int NT = 256, EPI0 = 4;               // warps 0-1 A, 2 B, 3 MMA, 4-7 epilogue
+constexpr int NT = 384, EPI0 = 4;               // warps 0-1 A, 2 B, 3 MMA, 4-11 epilogue
 constexpr int A_LANES = 64;                     // threads gathering A
 constexpr float kMargin = 0.009f;
 constexpr uint32_t kTmemCols = 2 * TN;          // two accumulators
@@ -66,19 +68,6 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool v
 __device__ __forceinline__ void cp_async_arrive_noinc(uint32_t bar) {
     asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];\n" ::"r"(bar) : "memory");
 }
-// Named barrier 2 over the four epilogue warps; the OR form returns the same
-// value to all of them.
-__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 2, 128;\n" ::: "memory"); }
-__device__ __forceinline__ bool epi_or(bool v) {
-    uint32_t r;
-    asm volatile(
-        "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.or.pred p, 2, 128, q;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(r)
-        : "r"((uint32_t)v)
-        : "memory");
-    return r != 0;
-}
-
 // Swizzled byte offset of 16-byte chunk c (0..7) of row r in an operand tile.
 __device__ __forceinline__ uint32_t sw128(int r, int c) {
     return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
@@ -111,7 +100,7 @@ __global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUten
     extern __shared__ __align__(1024) unsigned char smraw[];
     __shared__ uint64_t fullA[STAGES], fullB[STAGES], emptyBar[STAGES], tfullBar[2], temptyBar[2], doneBar, neverBar;
     __shared__ uint32_t tmemBase;
-    __shared__ int colPoints[2][TN], colCount[2][TN];
+    __shared__ int colPts[8][32];  // each epilogue warp's 32 column ids of its current tile
     __shared__ volatile int abortFlag;
     __shared__ volatile long long bIssued, bUsed;
 
@@ -128,7 +117,7 @@ __global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUten
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(tc::smem_u32(&tfullBar[b]), 1);
-            tc::mbar_init(tc::smem_u32(&temptyBar[b]), 4);
+            tc::mbar_init(tc::smem_u32(&temptyBar[b]), 8);
         }
         tc::mbar_init(tc::smem_u32(&doneBar), 1);
         tc::mbar_init(tc::smem_u32(&neverBar), 1);  // the stall test's barrier: nothing arrives on it
@@ -137,7 +126,6 @@ __global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUten
         bUsed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    for (int i = tid; i < 2 * TN; i += NT) colCount[i / TN][i % TN] = 0;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
                          tc::smem_u32(&tmemBase)),
@@ -263,52 +251,61 @@ __global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUten
             tc::mma_commit(tc::smem_u32(&doneBar));  // arrives once every MMA issued above has completed
         }
     } else {
-        // ---------------- epilogue: thread et owns row et of the tile ----------------
-        const int et = tid - EPI0 * 32, quarter = warp & 3;
-        int i = 0;
-        for (int64_t b = blockIdx.x; b < total; b += gridDim.x, ++i) {
-            const int buf = i & 1;
-            const TileIds ti = tile_ids(a, b);
-            const int row = quarter * 32 + lane;  // TMEM lane = tile row
+        // ---------------- epilogue: eight independent warps ----------------
+        // Warp w reads TMEM lanes 32 (w % 4) .. + 31 (the tile's rows) and one
+        // half of the 64 columns (w >= 8: the upper half); a thread owns one
+        // row's 32 columns.  The next tile's ids are fetched while this tile's
+        // MMAs run, and nothing is shared with the other epilogue warps.
+        const int quarter = warp & 3, half = (warp - EPI0) >> 2;
+        const int row = quarter * 32 + lane;  // TMEM lane = tile row
+        int* colPt = colPts[warp - EPI0];
+        long long myPairs = 0;
+        auto fetch = [&](int64_t b, int& p, int& slot, int& cpt, TileIds& ti) {
+            ti = tile_ids(a, b);
             const int64_t q = ti.mbeg + row;
-            int p = -1, mySlot = 0;
+            p = -1;
+            slot = 0;
             if (q < ti.mend) {
                 const int2 mm = a.members[q];
                 p = mm.x;
-                mySlot = mm.y;
+                slot = mm.y;
             }
-            if (et < TN) {
-                const int side = ti.l / a.nproj, r = ti.l % a.nproj;
-                const int c = ti.ct * TN + et;
-                colPoints[buf][et] = c < a.m ? a.topM[(size_t)r * 2 * a.m + side * a.m + c] : -1;
-            }
-            // the column ids are in, the previous use of colCount[buf] is flushed,
-            // and every epilogue warp sees the same stop decision
-            if (epi_or(abortFlag != 0)) break;
-            const int* colPoint = colPoints[buf];
+            const int side = ti.l / a.nproj, r = ti.l % a.nproj;
+            const int c = ti.ct * TN + half * 32 + lane;
+            cpt = c < a.m ? __ldg(a.topM + (size_t)r * 2 * a.m + side * a.m + c) : -1;
+        };
+        int nP = -1, nSlot = 0, nCol = -1;
+        TileIds nTi{};
+        if ((int64_t)blockIdx.x < total) fetch(blockIdx.x, nP, nSlot, nCol, nTi);
+        int i = 0;
+        for (int64_t b = blockIdx.x; b < total && !abortFlag; b += gridDim.x, ++i) {
+            const int buf = i & 1;
+            const int p = nP, mySlot = nSlot, ct = nTi.ct;
+            __syncwarp();
+            colPt[lane] = nCol;
+            __syncwarp();
+            if (b + gridDim.x < total) fetch(b + gridDim.x, nP, nSlot, nCol, nTi);  // under this tile's MMAs
             if (!tc::mbar_wait_or(tc::smem_u32(&tfullBar[buf]), (uint32_t)((i >> 1) & 1), &abortFlag)) {
-                stop();  // the next tile's epi_or ends every epilogue warp
-                if (!SWEEP) epi_sync();
-                continue;
+                stop();
+                break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t tacc = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * TN);
-            const int ct = ti.ct;
-            uint64_t bits = 0;
-            int nPass = 0;
+            const uint32_t tacc =
+                tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * TN + half * 32);
+            const int cbase = ct * TN + half * 32;  // the tile's first column of this half, in list order
             if constexpr (SWEEP) {
 #pragma unroll 1
-                for (int c16 = 0; c16 < TN / 16; ++c16) {
+                for (int c16 = 0; c16 < 2; ++c16) {
                     float v[16];
                     tc::tmem_ld16(tacc + (uint32_t)(c16 * 16), v);
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
-                        const int col = c16 * 16 + j;
-                        const int qq = colPoint[col];
+                        const int col = c16 * 16 + j;  // within the half
+                        const int qq = colPt[col];
                         bool unsure = false;
                         if (p >= 0 && qq >= 0) {  // keep the screened distance, re-decide near any eps
                             const float dist = 1.0f - v[j];
-                            a.dists[((size_t)p * 2 * a.k + mySlot) * a.m + ct * TN + col] = dist;
+                            a.dists[((size_t)p * 2 * a.k + mySlot) * a.m + cbase + col] = dist;
                             if (p != qq)
                                 for (int e = 0; e < a.nSweep; ++e) unsure |= fabsf(dist - a.sweepEps[e]) <= kMargin;
                         }
@@ -322,7 +319,7 @@ __global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUten
                                 const unsigned long long at = at0 + __popc(um & ((1u << lane) - 1u));
                                 if ((int64_t)at < qcap)
                                     queue[at] = ((uint64_t)(uint32_t)p << 32) | ((uint32_t)mySlot << 16) |
-                                                (uint32_t)(ct * TN + col);
+                                                (uint32_t)(cbase + col);
                                 else
                                     atomicExch(err, 2);
                             }
@@ -333,79 +330,67 @@ __global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUten
                 __syncwarp();
                 if (lane == 0) tc::mbar_arrive(tc::smem_u32(&temptyBar[buf]));
             } else {
-                // The row's 64 decisions as bit words: pass (screened distance
+                // The row's 32 decisions as bit words: pass (screened distance
                 // below eps - margin), unsure (within the margin), near zero (the
                 // only place the point itself can be among the candidates); then
                 // the columns that do not exist, the row's own point and empty
                 // rows are masked out.
-                uint64_t uw = 0, zw = 0;
+                uint32_t bits = 0, uw = 0, zw = 0;
                 const float lo = a.eps - kMargin, hi = a.eps + kMargin;
 #pragma unroll
-                for (int c16 = 0; c16 < TN / 16; ++c16) {
+                for (int c16 = 0; c16 < 2; ++c16) {
                     float v[16];
                     tc::tmem_ld16(tacc + (uint32_t)(c16 * 16), v);
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         const float dist = 1.0f - v[j];
                         const bool pass = dist <= lo;
-                        bits |= (uint64_t)pass << (c16 * 16 + j);
-                        uw |= (uint64_t)(!pass && dist <= hi) << (c16 * 16 + j);
-                        zw |= (uint64_t)(dist <= kMargin) << (c16 * 16 + j);
+                        bits |= (uint32_t)pass << (c16 * 16 + j);
+                        uw |= (uint32_t)(!pass && dist <= hi) << (c16 * 16 + j);
+                        zw |= (uint32_t)(dist <= kMargin) << (c16 * 16 + j);
                     }
                 }
                 // the accumulator is in registers: the MMAs may reuse it
                 asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
                 __syncwarp();
                 if (lane == 0) tc::mbar_arrive(tc::smem_u32(&temptyBar[buf]));
-                const int nvalid = a.m - ct * TN;
-                uint64_t keep = p < 0 ? 0ull : (nvalid >= 64 ? ~0ull : (1ull << nvalid) - 1ull);
-                for (uint64_t z = zw & keep & (bits | uw); z; z &= z - 1) {  // rare: is the row's point a candidate?
-                    const int col = __ffsll((long long)z) - 1;
-                    if (colPoint[col] == p) keep &= ~(1ull << col);
+                const int nvalid = a.m - cbase;
+                uint32_t keep = p < 0 || nvalid <= 0 ? 0u : (nvalid >= 32 ? ~0u : (1u << nvalid) - 1u);
+                for (uint32_t z = zw & keep & (bits | uw); z; z &= z - 1) {  // rare: is the row's point a candidate?
+                    const int col = __ffs(z) - 1;
+                    if (colPt[col] == p) keep &= ~(1u << col);
                 }
                 bits &= keep;
                 uw &= keep;
                 if (__any_sync(0xffffffffu, uw != 0)) {  // pairs within the margin go to the queue
-                    const int cnt = __popcll(uw);
+                    const int cnt = __popc(uw);
                     if (cnt) {
                         unsigned long long at = atomicAdd(qcount, (unsigned long long)cnt);
-                        for (uint64_t u = uw; u; u &= u - 1, ++at) {
-                            const int col = __ffsll((long long)u) - 1;
+                        for (uint32_t u = uw; u; u &= u - 1, ++at) {
+                            const int col = __ffs(u) - 1;
                             if ((int64_t)at < qcap)
                                 queue[at] = ((uint64_t)(uint32_t)p << 32) | ((uint32_t)mySlot << 16) |
-                                            (uint32_t)(ct * TN + col);
+                                            (uint32_t)(cbase + col);
                             else
                                 atomicExch(err, 2);
                         }
                     }
                 }
-                nPass = __popcll(bits);
-                int cc0 = 0, cc1 = 0;  // passes of columns lane and lane + 32
+                // this half of the row's 64-bit mask word (little endian: columns 0-31 low)
+                if (p >= 0)
+                    reinterpret_cast<uint32_t*>(a.masks)[(((size_t)p * 2 * a.k + mySlot) * a.W + ct) * 2 + half] = bits;
+                myPairs += __popc(bits);
+                int cc = 0;  // passes of column `lane` of this half over the warp's 32 rows
 #pragma unroll
-                for (int col = 0; col < TN; ++col) {
-                    const int pc = __popc(__ballot_sync(0xffffffffu, (bits >> col) & 1ull));
-                    if (lane == (col & 31)) {
-                        if (col < 32) cc0 += pc;
-                        else cc1 += pc;
-                    }
+                for (int col = 0; col < 32; ++col) {
+                    const int pc = __popc(__ballot_sync(0xffffffffu, (bits >> col) & 1u));
+                    if (lane == col) cc = pc;
                 }
-                if (cc0) atomicAdd(&colCount[buf][lane], cc0);
-                if (cc1) atomicAdd(&colCount[buf][lane + 32], cc1);
-                if (p >= 0) a.masks[((size_t)p * 2 * a.k + mySlot) * a.W + ct] = bits;
-            }
-            const int wp = warp_sum(nPass);
-            if (lane == 0 && wp) atomicAdd(a.pairs, (unsigned long long)wp);
-            if constexpr (!SWEEP) {
-                epi_sync();  // every warp's column counts for this tile are in
-                if (et < TN) {
-                    const int cnt = colCount[buf][et];
-                    if (cnt) {
-                        atomicAdd(a.inRaw + colPoint[et], cnt);
-                        colCount[buf][et] = 0;
-                    }
-                }
+                if (cc) atomicAdd(a.inRaw + colPt[lane], cc);
             }
         }
+        const int wp = warp_sum((int)myPairs);
+        if (lane == 0 && wp) atomicAdd(a.pairs, (unsigned long long)wp);
     }
     __syncthreads();
     if (tid == 0) {
