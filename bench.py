@@ -56,6 +56,12 @@ FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # nominal FP32 CUDA-core peak
 # `python bench.py --single-fit 1000000 --precision 0` (profiles/k_dist_fp32_cfg2.md):
 # 23.29 GB read + 0.370 GB written (tiles run in point-chunk order).
 K_DIST_TRAFFIC_1M = 23.29e9 + 0.370e9
+# One CPU fit of the whole 1M x 784 config-2 workload (the reference arm's code,
+# all 16 host cores of the GPU machine): `python bench.py --impl reference
+# --cpu-full-fit`, recorded in profiles/cpu_full_fit_cfg2_1Mx784.md (23 minutes,
+# too long to repeat inside a benchmark run).
+CPU_FULL_FIT_CFG2 = {"seconds": 1389.7, "value": 719.6, "unit": "points/s", "cores": 16, "kind": "port",
+                     "source": "profiles/cpu_full_fit_cfg2_1Mx784.md"}
 # sngDBSCAN, the reference's sampling baseline that its benchmark loop runs
 # next to fit_sDbscan (src/main.cpp:57-73): samplingProb 0.01 (the default,
 # 10,000 draws per point at 1M points), seed 42, the workload's eps / minPts.
@@ -679,6 +685,8 @@ def run_ours(args, cfg):
                                 str(args.config), "--steps", "2", "--warmup", "1", "--cpu-sample",
                                 str(args.cpu_sample)])
         cpu = ref.get("cpu_baseline") if ref else None
+        if cpu is not None and cfg["workload"].startswith("cfg2"):
+            cpu = dict(cpu, full_fit=CPU_FULL_FIT_CFG2)  # the same config, all 1M points, recorded once
     line = {
         "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
