@@ -85,6 +85,22 @@ def _dist_env():
     return ws, rank, local
 
 
+def _h2d_copy_ms(src_pinned, dst, reps=3):
+    """Best of `reps` plain host -> device copies of a pinned tensor (CUDA events)."""
+    import torch
+    best = None
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        dst.copy_(src_pinned, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1)
+        best = t if best is None else min(best, t)
+    return best
+
+
 def _max_over_ranks(x: float, ws: int, device) -> float:
     """The largest of every rank's x: a replicated job takes its slowest
     replica's time."""
@@ -357,8 +373,11 @@ def run_batched(args, local, cpu=True):
         e.close()
     rate = lambda sec: total_n * len(eps_list) / sec
     out = {"workload": "cfg5_64sets_x8eps", "value": rate(bms / 1e3), "unit": "point-clusterings/s",
-           "form": "BF16+recheck, one CUDA graph", "ms_per_batch": bms, "sets": len(sets), "points": total_n,
+           "form": "BF16+recheck, one CUDA graph (per set the autotuner keeps the screening or a plain tile "
+                   "shape, whichever ran the set's distance stage faster)",
+           "ms_per_batch": bms, "sets": len(sets), "points": total_n,
            "eps": [round(e, 2) for e in eps_list], "launches_per_batch": 1, "graph_lanes": blanes[0],
+           "screened_sets": blanes[1].count(0),
            "setup_s": bsetup, "labels_identical_to_plain": bf16_identical,
            "plain_graph": {"value": rate(pms / 1e3), "ms_per_batch": pms, "graph_lanes": planes[0],
                            "tile_variants": {str(v): planes[1].count(v) for v in sorted(set(planes[1]))},
@@ -649,6 +668,7 @@ def run_ours(args, cfg):
     e2e_value = _replica_rate(n, args.steps, ws, e2e_s)
     assert all(np.array_equal(a, b) for a, b in zip(res_e2e[:1], res[:1])), "host-input and device-input fits disagree"
     d2h = n * 8 if optics else n * 4 + 4
+    h2d_ms = _h2d_copy_ms(Xh_t, X)  # Xh_t holds X's own values, so X is unchanged
 
     sng = None
     if not args.no_sng and cfg["workload"].startswith("cfg2"):
@@ -703,7 +723,10 @@ def run_ours(args, cfg):
         "clocks": clk.summary(),
         "e2e": {"value": e2e_value, "unit": "points/s", "h2d_bytes_per_step": n * d * 4,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / args.steps,
-                "stage_ms": e2e_stages},
+                "stage_ms": e2e_stages,
+                "h2d_link": {"copy_ms": h2d_ms, "gbs": n * d * 4 / (h2d_ms / 1e3) / 1e9,
+                             "note": "one plain pinned-host -> device copy of the step's input on this box "
+                                     "(the upload floor of the step)"}},
         "gpu_launches": launches,
         "roofline": roofline,
         "cpu_baseline": cpu,

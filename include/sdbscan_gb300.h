@@ -269,12 +269,14 @@ const char* sdb_last_error(sdb_engine* e);
  * one CUDA graph and replayed with a single launch.  No reference counterpart
  * (the reference runs test_sDbscan per dataset, src/sDbscan.cpp:980-1039).
  * p->precision applies to every set (BF16: screened distances, labels equal
- * to FP32).
+ * to FP32, where the autotuner finds the screening faster than the plain
+ * tiles for that set).
  *   X_device[i]: d_i x n_i column-major data of set i, device memory, kept
  *                valid for the batch's lifetime
- * The batch plans every set once (sizing run; with FP32 precision and
- * topM <= 50 it also times the three distance tile shapes per set and keeps
- * the fastest, sdb_batch_tile_variant), then times graphs with 4, 8, 16, 32 and 64
+ * The batch plans every set once (sizing run; with topM <= 50 it also times
+ * the three plain distance tile shapes per set and, with BF16 precision, the
+ * tensor-core screening, and keeps the fastest, sdb_batch_tile_variant), then
+ * times graphs with 4, 8, 16, 32 and 64
  * sets in flight and keeps the fastest (sdb_batch_lanes).
  * sdb_batch_run replays it; sdb_batch_labels reads set i's labelling for eps
  * index j. */
@@ -285,9 +287,9 @@ sdb_status sdb_batch_create(int32_t n_sets, const int32_t* n_points, const int32
 sdb_status sdb_batch_run(sdb_batch* b, float* elapsed_ms);
 sdb_status sdb_batch_labels(sdb_batch* b, int32_t set, int32_t eps_index, int32_t* labels, int32_t* n_clusters);
 int32_t sdb_batch_lanes(sdb_batch* b);
-/* The plain distance kernel's tile shape the autotuner kept for set i (FP32
- * precision, topM <= 50; the shapes of sdb_set_tile_variant, 1..3); 0 = the
- * default rule (by topM); -1 for a bad index. */
+/* The distance stage the autotuner kept for set i (topM <= 50): a plain tile
+ * shape of sdb_set_tile_variant, 1..3, or 0 = the default (BF16 precision:
+ * the tensor-core screening; FP32: the shape by topM); -1 for a bad index. */
 int32_t sdb_batch_tile_variant(sdb_batch* b, int32_t set);
 void sdb_batch_destroy(sdb_batch* b);
 const char* sdb_batch_last_error(sdb_batch* b);

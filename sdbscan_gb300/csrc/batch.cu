@@ -5,8 +5,9 @@
 // every dataset's index, distances and per-eps core/cluster stages — into one
 // CUDA graph.  Datasets run on their engines' own streams; at most `lanes` of
 // them run at a time (set i waits for set i - lanes).  The batch's autotuner
-// picks, per set, the plain distance kernel's tile shape (timing the set's
-// sweep with each) and then the lane count (timing each candidate graph).
+// picks, per set, the distance stage's form (the plain kernel's tile shapes
+// and, in BF16 mode, the tensor-core screening, timing the set's sweep with
+// each) and then the lane count (timing each candidate graph).
 // sdb_batch_run replays the graph: one launch for all the clusterings.
 #include <cuda_runtime.h>
 
@@ -145,11 +146,23 @@ sdb_status sdb_batch_create(int32_t n_sets, const int32_t* n_points, const int32
             *out = b;
             return batch_fail(b, s, "set " + std::to_string(i) + ": " + e->err);
         }
-        // tile autotuner: when the set's distances run on the plain kernel and
-        // the tile shapes all apply (m <= 50), time the distance stage with each
-        if (q.precision == SDB_PREC_FP32 && q.topM <= 50) {
+        // tile autotuner: when the tile shapes all apply (m <= 50), time the
+        // set's distance stage with each plain shape and, in BF16 mode, with
+        // the tensor-core screening too; the set keeps the fastest (a sweep's
+        // screening re-decides the pairs near every eps, which on small sets
+        // of low dimension can cost more than it saves)
+        if (q.topM <= 50) {
             float best = 1e30f;
             int bestV = 0;
+            if (q.precision == SDB_PREC_BF16) {
+                s = e->fit(X_device[i], true, eps[0], minPts, false, &sw);
+                if (s != SDB_OK) {
+                    *out = b;
+                    return batch_fail(b, s, "set " + std::to_string(i) + ": " + e->err);
+                }
+                best = e->stageMs[4];
+                e->prm.precision = SDB_PREC_FP32;
+            }
             for (int v : {1, 2, 3}) {
                 e->distVariant = v;
                 s = e->fit(X_device[i], true, eps[0], minPts, false, &sw);
@@ -163,6 +176,7 @@ sdb_status sdb_batch_create(int32_t n_sets, const int32_t* n_points, const int32
                 }
             }
             e->distVariant = bestV;
+            if (bestV == 0) e->prm.precision = SDB_PREC_BF16;  // the screening won
         }
     }
     // autotune the number of datasets in flight

@@ -151,8 +151,12 @@ struct ProjectArgs {
     float* scale;        // n: per-point norm / sum (scratch)
     const double* compCosh;  // Chi2/JS: cosh(PI * c * L) for c = 1..components (host-computed)
     double ln4;              // JS: log(4.0) as the host computes it
+    uint16_t* Xb;            // Cosine, fhtDim <= 2048: BF16 copy of Xt (n x ldb, zero padded), or null
+    int ldb;                 // its row stride, <= fhtDim
 };
 int launch_project(const ProjectArgs& a, cudaStream_t st);
+// Chunks in one full wave of k_project (a block per chunk, four blocks per SM).
+inline int project_wave_chunks() { return sm_count() * 4; }
 // transformData alone into Xt (uses X, ldx, Xt, ld, n, d, dist, scale, err).
 int launch_transform(const ProjectArgs& a, cudaStream_t st);
 
@@ -262,6 +266,7 @@ struct DistArgs {
     long long stallSpins;       // > 0: the stall test (sdb_set_debug_limits)
     int nSweep;                 // BF16 sweep: eps values whose margins are re-decided exactly
     float sweepEps[16];
+    const float* sqNorm;        // L2 BF16 screening: per point, the squared norm of its row of Xt
 };
 constexpr int kMaxScreenedSweep = 16;
 int launch_dist(const DistArgs& a, cudaStream_t st);
@@ -276,7 +281,11 @@ int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream
 int launch_to_bf16_split(const float* Xt, int ld, int n, void* Xs, int ldb, cudaStream_t st);
 int launch_screen_reset(const DistArgs& a, cudaStream_t st);
 // BF16 screening: Cb (dist_tc_cand_bytes) receives the lists' candidate rows.
+// Cosine: Xb holds the BF16 rows (stride ldb); L2: the split [hi | lo] rows
+// (stride 2 ldb, launch_to_bf16_split) and a.sqNorm the squared row norms.
 size_t dist_tc_cand_bytes(const DistArgs& a, int ldb);
+// Squared norms of the rows of Xt (n x ld), any summation order (screening only).
+int launch_sq_norms(const float* Xt, int ld, int n, float* out, cudaStream_t st);
 int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, void* Cb, uint64_t* queue, int64_t qcap,
                    unsigned long long* qcount, int32_t* err, cudaStream_t st);
 int launch_recheck(const DistArgs& a, const uint64_t* queue, const unsigned long long* qcount, int64_t qcap,

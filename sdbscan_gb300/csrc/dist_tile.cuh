@@ -39,8 +39,12 @@ template <int DIST> __device__ __forceinline__ float acc_step(float acc, float a
     } else if (DIST == DIST_L1) {
         return __fadd_rn(acc, fabsf(__fsub_rn(a, b)));
     } else if (DIST == DIST_CHI2) {
-        if (a > 0.0f && b > 0.0f) acc = __fadd_rn(acc, __fdiv_rn(__fmul_rn(a, b), __fadd_rn(a, b)));
-        return acc;
+        // Branch-free: every lane divides (1 / 1 where an entry is not
+        // positive) and adds the term or +0; acc >= +0, so acc + 0 == acc and
+        // the sum is bit-identical to skipping the term.
+        const bool both = a > 0.0f && b > 0.0f;
+        const float q = __fdiv_rn(both ? __fmul_rn(a, b) : 1.0f, both ? __fadd_rn(a, b) : 1.0f);
+        return __fadd_rn(acc, both ? q : 0.0f);
     } else {  // JS with EPSILON = 1e-6 added to both (src/Utilities.h:248-266)
         const float x = __fadd_rn(a, 1e-6f), y = __fadd_rn(b, 1e-6f);
         const float l2 = 0.693147182464599609375f;  // (float)log(2.0)
@@ -67,16 +71,17 @@ template <int DIST> __device__ __forceinline__ float pair_distance(const float* 
     return finish<DIST>(acc);
 }
 
-// Exact Cosine distances of 32 pairs, one per lane of the calling warp:
-// rows[0..31] point at the lanes' first rows, rows[32..63] at their second
-// rows (transformed data, stride ld, zero padded; rows in the warp's shared
+// Exact distances of 32 pairs, one per lane of the calling warp: rows[0..31]
+// point at the lanes' first rows, rows[32..63] at their second rows
+// (transformed data, stride ld, zero padded; rows in the warp's shared
 // memory, written before the call and synchronised with __syncwarp).  Both
 // rows of every pair are staged through tile (64 x 33 floats of the warp's
 // shared memory) 32 dimensions at a time with coalesced loads, the next chunk
-// prefetched into registers; each lane runs its pair's sequential fmaf chain
-// in ascending dimension order (fmaf(0, 0, s) = s past d), the plain path's
-// arithmetic.  Returns 1 - dot.
-__device__ __forceinline__ float warp_staged_cosine(const float* const* rows, float (*tile)[33], int ld) {
+// prefetched into registers; each lane runs its pair's sequential chain in
+// ascending dimension order (a zero-padded dimension leaves it unchanged),
+// the plain path's arithmetic (acc_step, finish).
+template <int DIST>
+__device__ __forceinline__ float warp_staged(const float* const* rows, float (*tile)[33], int ld) {
     const int lane = threadIdx.x & 31;
     float stage[64];
 #pragma unroll
@@ -91,11 +96,19 @@ __device__ __forceinline__ float warp_staged_cosine(const float* const* rows, fl
 #pragma unroll
             for (int r = 0; r < 64; ++r) stage[r] = cn < ld ? __ldg(rows[r] + cn) : 0.0f;
         }
+        const int tn = min(32, ld - c);
+        if (tn == 32) {
 #pragma unroll
-        for (int t = 0; t < 32; ++t) s = __fmaf_rn(tile[lane][t], tile[32 + lane][t], s);
+            for (int t = 0; t < 32; ++t) s = acc_step<DIST>(s, tile[lane][t], tile[32 + lane][t]);
+        } else {
+            for (int t = 0; t < tn; ++t) s = acc_step<DIST>(s, tile[lane][t], tile[32 + lane][t]);
+        }
         __syncwarp();
     }
-    return __fsub_rn(1.0f, s);
+    return finish<DIST>(s);
+}
+__device__ __forceinline__ float warp_staged_cosine(const float* const* rows, float (*tile)[33], int ld) {
+    return warp_staged<DIST_COSINE>(rows, tile, ld);
 }
 
 // acc[i][j] = accumulated distance terms of (row ty + 16 i, column tx + TX j)

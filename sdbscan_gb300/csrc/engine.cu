@@ -114,8 +114,8 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &counters, &E, &Rt, &signs, &compCosh, &dists, &coreDist, &nbOff, &nbIdx, &nbDist, &nbFill, &hubIdx,
             &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig, &Rb, &newMasks, &coreEps, &sampleFlag,
             &noiseFlag, &noiseCores, &noisePts, &PcT, &numCore, &pairRound, &sngCols, &sngMult, &sngColOf, &sngExtras,
-            &sngExtraPass, &sngMask, &rowDeg, &colCnt, &sngUb, &sngHeavy, &chunkOff, &tileKey, &keyOff, &tilePerm, &Cb, &tileKeyTc, &keyOffTc, &tilePermTc, &sngWords, &hashOffB, &hashIdB,
-            &hashDistB};
+            &sngExtraPass, &sngMask, &rowDeg, &colCnt, &sngUb, &sngHeavy, &chunkOff, &tileKey, &keyOff, &tilePerm,
+            &Cb, &tileKeyTc, &keyOffTc, &tilePermTc, &sngWords, &hashOffB, &hashIdB, &hashDistB, &sqNorm};
 }
 
 // ---------------------------------------------------------------------------
@@ -214,7 +214,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     const int W = (m + 63) / 64;
     const int L = 2 * D;
     // top-m threshold chunks: eight full waves of projection blocks (4 per
-    // SM; half a wave per upload segment), and at least 4m chunks so the
+    // SM; a wave or more per upload segment), and at least 4m chunks so the
     // chunk maxima bound the m-th value
     const int chunksWanted = std::max(sm_count() * 4 * 8, 4 * m);
     const int chunk = std::max(8, (n + chunksWanted - 1) / chunksWanted);
@@ -223,6 +223,15 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     while (cap < 8 * m) cap <<= 1;
     const int64_t maxTiles = ((int64_t)n * 2 * k / TMr + L) * nct;
     const bool rff = p.distance == SDB_L1 || p.distance == SDB_L2;
+    // BF16 tensor-core screening of the candidate distances: Cosine sDBSCAN
+    // fits and eps sweeps of up to kMaxScreenedSweep values (the projection
+    // kernel writes the BF16 copy of the rows when it runs its register path),
+    // and L2 sDBSCAN fits (split-BF16 rows, made for the embedding GEMM)
+    const bool screen = p.precision == SDB_PREC_BF16 && !optics &&
+                        ((p.distance == SDB_COSINE && (!sweep || sw->nEps <= kMaxScreenedSweep)) ||
+                         (p.distance == SDB_L2 && !sweep));
+    const int ldb = (d + 63) / 64 * 64;
+    const bool fuseXb = screen && p.distance == SDB_COSINE && fhtDim <= 2048 && ldb <= fhtDim;
 
     // allocations (grow-only)
     bool ok = true;
@@ -321,6 +330,11 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     pa.scale = f32(scale);
     pa.compCosh = static_cast<const double*>(compCosh.ptr);
     pa.ln4 = ln4;
+    if (fuseXb) {
+        if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * ldb)) return SDB_ERR_NOMEM;
+        pa.Xb = static_cast<uint16_t*>(Xb.ptr);
+        pa.ldb = ldb;
+    }
     if (rff) {
         if (!capture)
             SDB_CK(cudaMemcpyAsync(Rt.ptr, hostRt.data(), sizeof(float) * hostRt.size(), cudaMemcpyHostToDevice, st));
@@ -330,7 +344,6 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         if (p.precision == SDB_PREC_BF16) {
             // the embedding GEMM on the tensor cores from split-BF16 copies of X
             // and R; the FP32 kernel after it runs only if the tensor-core one failed
-            const int ldb = (d + 63) / 64 * 64;
             if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * 2 * ldb) ||
                 !ensure(Rb, sizeof(uint16_t) * (size_t)h * 2 * ldb))
                 return SDB_ERR_NOMEM;
@@ -348,12 +361,11 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     if (overlapUpload) {
         const int segs = std::min(kUploadSegs, G);
         SDB_CK(cudaEventRecord(segEv[kUploadSegs], st));  // Xin is free once the stream got here
-        SDB_CK(cudaStreamWaitEvent(copyStream, segEv[kUploadSegs], 0));
-        SDB_CK(cudaStreamWaitEvent(copyStream2, segEv[kUploadSegs], 0));
+        for (int c = 0; c < kCopyStreams; ++c) SDB_CK(cudaStreamWaitEvent(copyStream[c], segEv[kUploadSegs], 0));
         for (int sgi = 0; sgi < segs; ++sgi) {
             const int cb = (int)((int64_t)G * sgi / segs), ce = (int)((int64_t)G * (sgi + 1) / segs);
             const size_t pb = (size_t)cb * chunk, pe = std::min<size_t>((size_t)n, (size_t)ce * chunk);
-            cudaStream_t cs = (sgi & 1) ? copyStream2 : copyStream;  // one cudaMemcpyAsync per segment
+            cudaStream_t cs = copyStream[sgi % kCopyStreams];  // one cudaMemcpyAsync per segment
             SDB_CK(cudaMemcpyAsync(static_cast<float*>(Xin.ptr) + pb * d, X + pb * d, sizeof(float) * (pe - pb) * d,
                                    cudaMemcpyHostToDevice, cs));
             SDB_CK(cudaEventRecord(segEv[sgi], cs));
@@ -468,24 +480,28 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     da.waitErr = i32(errFlags) + 8;
     da.stallSpins = dbgStallSpins;
     SDB_CK(cudaMemsetAsync(inRaw.ptr, 0, sizeof(int32_t) * n, st));
-    // BF16 tensor-core screening + exact FP32 re-decision near eps (Cosine
-    // sDBSCAN fits and eps sweeps of up to kMaxScreenedSweep values).  The
+    // BF16 tensor-core screening + exact FP32 re-decision near eps.  The
     // plain kernel is launched after it in every case and runs only if the
     // screening raised its flag (queue overflow or a timed-out wait), so the
     // stage needs no host synchronisation and can be captured in a graph.
-    if (p.precision == SDB_PREC_BF16 && p.distance == SDB_COSINE && !optics &&
-        (!sweep || sw->nEps <= kMaxScreenedSweep)) {
+    if (screen) {
         if (sweep) {  // ascending, as the rounds run
             da.nSweep = sw->nEps;
             for (int e = 0; e < sw->nEps; ++e) da.sweepEps[e] = sw->eps[e];
             std::sort(da.sweepEps, da.sweepEps + sw->nEps);
         }
-        const int ldb = (d + 63) / 64 * 64;
         const int64_t qcap = dbgQueueCap > 0 ? dbgQueueCap : std::max<int64_t>(1 << 20, (int64_t)n * 2 * k * m / 8);
-        if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * ldb) || !ensure(queue, sizeof(uint64_t) * (size_t)qcap) ||
-            !ensure(Cb, dist_tc_cand_bytes(da, ldb)))
+        const bool l2 = p.distance == SDB_L2;  // split rows [hi | lo] from stage 1, squared norms
+        if (!ensure(Xb, sizeof(uint16_t) * (size_t)n * (l2 ? 2 : 1) * ldb) ||
+            !ensure(queue, sizeof(uint64_t) * (size_t)qcap) || !ensure(Cb, dist_tc_cand_bytes(da, ldb)) ||
+            (l2 && !ensure(sqNorm, sizeof(float) * (size_t)n)))
             return SDB_ERR_NOMEM;
-        L_(launch_to_bf16(f32(Xt), ld, n, Xb.ptr, ldb, st));
+        if (l2) {
+            L_(launch_sq_norms(f32(Xt), ld, n, f32(sqNorm), st));
+            da.sqNorm = f32(sqNorm);
+        } else if (!fuseXb) {
+            L_(launch_to_bf16(f32(Xt), ld, n, Xb.ptr, ldb, st));
+        }
         // the tensor-core kernel takes the tiles by (super-chunk, list): the
         // rows of 8 point chunks stay in L2 while every list passes over them
         const size_t nKeys = tile_order_list_keys(ia, kSuperChunk);
@@ -734,12 +750,15 @@ sdb_status sdb_engine_create(int32_t n_points, int32_t n_features, int32_t devic
     e->d = n_features;
     e->device = device;
     sdb_params_default(&e->prm);
-    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&e->copyStream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&e->copyStream2, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
         sdb_engine_destroy(e);
         return SDB_ERR_CUDA;
     }
+    for (int c = 0; c < sdb_engine::kCopyStreams; ++c)
+        if (cudaStreamCreateWithFlags(&e->copyStream[c], cudaStreamNonBlocking) != cudaSuccess) {
+            sdb_engine_destroy(e);
+            return SDB_ERR_CUDA;
+        }
     for (int i = 0; i <= sdb_engine::kUploadSegs; ++i)
         if (cudaEventCreateWithFlags(&e->segEv[i], cudaEventDisableTiming) != cudaSuccess) {
             sdb_engine_destroy(e);
@@ -763,15 +782,15 @@ void sdb_engine_destroy(sdb_engine* e) {
     if (!e) return;
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
-    if (e->copyStream) cudaStreamSynchronize(e->copyStream);
-    if (e->copyStream2) cudaStreamSynchronize(e->copyStream2);
+    for (cudaStream_t cs : e->copyStream)
+        if (cs) cudaStreamSynchronize(cs);
     e->free_all();
     for (int i = 0; i < 9; ++i)
         if (e->ev[i]) cudaEventDestroy(e->ev[i]);
     for (int i = 0; i <= sdb_engine::kUploadSegs; ++i)
         if (e->segEv[i]) cudaEventDestroy(e->segEv[i]);
-    if (e->copyStream) cudaStreamDestroy(e->copyStream);
-    if (e->copyStream2) cudaStreamDestroy(e->copyStream2);
+    for (cudaStream_t cs : e->copyStream)
+        if (cs) cudaStreamDestroy(cs);
     if (e->hostErr) cudaFreeHost(e->hostErr);
     if (e->hostCounters) cudaFreeHost(e->hostCounters);
     if (e->stream) cudaStreamDestroy(e->stream);

@@ -58,11 +58,14 @@ struct sdb_engine {
     bool sngParamsSet = false;  // set_sngParams (enough for the sng fits)
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[9] = {};
-    // host input is uploaded in segments on two copy streams (alternating, so
-    // two copies are in flight), each segment's projection starting as soon
-    // as its rows have landed
-    static constexpr int kUploadSegs = 16;
-    cudaStream_t copyStream = nullptr, copyStream2 = nullptr;
+    // host input is uploaded in segments, spread round-robin over the copy
+    // streams, each segment's projection starting as soon as its rows have
+    // landed.  One stream: a single copy already runs at the host link's rate,
+    // and concurrent copies only delay each segment's arrival (1M x 784 from
+    // pinned memory: projection stage 15.7 ms with one stream, 21.0 with two,
+    // 23.9 with four, against 14.8 ms for the bare copy)
+    static constexpr int kUploadSegs = 16, kCopyStreams = 1;
+    cudaStream_t copyStream[kCopyStreams] = {};
     cudaEvent_t segEv[kUploadSegs + 1] = {};
     std::string err;
 
@@ -79,8 +82,8 @@ struct sdb_engine {
         rootFlag, labels, nClusters, scanTmp, errFlags, counters, E, Rt, signs, compCosh, dists, coreDist, nbOff,
         nbIdx, nbDist, nbFill, hubIdx, kMask, firstMasks, Xb, queue, sweepLabels, sweepNcl, sig, Rb, newMasks,
         coreEps, sampleFlag, noiseFlag, noiseCores, noisePts, PcT, numCore, pairRound, sngCols, sngMult, sngColOf,
-        sngExtras, sngExtraPass, sngMask, rowDeg, colCnt, sngUb, sngHeavy, chunkOff, tileKey, keyOff, tilePerm, Cb, tileKeyTc, keyOffTc, tilePermTc, sngWords, hashOffB,
-        hashIdB, hashDistB;
+        sngExtras, sngExtraPass, sngMask, rowDeg, colCnt, sngUb, sngHeavy, chunkOff, tileKey, keyOff, tilePerm, Cb,
+        tileKeyTc, keyOffTc, tilePermTc, sngWords, hashOffB, hashIdB, hashDistB, sqNorm;
 
     // results
     bool haveLabels = false, haveOptics = false, haveFit = false, lastOptics = false;

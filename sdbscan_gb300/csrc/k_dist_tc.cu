@@ -37,6 +37,18 @@
 // queue and is recomputed by k_recheck with the plain path's exact sequential
 // FP32 dot.  The resulting masks are identical to the plain FP32 path's.
 //
+// L2 (single fits): the operands are split BF16 copies, x = hi + lo + r with
+// |r| <= 2^-16 |x| elementwise; the member rows enter as [hi | lo | hi] and the
+// candidate rows as [hi | hi | lo], so one K = 3 d GEMM gives
+// hi.hi + lo.hi + hi.lo = x.y - e with |e| <= 3.02 * 2^-16 sum|x_i y_i|.  The
+// screened squared distance nx + ny - 2 v (nx, ny: squared row norms in FP32)
+// then differs from the reference's FP32 sum of squared differences by less
+// than tolRel (nx + ny) + tolAbs, with tolRel covering the split, the
+// tensor-core accumulation (K 2^-23), the norms (d 2^-23) and the FP32 updates,
+// and tolAbs the reference's own rounding and its sqrt near eps
+// (sum|x_i y_i| <= (nx + ny) / 2).  Pairs within that band of eps^2 are
+// re-decided exactly, as for Cosine.
+//
 // Every wait on an mbarrier is bounded.  A wait that runs out stops every
 // role (a shared abort flag) and raises the error flag, after which the plain
 // FP32 kernel redoes the stage; before freeing its tensor memory the CTA waits
@@ -45,6 +57,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cmath>
 
 #include "common.cuh"
 #include "dist_tile.cuh"
@@ -89,24 +102,30 @@ __device__ __forceinline__ TileIds tile_ids(const DistArgs& a, int64_t b) {
     return r;
 }
 
-// SWEEP: store the screened distance of every pair and queue the pairs near
-// any of the sweep's eps values (masks follow per eps from the distances);
-// otherwise decide against eps and write the masks.
-template <bool SWEEP>
+// SWEEP (Cosine): store the screened distance of every pair and queue the
+// pairs near any of the sweep's eps values (masks follow per eps from the
+// distances); otherwise decide against eps and write the masks.
+template <int DIST, bool SWEEP>
 __global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUtensorMap tmC, DistArgs a,
                                                   const __nv_bfloat16* __restrict__ Xb, int ldb,
                                                   uint64_t* __restrict__ queue, int64_t qcap,
-                                                  unsigned long long* __restrict__ qcount, int32_t* __restrict__ err) {
+                                                  unsigned long long* __restrict__ qcount, int32_t* __restrict__ err,
+                                                  float tolRel, float tolAbs) {
+    static_assert(DIST == DIST_COSINE || (DIST == DIST_L2 && !SWEEP), "screened distances: Cosine, L2 fits");
+    constexpr bool L2 = DIST == DIST_L2;
     extern __shared__ __align__(1024) unsigned char smraw[];
     __shared__ uint64_t fullA[STAGES], fullB[STAGES], emptyBar[STAGES], tfullBar[2], temptyBar[2], doneBar, neverBar;
     __shared__ uint32_t tmemBase;
     __shared__ int colPts[8][32];  // each epilogue warp's 32 column ids of its current tile
+    __shared__ float colNrm[8][32];  // L2: their squared norms
     __shared__ volatile int abortFlag;
     __shared__ volatile long long bIssued, bUsed;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t base = (tc::smem_u32(smraw) + 1023u) & ~1023u;  // 1024-aligned operand tiles
-    const int nk = ldb / TKB;
+    const int nkb = ldb / TKB;              // stages per operand segment
+    const int nk = (L2 ? 3 : 1) * nkb;      // L2: [hi | lo | hi] x [hi | hi | lo]
+    const int ldx = (L2 ? 2 : 1) * ldb;     // row stride of Xb
     const int64_t total = *a.tileTotal;
 
     if (tid == 0) {
@@ -153,7 +172,7 @@ __global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUten
 #pragma unroll
             for (int u = 0; u < 16; ++u) {
                 const int64_t q = ti.mbeg + 8 * u + (tid >> 3);
-                src[u] = q < ti.mend ? Xb + (size_t)__ldg(&a.members[q].x) * ldb + c * 8 : nullptr;
+                src[u] = q < ti.mend ? Xb + (size_t)__ldg(&a.members[q].x) * ldx + c * 8 : nullptr;
             }
             bool bad = false;
             for (int kc = 0; kc < nk; ++kc, ++it) {
@@ -165,10 +184,11 @@ __global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUten
                 }
                 if (abortFlag) break;
                 const uint32_t sA = base + s * STAGE_BYTES;
+                const int ks = L2 && kc >= 2 * nkb ? kc - 2 * nkb : kc;  // the stage's source chunk of the row
 #pragma unroll
                 for (int u = 0; u < 16; ++u) {
                     const int row = 8 * u + (tid >> 3);
-                    cp_async16(sA + sw128(row, c), src[u] != nullptr ? src[u] + kc * TKB : Xb, src[u] != nullptr);
+                    cp_async16(sA + sw128(row, c), src[u] != nullptr ? src[u] + ks * TKB : Xb, src[u] != nullptr);
                 }
                 cp_async_arrive_noinc(tc::smem_u32(&fullA[s]));
             }
@@ -259,6 +279,7 @@ __global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUten
         const int quarter = warp & 3, half = (warp - EPI0) >> 2;
         const int row = quarter * 32 + lane;  // TMEM lane = tile row
         int* colPt = colPts[warp - EPI0];
+        float* colN = colNrm[warp - EPI0];
         long long myPairs = 0;
         auto fetch = [&](int64_t b, int& p, int& slot, int& cpt, TileIds& ti) {
             ti = tile_ids(a, b);
@@ -283,7 +304,9 @@ __global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUten
             const int p = nP, mySlot = nSlot, ct = nTi.ct;
             __syncwarp();
             colPt[lane] = nCol;
+            if constexpr (L2) colN[lane] = nCol >= 0 ? __ldg(a.sqNorm + nCol) : 0.0f;
             __syncwarp();
+            const float nx = L2 && p >= 0 ? __ldg(a.sqNorm + p) : 0.0f;
             if (b + gridDim.x < total) fetch(b + gridDim.x, nP, nSlot, nCol, nTi);  // under this tile's MMAs
             if (!tc::mbar_wait_or(tc::smem_u32(&tfullBar[buf]), (uint32_t)((i >> 1) & 1), &abortFlag)) {
                 stop();
@@ -336,18 +359,31 @@ __global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUten
                 // the columns that do not exist, the row's own point and empty
                 // rows are masked out.
                 uint32_t bits = 0, uw = 0, zw = 0;
-                const float lo = a.eps - kMargin, hi = a.eps + kMargin;
 #pragma unroll
                 for (int c16 = 0; c16 < 2; ++c16) {
                     float v[16];
                     tc::tmem_ld16(tacc + (uint32_t)(c16 * 16), v);
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
-                        const float dist = 1.0f - v[j];
-                        const bool pass = dist <= lo;
+                        bool pass, near, zero;
+                        if constexpr (L2) {
+                            // squared distances against eps^2, within a per-pair band
+                            const float ny = colN[c16 * 16 + j];
+                            const float d2 = nx + ny - 2.0f * v[j];
+                            const float tol = tolRel * (nx + ny) + tolAbs;
+                            const float e2 = a.eps * a.eps;
+                            pass = d2 <= e2 - tol;
+                            near = d2 <= e2 + tol;
+                            zero = d2 <= tol;
+                        } else {
+                            const float dist = 1.0f - v[j];
+                            pass = dist <= a.eps - kMargin;
+                            near = dist <= a.eps + kMargin;
+                            zero = dist <= kMargin;
+                        }
                         bits |= (uint32_t)pass << (c16 * 16 + j);
-                        uw |= (uint32_t)(!pass && dist <= hi) << (c16 * 16 + j);
-                        zw |= (uint32_t)(dist <= kMargin) << (c16 * 16 + j);
+                        uw |= (uint32_t)(!pass && near) << (c16 * 16 + j);
+                        zw |= (uint32_t)zero << (c16 * 16 + j);
                     }
                 }
                 // the accumulator is in registers: the MMAs may reuse it
@@ -406,30 +442,52 @@ __global__ void __launch_bounds__(NT, 1) k_dist_tc(const __grid_constant__ CUten
 
 // Cb: the BF16 rows of every list's candidates, list-major, nct * 64 rows per
 // list (row ct * 64 + j = candidate ct * 64 + j of the list, zero past m), the
-// B operand of k_dist_tc as plain tiles.
-__global__ void k_gather_cand(const DistArgs a, const __nv_bfloat16* __restrict__ Xb, int ldb,
+// B operand of k_dist_tc as plain tiles.  Cosine: rows of Xb (ldb wide); L2:
+// [hi | hi | lo] from the split rows [hi | lo] of Xb (3 ldb wide).
+__global__ void k_gather_cand(const DistArgs a, const __nv_bfloat16* __restrict__ Xb, int ldb, int segs,
                               __nv_bfloat16* __restrict__ Cb) {
-    const int rowsPerList = a.nct * TN, per = ldb / 8;
+    const int rowsPerList = a.nct * TN, ldc = segs * ldb, per = ldc / 8;
+    const int ldx = segs == 3 ? 2 * ldb : ldb;
     const size_t total = (size_t)2 * a.nproj * rowsPerList * per;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const size_t row = i / per;
         const int c8 = (int)(i % per) * 8;
+        const int seg = c8 / ldb, off = c8 % ldb;
+        const int srcCol = (segs == 3 && seg == 2 ? ldb : 0) + off;  // segments 0, 1: hi; 2: lo
         const int l = (int)(row / rowsPerList), j = (int)(row % rowsPerList);
         const int r = l % a.nproj, side = l / a.nproj;
         uint4 v = make_uint4(0, 0, 0, 0);
         if (j < a.m) {
             const int q = __ldg(a.topM + (size_t)r * 2 * a.m + side * a.m + j);
-            v = __ldg(reinterpret_cast<const uint4*>(Xb + (size_t)q * ldb + c8));
+            v = __ldg(reinterpret_cast<const uint4*>(Xb + (size_t)q * ldx + srcCol));
         }
-        *reinterpret_cast<uint4*>(Cb + row * ldb + c8) = v;
+        *reinterpret_cast<uint4*>(Cb + row * ldc + c8) = v;
+    }
+}
+
+// Squared norm of each row of Xt: a warp per row, 16-byte loads.
+__global__ void k_sq_norms(const float* __restrict__ Xt, int ld, int n, float* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < n; p += warps) {
+        const float4* x = reinterpret_cast<const float4*>(Xt + (size_t)p * ld);
+        float s = 0.0f;
+        for (int c = lane; c < ld / 4; c += 32) {
+            const float4 v = __ldg(x + c);
+            s = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, s))));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) out[p] = s;
     }
 }
 
 // Exact re-decision of the queued pairs: a warp takes 32 queue entries, one
 // per lane, and computes their distances with the plain path's sequential
-// FP32 dot (dtile::warp_staged_cosine), so the decision equals k_dist's.
+// FP32 arithmetic (dtile::warp_staged), so the decision equals k_dist's.
 constexpr int RC_WARPS = 4;
 
+template <int DIST>
 __global__ void __launch_bounds__(RC_WARPS * 32) k_recheck(DistArgs a, const uint64_t* __restrict__ queue,
                                                            const unsigned long long* __restrict__ qcount,
                                                            int64_t qcap) {
@@ -454,7 +512,7 @@ __global__ void __launch_bounds__(RC_WARPS * 32) k_recheck(DistArgs a, const uin
         rows[w][lane] = a.Xt + (size_t)p * a.ld;
         rows[w][32 + lane] = a.Xt + (size_t)q * a.ld;
         __syncwarp();
-        const float dist = dtile::warp_staged_cosine(rows[w], tile[w], a.ld);
+        const float dist = dtile::warp_staged<DIST>(rows[w], tile[w], a.ld);
         if (a.dists != nullptr) {  // eps sweep: store the exact distance; masks follow per eps
             if (valid) a.dists[((size_t)p * 2 * a.k + slot) * a.m + col] = dist;
             __syncwarp();
@@ -528,26 +586,49 @@ int launch_to_bf16(const float* Xt, int ld, int n, void* Xb, int ldb, cudaStream
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
+static int cand_segs(const DistArgs& a) { return a.dist == DIST_L2 ? 3 : 1; }
+
 size_t dist_tc_cand_bytes(const DistArgs& a, int ldb) {
-    return sizeof(uint16_t) * (size_t)2 * a.nproj * a.nct * TN * ldb;
+    return sizeof(uint16_t) * (size_t)2 * a.nproj * a.nct * TN * cand_segs(a) * ldb;
 }
 
 int launch_dist_tc(const DistArgs& a, const void* Xb, int ldb, void* Cb, uint64_t* queue, int64_t qcap,
                    unsigned long long* qcount, int32_t* err, cudaStream_t st) {
     if (ldb % TKB != 0 || (reinterpret_cast<uintptr_t>(Xb) & 15) || (reinterpret_cast<uintptr_t>(Cb) & 15)) return -1;
+    if (a.dist != DIST_COSINE && !(a.dist == DIST_L2 && a.dists == nullptr && a.sqNorm != nullptr)) return -1;
+    const int segs = cand_segs(a);
     const int rows = 2 * a.nproj * a.nct * TN;
-    k_gather_cand<<<sm_count() * 8, 256, 0, st>>>(a, static_cast<const __nv_bfloat16*>(Xb), ldb,
+    k_gather_cand<<<sm_count() * 8, 256, 0, st>>>(a, static_cast<const __nv_bfloat16*>(Xb), ldb, segs,
                                                   static_cast<__nv_bfloat16*>(Cb));
     if (cudaPeekAtLastError() != cudaSuccess) return -1;
     CUtensorMap tmC;
-    if (!tc::encode_bf16_2d(&tmC, Cb, rows, ldb, TKB, TN)) return -1;
+    if (!tc::encode_bf16_2d(&tmC, Cb, rows, segs * ldb, TKB, TN)) return -1;
     const size_t sm = (size_t)STAGES * STAGE_BYTES + 1024;
-    auto kern = a.dists != nullptr ? k_dist_tc<true> : k_dist_tc<false>;
+    auto kern = a.dist == DIST_L2 ? k_dist_tc<DIST_L2, false>
+                                  : (a.dists != nullptr ? k_dist_tc<DIST_COSINE, true> : k_dist_tc<DIST_COSINE, false>);
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return -1;
+    // L2 band (see the decision rule above): split error, tensor-core
+    // accumulation over K = 3 ldb, the FP32 norms over ld, the FP32 updates;
+    // then the reference's own sum of squares and its sqrt at eps
+    float tolRel = 0.0f, tolAbs = 0.0f;
+    if (a.dist == DIST_L2) {
+        const double u23 = std::ldexp(1.0, -23);
+        tolRel = (float)(3.1 * std::ldexp(1.0, -16) + (3.0 * ldb + a.ld) * u23 + 4.0 * u23);
+        tolAbs = (float)(((double)a.ld * u23 + 8.0 * u23) * (double)a.eps * a.eps * 1.01 + 1e-30);
+    }
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(a.nTiles, (int64_t)sm_count()));
-    kern<<<grid, NT, sm, st>>>(tmC, a, static_cast<const __nv_bfloat16*>(Xb), ldb, queue, qcap, qcount, err);
+    kern<<<grid, NT, sm, st>>>(tmC, a, static_cast<const __nv_bfloat16*>(Xb), ldb, queue, qcap, qcount, err, tolRel,
+                               tolAbs);
     return cudaPeekAtLastError() == cudaSuccess ? 2 : -1;
+}
+
+int launch_sq_norms(const float* Xt, int ld, int n, float* out, cudaStream_t st) {
+    if (n <= 0) return 0;
+    if ((ld & 3) || (reinterpret_cast<uintptr_t>(Xt) & 15)) return -1;
+    const int grid = (int)std::min<int64_t>(((int64_t)n + 7) / 8, (int64_t)sm_count() * 16);
+    k_sq_norms<<<grid, 256, 0, st>>>(Xt, ld, n, out);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
 int launch_screen_reset(const DistArgs& a, cudaStream_t st) {
@@ -557,7 +638,8 @@ int launch_screen_reset(const DistArgs& a, cudaStream_t st) {
 
 int launch_recheck(const DistArgs& a, const uint64_t* queue, const unsigned long long* qcount, int64_t qcap,
                    cudaStream_t st) {
-    k_recheck<<<sm_count() * 8, RC_WARPS * 32, 0, st>>>(a, queue, qcount, qcap);
+    if (a.dist == DIST_L2) k_recheck<DIST_L2><<<sm_count() * 8, RC_WARPS * 32, 0, st>>>(a, queue, qcount, qcap);
+    else k_recheck<DIST_COSINE><<<sm_count() * 8, RC_WARPS * 32, 0, st>>>(a, queue, qcount, qcap);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 

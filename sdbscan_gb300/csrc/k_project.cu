@@ -300,12 +300,14 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
         float v[NJ];
         if (EMB == 0) {
             // Cosine: the transformed row is the embedding; one division per element
+            __nv_bfloat16* xb = a.Xb ? reinterpret_cast<__nv_bfloat16*>(a.Xb) + (size_t)p * a.ldb : nullptr;
 #pragma unroll
             for (int j = 0; j < NJ; ++j) {
                 const int e = (int)l + 32 * j;
                 float t = 0.0f;
                 if (e < a.d) t = a.do_transform ? __fdiv_rn(x[e], sc) : x[e];
                 if (e < a.ld) a.Xt[(size_t)p * a.ld + e] = t;
+                if (xb && e < a.ldb) xb[e] = __float2bfloat16_rn(t);  // the tensor-core copy, zero padded
                 v[j] = t;
             }
             for (int e = (int)l + 32 * NJ; e < a.ld; e += 32) {
@@ -594,7 +596,7 @@ int launch_project_nje(const ProjectArgs& a, const float* scale, cudaStream_t st
     const int G = (a.chunkEnd > 0 ? a.chunkEnd : (a.n + a.chunk - 1) / a.chunk) - a.chunkBase;
     if (G <= 0) return 0;
     // one full wave of 4 blocks per SM; the blocks walk the launch's chunks grid-stride
-    const int grid = std::min(G, sm_count() * 4);
+    const int grid = std::min(G, project_wave_chunks());
     const int nsw = (3 * a.fhtDim + 31) / 32;
     const int rowLen = EMB == 2 ? ((a.d + 3) & ~3) + a.fhtDim : 0;
     const size_t xs = (size_t)((a.d + 3) & ~3);
@@ -621,6 +623,8 @@ int launch_project_nj(const ProjectArgs& a, const float* scale, cudaStream_t st)
 
 int launch_project(const ProjectArgs& a, cudaStream_t st) {
     float* scale = a.scale;
+    // the BF16 copy is written by the register kernels' Cosine path only
+    if (a.Xb && (a.dist != DIST_COSINE || a.fhtDim > 2048 || a.ldb > a.fhtDim)) return -1;
     const int G = (a.n + a.chunk - 1) / a.chunk;
     const int pb = a.chunkBase * a.chunk, pe = std::min(a.n, (a.chunkEnd > 0 ? a.chunkEnd : G) * a.chunk);
     if (pe > pb)

@@ -347,6 +347,34 @@ def test_bf16_screening_equals_plain(gen, n, d, k, m, eps, minPts):
     assert l16[1] == l32[1]
 
 
+@pytest.mark.parametrize("n,d,ker,sigma,eps", [(12000, 32, 256, 1.5, 0.55), (16000, 192, 512, 6.0, 1.72)])
+def test_bf16_l2_screening_is_exact_on_its_candidates(port, n, d, ker, sigma, eps):
+    """L2 in BF16 mode: the split-BF16 tensor-core screening with exact FP32
+    re-decision inside the per-pair band gives, on the fit's own candidate
+    sets (its top-k / top-m, which the BF16 embedding GEMM shapes), exactly
+    the oracle's neighbourhood sizes, core flags and labels."""
+    from sdbscan_gb300 import capi, datasets
+    X = datasets.cfg3_aniso_l2(n, d, n_comp=8, scale=0.1, seed=97)[0]
+    eng = capi.Engine(n, d)
+    eng.set_params(n_proj=512, topK=5, topM=40, distance="L2", ker_n_features=ker, ker_sigma=sigma, random_seed=4,
+                   precision=capi.PREC_BF16)
+    eng.fit_sdbscan(X, eps, 10)
+    c = eng.counters()
+    assert c["fallbacks"] == 0
+    assert c["rechecked"] > 0  # pairs fell inside the band and were re-decided
+    tK, tM = eng.topk(), eng.topm()
+    Xt, rc = port.transform(X, "L2")
+    assert rc == 0
+    ocore, odeg, olabels, oncl = port.core_cluster_lean(Xt, "L2", tK, tM, eps, 10)
+    core, deg = eng.core()
+    labels, ncl = eng.labels()
+    np.testing.assert_array_equal(deg, odeg)
+    np.testing.assert_array_equal(core, ocore)
+    np.testing.assert_array_equal(labels, olabels)
+    assert ncl == oncl
+    assert 0 < ocore.sum() < n
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_eps_sweep_equals_separate_fits(precision):
     """test_sDbscan's pattern (index and distances once, then per eps) gives
@@ -390,8 +418,8 @@ def test_batch_graph_equals_sweeps(precision):
             np.testing.assert_array_equal(lb, labels[j])
             assert nb == ncl[j]
     assert b.lanes() >= 1
-    # plain distances: the autotuner picked a tile shape per set; BF16 sets screen on the tensor cores
-    assert all(v in ((1, 2, 3) if precision == 0 else (0,)) for v in b.tile_variants())
+    # the autotuner picked a plain tile shape per set, or (BF16) the tensor-core screening (0)
+    assert all(v in ((1, 2, 3) if precision == 0 else (0, 1, 2, 3)) for v in b.tile_variants())
     b.close()
     torch.cuda.synchronize()
 
