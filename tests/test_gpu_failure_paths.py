@@ -75,9 +75,10 @@ def test_bf16_queue_overflow_falls_back_to_fp32():
 
 
 def test_bf16_embedding_stall_falls_back_to_fp32():
-    """L2, BF16 mode: the tensor-core random-Fourier embedding stalls, the
-    FP32 embedding replaces it, and the fit equals a plain FP32 fit bit for
-    bit (both use the FP32 embedding then)."""
+    """L2, BF16 mode: the tensor-core random-Fourier embedding and the
+    tensor-core distance screening both stall, the FP32 embedding and the
+    plain distance kernel replace them, and the fit equals a plain FP32 fit bit
+    for bit (both use the FP32 embedding then)."""
     from sdbscan_gb300 import capi, datasets
     X = datasets.cfg3_aniso_l2(8000, 32, n_comp=8, scale=0.1, seed=93)[0]
     out = {}
@@ -88,7 +89,7 @@ def test_bf16_embedding_stall_falls_back_to_fp32():
         eng.set_debug_limits(stall_spins=lim)
         eng.fit_sdbscan(X, 0.9, 10)
         out[prec] = (eng.labels(), eng.projections(), eng.counters()["fallbacks"])
-    assert out[1][2] == 1
+    assert out[1][2] == 2  # the embedding and the screening
     np.testing.assert_array_equal(out[1][1], out[0][1])
     np.testing.assert_array_equal(out[1][0][0], out[0][0][0])
 
