@@ -658,10 +658,13 @@ def run_ours(args, cfg):
     barrier()
     t0 = time.perf_counter()
     e2e_stages = {}
+    e2e_upload_stage = []  # per step: the projection stage, which the upload feeds
     for _ in range(args.steps):
         fit_host(Xh, cfg["eps"], cfg["minPts"])
         res_e2e = result()
-        for k_, v_ in eng.stage_ms().items():
+        st_ = eng.stage_ms()
+        e2e_upload_stage.append(round(st_["project"], 2))
+        for k_, v_ in st_.items():
             e2e_stages[k_] = e2e_stages.get(k_, 0.0) + v_ / args.steps
     barrier()
     e2e_s = _max_over_ranks(time.perf_counter() - t0, ws, f"cuda:{local}")
@@ -723,7 +726,7 @@ def run_ours(args, cfg):
         "clocks": clk.summary(),
         "e2e": {"value": e2e_value, "unit": "points/s", "h2d_bytes_per_step": n * d * 4,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / args.steps,
-                "stage_ms": e2e_stages,
+                "stage_ms": e2e_stages, "project_stage_ms_per_step": e2e_upload_stage,
                 "h2d_link": {"copy_ms": h2d_ms, "gbs": n * d * 4 / (h2d_ms / 1e3) / 1e9,
                              "note": "one plain pinned-host -> device copy of the step's input on this box "
                                      "(the upload floor of the step)"}},
