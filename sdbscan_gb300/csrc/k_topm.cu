@@ -18,6 +18,8 @@
 // counts such boundary ties.
 #include "common.cuh"
 
+#include <algorithm>
+
 namespace sdb {
 namespace {
 
@@ -95,31 +97,49 @@ __global__ void k_thresholds(TopMArgs a) {
     if (threadIdx.x == 0) (side == 0 ? a.thrMax : a.thrMin)[r] = __uint_as_float(selPrefix);  // raw key bits
 }
 
-// One thread per 4 consecutive projections of a point.
-__global__ void k_collect(TopMArgs a) {
-    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;  // float4 index
-    const size_t per_row = (size_t)a.nproj / 4;
-    const size_t total = (size_t)a.n * per_row;
-    if (q >= total) return;
-    const int p = (int)(q / per_row);
-    const int r0 = (int)(q % per_row) * 4;
-    const float4 v4 = __ldcs(reinterpret_cast<const float4*>(a.P + (size_t)p * a.nproj) + (r0 / 4));
-    const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+// A block takes kCollectRows consecutive points; a thread takes 4
+// consecutive vectors of them (16-byte loads, all rows' loads issued before
+// any compare, the vectors' thresholds loaded once).
+constexpr int kCollectRows = 8;
+__global__ void __launch_bounds__(256) k_collect(TopMArgs a) {
+    const int per_row = a.nproj / 4;
+    const int p0 = blockIdx.x * kCollectRows;
+    for (int c4 = threadIdx.x; c4 < per_row; c4 += blockDim.x) {
+        const int r0 = c4 * 4;
+        float4 v4[kCollectRows];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        const int r = r0 + t;
-        const uint32_t kc = key_of(vv[t]);
-        const uint32_t kf = key_of(-vv[t]);
-        const uint32_t tc = __float_as_uint(__ldg(a.thrMax + r));
-        const uint32_t tf = __float_as_uint(__ldg(a.thrMin + r));
-        if (kc >= tc) {
-            const int slot = atomicAdd(a.candCount + r, 1);
-            if (slot < a.cap) a.cand[(size_t)r * a.cap + slot] = ((uint64_t)kc << 32) | (uint32_t)(0xffffffffu - (uint32_t)p);
-        }
-        if (kf >= tf) {
-            const int list = a.nproj + r;
-            const int slot = atomicAdd(a.candCount + list, 1);
-            if (slot < a.cap) a.cand[(size_t)list * a.cap + slot] = ((uint64_t)kf << 32) | (uint32_t)(0xffffffffu - (uint32_t)p);
+        for (int i = 0; i < kCollectRows; ++i)
+            v4[i] = p0 + i < a.n ? __ldcs(reinterpret_cast<const float4*>(a.P + (size_t)(p0 + i) * a.nproj) + c4)
+                                 : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const float4 tcv = __ldg(reinterpret_cast<const float4*>(a.thrMax) + c4);
+        const float4 tfv = __ldg(reinterpret_cast<const float4*>(a.thrMin) + c4);
+        const uint32_t tc[4] = {__float_as_uint(tcv.x), __float_as_uint(tcv.y), __float_as_uint(tcv.z),
+                                __float_as_uint(tcv.w)};
+        const uint32_t tf[4] = {__float_as_uint(tfv.x), __float_as_uint(tfv.y), __float_as_uint(tfv.z),
+                                __float_as_uint(tfv.w)};
+#pragma unroll
+        for (int i = 0; i < kCollectRows; ++i) {
+            const int p = p0 + i;
+            if (p >= a.n) break;
+            const float vv[4] = {v4[i].x, v4[i].y, v4[i].z, v4[i].w};
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int r = r0 + t;
+                const uint32_t kc = key_of(vv[t]);
+                const uint32_t kf = key_of(-vv[t]);
+                if (kc >= tc[t]) {
+                    const int slot = atomicAdd(a.candCount + r, 1);
+                    if (slot < a.cap)
+                        a.cand[(size_t)r * a.cap + slot] = ((uint64_t)kc << 32) | (uint32_t)(0xffffffffu - (uint32_t)p);
+                }
+                if (kf >= tf[t]) {
+                    const int list = a.nproj + r;
+                    const int slot = atomicAdd(a.candCount + list, 1);
+                    if (slot < a.cap)
+                        a.cand[(size_t)list * a.cap + slot] =
+                            ((uint64_t)kf << 32) | (uint32_t)(0xffffffffu - (uint32_t)p);
+                }
+            }
         }
     }
 }
@@ -267,9 +287,10 @@ int launch_topm_thresholds(const TopMArgs& a, cudaStream_t st) {
 }
 
 int launch_topm_collect(const TopMArgs& a, cudaStream_t st) {
-    if (a.nproj % 4 == 0) {
-        const size_t total = (size_t)a.n * (a.nproj / 4);
-        k_collect<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(a);
+    if (a.nproj % 4 == 0 && (reinterpret_cast<uintptr_t>(a.P) & 15) == 0 &&
+        (reinterpret_cast<uintptr_t>(a.thrMax) & 15) == 0 && (reinterpret_cast<uintptr_t>(a.thrMin) & 15) == 0) {
+        const int threads = std::min(256, (a.nproj / 4 + 31) / 32 * 32);
+        k_collect<<<(unsigned)((a.n + kCollectRows - 1) / kCollectRows), threads, 0, st>>>(a);
     } else {
         const size_t total = (size_t)a.n * a.nproj;
         k_collect1<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(a);
