@@ -314,9 +314,11 @@ struct CoreArgs {
     int accumulate, round;
     uint64_t* newMasks;      // n x 2k x W (accumulate only)
     int32_t* coreEps;        // n: round at which the point became core, -1 before (accumulate only)
+    const uint64_t* multi;   // 2D x W: slots whose point another list holds too (launch_slot_sigs)
 };
+// Per-slot signatures (sig, 2D x m int4) and the multi-list slot bits (multi, 2D x W).
 int launch_slot_sigs(const int32_t* topM, int D, int m, const int64_t* hubOff, const int32_t* hubLists, void* sig,
-                     cudaStream_t st);
+                     uint64_t* multi, int W, cudaStream_t st);
 int launch_core_dedupe(const CoreArgs& a, const void* sig, cudaStream_t st);
 // hubIdx from hubOff (a scan of hub flags into idxTmp) and the hubs' list masks.
 int launch_hub_masks(const CoreArgs& a, int32_t* hubIdx, int64_t* idxTmp, uint32_t* kMask, int64_t* scanTmp,

@@ -115,7 +115,7 @@ std::vector<DevBuf*> sdb_engine::all_bufs() {
             &kMask, &firstMasks, &Xb, &queue, &sweepLabels, &sweepNcl, &sig, &Rb, &newMasks, &coreEps, &sampleFlag,
             &noiseFlag, &noiseCores, &noisePts, &PcT, &numCore, &pairRound, &sngCols, &sngMult, &sngColOf, &sngExtras,
             &sngExtraPass, &sngMask, &rowDeg, &colCnt, &sngUb, &sngHeavy, &chunkOff, &tileKey, &keyOff, &tilePerm,
-            &Cb, &tileKeyTc, &keyOffTc, &tilePermTc, &sngWords, &hashOffB, &hashIdB, &hashDistB, &sqNorm};
+            &Cb, &tileKeyTc, &keyOffTc, &tilePermTc, &sngWords, &hashOffB, &hashIdB, &hashDistB, &sqNorm, &multiMask};
 }
 
 // ---------------------------------------------------------------------------
@@ -263,7 +263,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     const int maskWords = (L + 31) / 32;
     const size_t maxHubs = std::min<size_t>((size_t)n, (size_t)L * m);
     ok &= ensure(hubIdx, sizeof(int32_t) * n) && ensure(kMask, sizeof(uint32_t) * maxHubs * maskWords) &&
-          ensure(sig, 16 * (size_t)L * m);
+          ensure(sig, 16 * (size_t)L * m) && ensure(multiMask, sizeof(uint64_t) * (size_t)L * W);
     if (rff) ok &= ensure(E, sizeof(float) * (size_t)n * ker) && ensure(Rt, sizeof(float) * hostRt.size());
     if (optics || sweep) ok &= ensure(dists, sizeof(float) * (size_t)n * 2 * k * m);
     if (optics) ok &= ensure(coreDist, sizeof(float) * n);
@@ -445,7 +445,8 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     L_(launch_scan_i64(i64(hubOff), i64(hubOff), (size_t)n + 1, i64(scanTmp), st));
     SDB_CK(cudaMemsetAsync(hubCount.ptr, 0, sizeof(int32_t) * n, st));
     L_(launch_hubs_scatter(ia, st));
-    L_(launch_slot_sigs(i32(topM), D, m, i64(hubOff), i32(hubLists), sig.ptr, st));
+    L_(launch_slot_sigs(i32(topM), D, m, i64(hubOff), i32(hubLists), sig.ptr, static_cast<uint64_t*>(multiMask.ptr), W,
+                        st));
     if (!ok) return fail(SDB_ERR_CUDA, std::string("index launch failed: ") + cudaGetErrorString(cudaGetLastError()));
     if (!capture) SDB_CK(cudaEventRecord(ev[4], st));
 
@@ -537,6 +538,7 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     ca.hubCount = i32(hubCount);
     ca.hubOff = i64(hubOff);
     ca.hubLists = i32(hubLists);
+    ca.multi = static_cast<const uint64_t*>(multiMask.ptr);
     ca.inRaw = i32(inRaw);
     ca.aCount = i32(aCount);
     ca.degree = i32(degree);

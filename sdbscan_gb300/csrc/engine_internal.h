@@ -83,7 +83,7 @@ struct sdb_engine {
         nbIdx, nbDist, nbFill, hubIdx, kMask, firstMasks, Xb, queue, sweepLabels, sweepNcl, sig, Rb, newMasks,
         coreEps, sampleFlag, noiseFlag, noiseCores, noisePts, PcT, numCore, pairRound, sngCols, sngMult, sngColOf,
         sngExtras, sngExtraPass, sngMask, rowDeg, colCnt, sngUb, sngHeavy, chunkOff, tileKey, keyOff, tilePerm, Cb,
-        tileKeyTc, keyOffTc, tilePermTc, sngWords, hashOffB, hashIdB, hashDistB, sqNorm;
+        tileKeyTc, keyOffTc, tilePermTc, sngWords, hashOffB, hashIdB, hashDistB, sqNorm, multiMask;
 
     // results
     bool haveLabels = false, haveOptics = false, haveFit = false, lastOptics = false;

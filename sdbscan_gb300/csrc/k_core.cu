@@ -93,6 +93,19 @@ __global__ void k_slot_sigs(const int32_t* __restrict__ topM, int D, int m, cons
     sig[q] = make_int4(o[0], o[1], o[2], c);
 }
 
+// multi[l][w] bit j: the point in slot 64 w + j of list l is held by another
+// list too.  Most slots hold a point of one list only (about 84 % of the
+// passing pairs at 1M x 784); such an occurrence is the first and only one.
+__global__ void k_multi_bits(const int4* __restrict__ sig, int D, int m, int W, uint64_t* __restrict__ multi) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= 2 * D * W) return;
+    const int l = q / W, wd = q % W;
+    uint64_t bits = 0;
+    for (int j = 0; j < 64 && wd * 64 + j < m; ++j)
+        bits |= (uint64_t)(sig[(size_t)l * m + wd * 64 + j].w > 0) << j;
+    multi[q] = bits;
+}
+
 __device__ __forceinline__ bool has_list(const uint32_t* km, int lst) { return (km[lst >> 5] >> (lst & 31)) & 1u; }
 
 // Multiplicity and first-occurrence test of candidate i, met through list l.
@@ -207,41 +220,128 @@ __device__ __forceinline__ void mark_lists(const CoreArgs& a, uint32_t* listMask
     __syncwarp();
 }
 
+// Per-warp shared memory of k_core_dedupe (after the two list masks).
+constexpr int kDdWords = 32;   // mask words per round, one per lane
+constexpr int kDdSlots = 62;   // 2k for k <= 31
+struct DedupeWarp {
+    uint32_t fresh[2 * kDdWords];       // first-occurrence bits found by the per-pair test (32-bit halves)
+    int32_t list[kDdSlots];             // per slot: its list
+    int32_t rowOff[kDdSlots];           // per slot: its list's row in topM
+    uint16_t item[kDdWords * 64];       // the round's pairs that need the per-pair test: (word, bit)
+};
+__host__ __device__ constexpr size_t dedupe_warp_bytes(int maskWords) {
+    return sizeof(uint32_t) * 2 * (size_t)maskWords + sizeof(DedupeWarp);
+}
+
 // Persistent warps, each over points p = warp, warp + total, ...
-__global__ void k_core_dedupe(CoreArgs a, const int4* __restrict__ sig) {
-    extern __shared__ uint32_t shm[];
+// A hub point (one a top-m list holds) visits its slots one by one, since each
+// of its first occurrences needs the in-candidates test.  Any other point takes
+// the pairs whose candidate no other list holds straight from the mask words
+// (first occurrence, multiplicity 1, nothing to correct) and runs the per-pair
+// test only on the others, gathered into a dense list first, so the warp's
+// instructions follow the ~16 % of pairs that need them rather than every slot.
+__global__ void __launch_bounds__(256, 4) k_core_dedupe(CoreArgs a, const int4* __restrict__ sig) {
+    extern __shared__ __align__(16) uint32_t shm[];
     const int w = threadIdx.x >> 5;
     const unsigned lane = lane_id();
     const int maskWords = (2 * a.nproj + 31) / 32;
-    uint32_t* km = shm + (size_t)w * 2 * maskWords;
+    uint32_t* km = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(shm) + (size_t)w * dedupe_warp_bytes(maskWords));
     uint32_t* listMask = km + maskWords;
+    DedupeWarp& sw = *reinterpret_cast<DedupeWarp*>(listMask + maskWords);
     for (int t = (int)lane; t < maskWords; t += 32) km[t] = 0u;
     __syncwarp();
     const int gw = blockIdx.x * (blockDim.x >> 5) + w;
     const int nw = gridDim.x * (blockDim.x >> 5);
     const int slots = 2 * a.k;
+    const int nWords = slots * a.W;
     const unsigned long long* mk64 = reinterpret_cast<const unsigned long long*>(a.masks);
     for (int p = gw; p < a.n; p += nw) {
+        const unsigned long long* pm = mk64 + (size_t)p * nWords;
         // a point without a passing pair (common in a sweep round) only clears
         // its first-occurrence words (this round's words when accumulating)
         bool any = false;
-        for (int t = (int)lane; t < slots * a.W; t += 32) any |= __ldg(mk64 + (size_t)p * slots * a.W + t) != 0ull;
+        for (int t = (int)lane; t < nWords; t += 32) any |= __ldg(pm + t) != 0ull;
         if (!__any_sync(0xffffffffu, any)) {
             uint64_t* out = a.accumulate ? a.newMasks : a.firstMasks;
-            for (int t = (int)lane; t < slots * a.W; t += 32) out[(size_t)p * slots * a.W + t] = 0ull;
+            for (int t = (int)lane; t < nWords; t += 32) out[(size_t)p * nWords + t] = 0ull;
             if (lane == 0) a.aCount[p] = 0;
             continue;
         }
         const int64_t h0 = a.hubOff[p], h1 = a.hubOff[p + 1];
-        const bool hub = h1 > h0;
-        if (hub) mark_lists(a, listMask, h0, h1, maskWords);
-        const int nd = visit_point(a, km, sig, p, a.firstMasks, [&](int, int, int, int i, bool first, int mult) {
-            if (!first) return;
-            int corr = mult - 1;
-            if (hub && in_candidates_of(a, listMask, a.hubLists + h0, (int)(h1 - h0), i)) corr += 1;
-            if (corr) atomicSub(a.inRaw + i, corr);
-        });
-        if (lane == 0) a.aCount[p] = nd;
+        if (h1 > h0) {
+            mark_lists(a, listMask, h0, h1, maskWords);
+            const int nd = visit_point(a, km, sig, p, a.firstMasks, [&](int, int, int, int i, bool first, int mult) {
+                if (!first) return;
+                int corr = mult - 1;
+                if (in_candidates_of(a, listMask, a.hubLists + h0, (int)(h1 - h0), i)) corr += 1;
+                if (corr) atomicSub(a.inRaw + i, corr);
+            });
+            if (lane == 0) a.aCount[p] = nd;
+            continue;
+        }
+        for (int j = (int)lane; j < slots; j += 32) {
+            const int l = __ldg(a.topK + (size_t)p * slots + j) + (j >= a.k ? a.nproj : 0);
+            sw.list[j] = l;
+            sw.rowOff[j] = (l % a.nproj) * 2 * a.m + (l / a.nproj) * a.m;
+            atomicOr(km + (l >> 5), 1u << (l & 31));
+        }
+        __syncwarp();
+        int distinct = 0;
+        for (int wb = 0; wb < nWords; wb += kDdWords) {
+            const int g = wb + (int)lane;  // this lane's mask word: slot g / W, word g % W
+            uint64_t mk = 0, mu = 0;
+            if (g < nWords) {
+                mk = __ldg(pm + g);
+                mu = __ldg(a.multi + (size_t)sw.list[g / a.W] * a.W + g % a.W);
+            }
+            const uint64_t sole = mk & ~mu, todo = mk & mu;
+            distinct += __popcll(sole);
+            sw.fresh[2 * lane] = 0u;
+            sw.fresh[2 * lane + 1] = 0u;
+            // gather the pairs that need the test: lane-serial over its word's bits
+            const int cnt = __popcll(todo);
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((int)lane >= o) incl += v;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            int at = incl - cnt;
+            for (uint64_t t = todo; t; t &= t - 1) sw.item[at++] = (uint16_t)((lane << 6) | (__ffsll((long long)t) - 1));
+            __syncwarp();
+            for (int t = (int)lane; t < total; t += 32) {
+                const int it = sw.item[t];
+                const int wl = it >> 6, bit = it & 63;
+                const int gg = wb + wl;
+                const int jj = gg / a.W, s = (gg % a.W) * 64 + bit;
+                const int l = sw.list[jj];
+                const int i = __ldg(a.topM + sw.rowOff[jj] + s);
+                int mult;
+                bool first;
+                occurrence(a, km, sig, l, s, i, mult, first);
+                if (!first) continue;
+                ++distinct;
+                atomicOr(&sw.fresh[2 * wl + (bit >> 5)], 1u << (bit & 31));
+                if (mult > 1) atomicSub(a.inRaw + i, mult - 1);
+            }
+            __syncwarp();
+            if (g < nWords) {
+                const size_t o = (size_t)p * nWords + g;
+                const uint64_t f64 = sole | ((uint64_t)sw.fresh[2 * lane + 1] << 32) | sw.fresh[2 * lane];
+                if (a.accumulate) {
+                    a.firstMasks[o] |= f64;
+                    a.newMasks[o] = f64;
+                } else {
+                    a.firstMasks[o] = f64;
+                }
+            }
+            __syncwarp();
+        }
+        for (int j = (int)lane; j < slots; j += 32) km[sw.list[j] >> 5] = 0u;
+        __syncwarp();
+        distinct = warp_sum(distinct);
+        if (lane == 0) a.aCount[p] = distinct;
     }
 }
 
@@ -355,15 +455,21 @@ static int core_grid(int n, int warps) {
 }
 
 int launch_slot_sigs(const int32_t* topM, int D, int m, const int64_t* hubOff, const int32_t* hubLists, void* sig,
-                     cudaStream_t st) {
+                     uint64_t* multi, int W, cudaStream_t st) {
     const int total = 2 * D * m;
     k_slot_sigs<<<(total + 255) / 256, 256, 0, st>>>(topM, D, m, hubOff, hubLists, static_cast<int4*>(sig));
-    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+    if (cudaPeekAtLastError() != cudaSuccess) return -1;
+    k_multi_bits<<<(2 * D * W + 255) / 256, 256, 0, st>>>(static_cast<const int4*>(sig), D, m, W, multi);
+    return cudaPeekAtLastError() == cudaSuccess ? 2 : -1;
 }
 
 int launch_core_dedupe(const CoreArgs& a, const void* sig, cudaStream_t st) {
     const int warps = 8;
-    const size_t sm = sizeof(uint32_t) * 2 * ((2 * a.nproj + 31) / 32) * warps;
+    if (2 * a.k > kDdSlots || a.multi == nullptr) return -1;
+    const size_t sm = dedupe_warp_bytes((2 * a.nproj + 31) / 32) * warps;
+    if (sm > 48 * 1024 &&
+        cudaFuncSetAttribute(k_core_dedupe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+        return -1;
     k_core_dedupe<<<core_grid(a.n, warps), warps * 32, sm, st>>>(a, static_cast<const int4*>(sig));
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
