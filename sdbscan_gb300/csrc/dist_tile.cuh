@@ -111,8 +111,26 @@ __device__ __forceinline__ float warp_staged_cosine(const float* const* rows, fl
     return warp_staged<DIST_COSINE>(rows, tile, ld);
 }
 
+// The thread's row group ty (0..15) and column group tx (0..TX-1).  A
+// quarter-warp's eight 16-byte fragment loads are conflict-free when its
+// column rows tx + TX j fall in eight different bank groups (row r's chunk
+// sits in group (5 r + c) mod 8 for the row stride of 20 floats).  For TX = 10
+// the plain tid % TX puts tx = 8, 9 next to 0, 1 in one quarter-warp (the same
+// groups); instead, of every five quarter-warps four take tx = 0..7 of one row
+// group each and the fifth takes tx = 8, 9 of all four.
+template <int TX> __device__ __forceinline__ void tile_coords(int tid, int& ty, int& tx) {
+    if constexpr (TX == 10) {
+        const int qw = tid >> 3, l8 = tid & 7, g = qw / 5, qi = qw % 5;
+        ty = 4 * g + (qi < 4 ? qi : (l8 >> 1));
+        tx = qi < 4 ? l8 : 8 + (l8 & 1);
+    } else {
+        ty = tid / TX;
+        tx = tid % TX;
+    }
+}
+
 // acc[i][j] = accumulated distance terms of (row ty + 16 i, column tx + TX j)
-// with ty = tid / TX, tx = tid % TX.  KT dimensions per stage, NST stages:
+// with (ty, tx) = tile_coords<TX>(tid).  KT dimensions per stage, NST stages:
 // As / Bs are NST x TM x (KT + 4) and NST x (TX * CN) x (KT + 4) floats of
 // shared memory (the +4 keeps the float4 fragment reads of consecutive rows
 // in different bank groups).  Ends with every copy landed; the caller
@@ -152,7 +170,8 @@ __device__ __forceinline__ void accumulate(const float* __restrict__ Xt, int ld,
 #pragma unroll
         for (int j = 0; j < CN; ++j) acc[i][j] = 0.0f;
 
-    const int ty = tid / TX, tx = tid % TX;
+    int ty, tx;
+    tile_coords<TX>(tid, ty, tx);
 #pragma unroll
     for (int s = 0; s < NST - 1; ++s) {
         if (s < nk) load_stage(s, s);

@@ -87,7 +87,8 @@ __global__ void __launch_bounds__(16 * TX, (dist_min_blocks<TX, CN, KT, NST>()))
 
     float acc[8][CN];
     accumulate<DIST, TX, CN, KT, NST>(a.Xt, a.ld, a.d, rowPoint, colPoint, As, Bs, acc);
-    const int ty = tid / TX, tx = tid % TX;
+    int ty, tx;
+    tile_coords<TX>(tid, ty, tx);
 
     // epilogue
     int myPass = 0;

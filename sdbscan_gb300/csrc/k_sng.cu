@@ -78,7 +78,8 @@ __global__ void __launch_bounds__(kNT, 2) k_sng_block(SngArgs a) {
 
     float acc[8][kCN];
     accumulate<DIST, kTX, kCN>(a.Xt, a.ld, a.d, rowPoint, colPoint, As, Bs, acc);
-    const int ty = tid / kTX, tx = tid % kTX;
+    int ty, tx;
+    tile_coords<kTX>(tid, ty, tx);
 
     int myPass = 0;
     int colPass[kCN];

@@ -106,7 +106,8 @@ __global__ void __launch_bounds__(BNT, 4) k_sngb_tile(SngBlockArgs a) {
 
     float acc[8][BCN];
     accumulate<DIST, BTX, BCN>(a.Xt, a.ld, a.d, rowPoint, colPoint, As, Bs, acc);
-    const int ty = tid / BTX, tx = tid % BTX;
+    int ty, tx;
+    tile_coords<BTX>(tid, ty, tx);
     int colPass[BCN] = {0, 0, 0, 0};
     int myPass = 0;
 #pragma unroll
