@@ -155,8 +155,8 @@ struct ProjectArgs {
     int ldb;                 // its row stride, <= fhtDim
 };
 int launch_project(const ProjectArgs& a, cudaStream_t st);
-// Chunks in one full wave of k_project (a block per chunk, four blocks per SM).
-inline int project_wave_chunks() { return sm_count() * 4; }
+// Chunks in one full wave of k_project (a block per chunk, five blocks per SM).
+inline int project_wave_chunks() { return sm_count() * 5; }
 // transformData alone into Xt (uses X, ldx, Xt, ld, n, d, dist, scale, err).
 int launch_transform(const ProjectArgs& a, cudaStream_t st);
 

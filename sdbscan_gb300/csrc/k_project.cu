@@ -230,7 +230,7 @@ __device__ bool warp_topk(const uint32_t (&key)[NJ], int nproj, int k, int32_t* 
 }
 
 template <int NJ, int EMB>
-__global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs a, const float* __restrict__ scale) {
+__global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 5)) k_project(ProjectArgs a, const float* __restrict__ scale) {
     extern __shared__ float smem[];
     const int warps = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
@@ -299,22 +299,28 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 3)) k_project(ProjectArgs
         // transformed row -> Xt (zero padded to ld)
         float v[NJ];
         if (EMB == 0) {
-            // Cosine: the transformed row is the embedding; one division per element
+            // Cosine: the transformed row is the embedding; one division per
+            // element, done in place on the warp's staged row by a rolled loop
+            // (32 unrolled divisions made the body too large for the
+            // instruction cache: 9.3 -> 8.2 ms at 1M x 784)
             __nv_bfloat16* xb = a.Xb ? reinterpret_cast<__nv_bfloat16*>(a.Xb) + (size_t)p * a.ldb : nullptr;
+            if (a.do_transform) {
+                float* xw = xbuf + buf * xs;
+#pragma unroll 1
+                for (int e = (int)l; e < a.d; e += 32) xw[e] = __fdiv_rn(xw[e], sc);
+                __syncwarp();
+            }
 #pragma unroll
             for (int j = 0; j < NJ; ++j) {
                 const int e = (int)l + 32 * j;
                 float t = 0.0f;
-                if (e < a.d) t = a.do_transform ? __fdiv_rn(x[e], sc) : x[e];
+                if (e < a.d) t = x[e];
                 if (e < a.ld) a.Xt[(size_t)p * a.ld + e] = t;
                 if (xb && e < a.ldb) xb[e] = __float2bfloat16_rn(t);  // the tensor-core copy, zero padded
                 v[j] = t;
             }
-            for (int e = (int)l + 32 * NJ; e < a.ld; e += 32) {
-                float t = 0.0f;
-                if (e < a.d) t = a.do_transform ? __fdiv_rn(x[e], sc) : x[e];
-                a.Xt[(size_t)p * a.ld + e] = t;
-            }
+            for (int e = (int)l + 32 * NJ; e < a.ld; e += 32)  // (the row is already divided)
+                a.Xt[(size_t)p * a.ld + e] = e < a.d ? x[e] : 0.0f;
         }
         for (int i = (int)l; EMB != 0 && i < a.ld; i += 32) {
             float t = 0.0f;
@@ -595,7 +601,7 @@ int launch_project_nje(const ProjectArgs& a, const float* scale, cudaStream_t st
     const int warps = 4;
     const int G = (a.chunkEnd > 0 ? a.chunkEnd : (a.n + a.chunk - 1) / a.chunk) - a.chunkBase;
     if (G <= 0) return 0;
-    // one full wave of 4 blocks per SM; the blocks walk the launch's chunks grid-stride
+    // one full wave of 5 blocks per SM; the blocks walk the launch's chunks grid-stride
     const int grid = std::min(G, project_wave_chunks());
     const int nsw = (3 * a.fhtDim + 31) / 32;
     const int rowLen = EMB == 2 ? ((a.d + 3) & ~3) + a.fhtDim : 0;
