@@ -362,6 +362,9 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
         const int segs = std::min(kUploadSegs, G);
         SDB_CK(cudaEventRecord(segEv[kUploadSegs], st));  // Xin is free once the stream got here
         for (int c = 0; c < kCopyStreams; ++c) SDB_CK(cudaStreamWaitEvent(copyStream[c], segEv[kUploadSegs], 0));
+        // every copy is queued before the first projection launch, so a delay
+        // of the host thread while it queues the launches cannot starve the
+        // copy engine
         for (int sgi = 0; sgi < segs; ++sgi) {
             const int cb = (int)((int64_t)G * sgi / segs), ce = (int)((int64_t)G * (sgi + 1) / segs);
             const size_t pb = (size_t)cb * chunk, pe = std::min<size_t>((size_t)n, (size_t)ce * chunk);
@@ -369,9 +372,11 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
             SDB_CK(cudaMemcpyAsync(static_cast<float*>(Xin.ptr) + pb * d, X + pb * d, sizeof(float) * (pe - pb) * d,
                                    cudaMemcpyHostToDevice, cs));
             SDB_CK(cudaEventRecord(segEv[sgi], cs));
+        }
+        for (int sgi = 0; sgi < segs; ++sgi) {
             SDB_CK(cudaStreamWaitEvent(st, segEv[sgi], 0));
-            pa.chunkBase = cb;
-            pa.chunkEnd = ce;
+            pa.chunkBase = (int)((int64_t)G * sgi / segs);
+            pa.chunkEnd = (int)((int64_t)G * (sgi + 1) / segs);
             L_(launch_project(pa, st));
         }
         pa.chunkBase = pa.chunkEnd = 0;
