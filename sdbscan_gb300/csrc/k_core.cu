@@ -234,12 +234,13 @@ __host__ __device__ constexpr size_t dedupe_warp_bytes(int maskWords) {
 }
 
 // Persistent warps, each over points p = warp, warp + total, ...
-// A hub point (one a top-m list holds) visits its slots one by one, since each
-// of its first occurrences needs the in-candidates test.  Any other point takes
-// the pairs whose candidate no other list holds straight from the mask words
-// (first occurrence, multiplicity 1, nothing to correct) and runs the per-pair
-// test only on the others, gathered into a dense list first, so the warp's
-// instructions follow the ~16 % of pairs that need them rather than every slot.
+// A point that is no hub (no top-m list holds it) takes the pairs whose
+// candidate no other list holds straight from the mask words (first
+// occurrence, multiplicity 1, nothing to correct) and runs the per-pair test
+// only on the others; a hub runs it on all its pairs, since each of its first
+// occurrences needs the in-candidates test too.  The pairs to test are first
+// gathered into a dense per-warp list, so the warp's instructions follow those
+// pairs rather than every slot and lane.
 __global__ void __launch_bounds__(256, 4) k_core_dedupe(CoreArgs a, const int4* __restrict__ sig) {
     extern __shared__ __align__(16) uint32_t shm[];
     const int w = threadIdx.x >> 5;
@@ -268,17 +269,8 @@ __global__ void __launch_bounds__(256, 4) k_core_dedupe(CoreArgs a, const int4* 
             continue;
         }
         const int64_t h0 = a.hubOff[p], h1 = a.hubOff[p + 1];
-        if (h1 > h0) {
-            mark_lists(a, listMask, h0, h1, maskWords);
-            const int nd = visit_point(a, km, sig, p, a.firstMasks, [&](int, int, int, int i, bool first, int mult) {
-                if (!first) return;
-                int corr = mult - 1;
-                if (in_candidates_of(a, listMask, a.hubLists + h0, (int)(h1 - h0), i)) corr += 1;
-                if (corr) atomicSub(a.inRaw + i, corr);
-            });
-            if (lane == 0) a.aCount[p] = nd;
-            continue;
-        }
+        const bool hub = h1 > h0;
+        if (hub) mark_lists(a, listMask, h0, h1, maskWords);
         for (int j = (int)lane; j < slots; j += 32) {
             const int l = __ldg(a.topK + (size_t)p * slots + j) + (j >= a.k ? a.nproj : 0);
             sw.list[j] = l;
@@ -292,7 +284,8 @@ __global__ void __launch_bounds__(256, 4) k_core_dedupe(CoreArgs a, const int4* 
             uint64_t mk = 0, mu = 0;
             if (g < nWords) {
                 mk = __ldg(pm + g);
-                mu = __ldg(a.multi + (size_t)sw.list[g / a.W] * a.W + g % a.W);
+                // a hub's every first occurrence needs the in-candidates test
+                mu = hub ? ~0ull : __ldg(a.multi + (size_t)sw.list[g / a.W] * a.W + g % a.W);
             }
             const uint64_t sole = mk & ~mu, todo = mk & mu;
             distinct += __popcll(sole);
@@ -323,7 +316,9 @@ __global__ void __launch_bounds__(256, 4) k_core_dedupe(CoreArgs a, const int4* 
                 if (!first) continue;
                 ++distinct;
                 atomicOr(&sw.fresh[2 * wl + (bit >> 5)], 1u << (bit & 31));
-                if (mult > 1) atomicSub(a.inRaw + i, mult - 1);
+                int corr = mult - 1;
+                if (hub && in_candidates_of(a, listMask, a.hubLists + h0, (int)(h1 - h0), i)) corr += 1;
+                if (corr) atomicSub(a.inRaw + i, corr);
             }
             __syncwarp();
             if (g < nWords) {
