@@ -134,11 +134,10 @@ __device__ __forceinline__ void set_k_mask(uint32_t* km, int l, bool on) {
     if (on) atomicOr(km + (l >> 5), 1u << (l & 31));
 }
 
-// Visits the passing slots of point p; f(jj, l, s, i, first, mult) on lanes.
-// Writes p's first-occurrence mask words when firstOut is given.
+// Visits the passing slots of point p, slot by slot; f(jj, l, s, i, first,
+// mult) on lanes (the sOPTICS list emission).
 template <typename F>
-__device__ __forceinline__ int visit_point(const CoreArgs& a, uint32_t* km, const int4* sig, int p,
-                                           uint64_t* firstOut, F&& f) {
+__device__ __forceinline__ void visit_point(const CoreArgs& a, uint32_t* km, const int4* sig, int p, F&& f) {
     const unsigned lane = lane_id();
     const int slots = 2 * a.k;
     const unsigned long long* mk64 = reinterpret_cast<const unsigned long long*>(a.masks);
@@ -156,7 +155,6 @@ __device__ __forceinline__ int visit_point(const CoreArgs& a, uint32_t* km, cons
     set_k_mask(km, lA, (int)lane < slots);
     set_k_mask(km, lB, (int)lane + 32 < slots);
     __syncwarp();
-    int distinct = 0;
     for (int jj = 0; jj < slots; ++jj) {
         const int src = jj & 31;
         const int l = __shfl_sync(0xffffffffu, jj < 32 ? lA : lB, src);
@@ -172,31 +170,18 @@ __device__ __forceinline__ int visit_point(const CoreArgs& a, uint32_t* km, cons
             } else {
                 mk = __ldg(mk64 + ((size_t)p * slots + jj) * a.W + wd);
             }
-            uint32_t fresh[2] = {0u, 0u};
             if (mk) {
 #pragma unroll
                 for (int half = 0; half < 2; ++half) {
                     const int bit = half * 32 + (int)lane;
-                    bool isFirst = false;
                     if ((mk >> bit) & 1ull) {
                         const int s = wd * 64 + bit;
                         const int i = __ldg(lst + s);
                         int mult;
+                        bool isFirst;
                         occurrence(a, km, sig, l, s, i, mult, isFirst);
                         f(jj, l, s, i, isFirst, mult);
-                        distinct += isFirst ? 1 : 0;
                     }
-                    fresh[half] = __ballot_sync(0xffffffffu, isFirst);
-                }
-            }
-            if (firstOut && lane == 0) {
-                const size_t at = ((size_t)p * slots + jj) * a.W + wd;
-                const uint64_t f64 = ((uint64_t)fresh[1] << 32) | fresh[0];
-                if (a.accumulate) {
-                    firstOut[at] |= f64;
-                    a.newMasks[at] = f64;
-                } else {
-                    firstOut[at] = f64;
                 }
             }
         }
@@ -205,7 +190,6 @@ __device__ __forceinline__ int visit_point(const CoreArgs& a, uint32_t* km, cons
     if ((int)lane < slots) km[lA >> 5] = 0u;
     if ((int)lane + 32 < slots) km[lB >> 5] = 0u;
     __syncwarp();
-    return warp_sum(distinct);
 }
 
 __device__ __forceinline__ void mark_lists(const CoreArgs& a, uint32_t* listMask, int64_t h0, int64_t h1,
@@ -365,7 +349,7 @@ __global__ void k_core_emit(CoreArgs a, const int4* __restrict__ sig, const int6
         if (lane == 0) *cursor = 0;
         __syncwarp();
         const int64_t row = nbOff[p];
-        visit_point(a, km, sig, p, nullptr, [&](int jj, int, int s, int i, bool first, int) {
+        visit_point(a, km, sig, p, [&](int jj, int, int s, int i, bool first, int) {
             if (!first) return;
             const float dd = a.dists[((size_t)p * 2 * a.k + jj) * a.m + s];
             const int pos = atomicAdd(cursor, 1);
