@@ -676,7 +676,7 @@ def run_ours(args, cfg):
     Xh_t.copy_(X)
     Xh = Xh_t.numpy()
     fit_host = eng.fit_soptics if optics else eng.fit_sdbscan
-    for _ in range(min(args.warmup, 2)):
+    for _ in range(max(2, args.warmup)):
         fit_host(Xh, cfg["eps"], cfg["minPts"])
         result()
     barrier()
