@@ -250,7 +250,10 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 5)) k_project(ProjectArgs
     // with cp.async while the current one is transformed
     const int xs = (a.d + 3) & ~3;
     float* xbuf = base + warps * rowLen + warps * a.nproj + (size_t)w * 2 * xs;
-    const bool vec16 = (a.ldx & 3) == 0 && (reinterpret_cast<uintptr_t>(a.X) & 15) == 0;
+    // 16-byte copies need whole 16-byte rows: L1 / L2 pass the padded Xt
+    // (ldx = ld, a multiple of 4) with any d, and d / 4 chunks would then
+    // leave the row's last d % 4 elements unstaged
+    const bool vec16 = (a.ldx & 3) == 0 && (a.d & 3) == 0 && (reinterpret_cast<uintptr_t>(a.X) & 15) == 0;
     auto fetch = [&](int pp, int b) {
         if (pp < min(a.n, (g + 1) * a.chunk)) {
             const float* src = a.X + (size_t)pp * a.ldx;
@@ -303,24 +306,59 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 5)) k_project(ProjectArgs
             // element, done in place on the warp's staged row by a rolled loop
             // (32 unrolled divisions made the body too large for the
             // instruction cache: 9.3 -> 8.2 ms at 1M x 784)
-            __nv_bfloat16* xb = a.Xb ? reinterpret_cast<__nv_bfloat16*>(a.Xb) + (size_t)p * a.ldb : nullptr;
             if (a.do_transform) {
                 float* xw = xbuf + buf * xs;
 #pragma unroll 1
                 for (int e = (int)l; e < a.d; e += 32) xw[e] = __fdiv_rn(xw[e], sc);
                 __syncwarp();
             }
+            // Xt row, zero padded to ld (a multiple of 4), 16 bytes per lane
+            // from the staged row; the staged chunk holding element d - 1 is
+            // the last one read, its elements past d are zeroed
+            {
+                const float4* x4 = reinterpret_cast<const float4*>(x);
+                float4* xt4 = reinterpret_cast<float4*>(a.Xt + (size_t)p * a.ld);
+#pragma unroll 1
+                for (int c = (int)l; c < a.ld / 4; c += 32) {
+                    float4 t = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (4 * c < a.d) {
+                        t = x4[c];
+                        if (4 * c + 1 >= a.d) t.y = 0.0f;
+                        if (4 * c + 2 >= a.d) t.z = 0.0f;
+                        if (4 * c + 3 >= a.d) t.w = 0.0f;
+                    }
+                    xt4[c] = t;
+                }
+            }
+            // the tensor-core copy (BF16, zero padded to ldb), 8 values per lane store
+            if (a.Xb) {
+                uint4* xb8 = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.Xb) + (size_t)p * a.ldb);
+#pragma unroll 1
+                for (int c = (int)l; c < a.ldb / 8; c += 32) {
+                    float f[8];
+                    if (8 * c + 8 <= a.d) {
+                        const float4 lo = reinterpret_cast<const float4*>(x)[2 * c];
+                        const float4 hi = reinterpret_cast<const float4*>(x)[2 * c + 1];
+                        f[0] = lo.x; f[1] = lo.y; f[2] = lo.z; f[3] = lo.w;
+                        f[4] = hi.x; f[5] = hi.y; f[6] = hi.z; f[7] = hi.w;
+                    } else {
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) f[u] = 8 * c + u < a.d ? x[8 * c + u] : 0.0f;
+                    }
+                    uint4 o;
+                    __nv_bfloat162 b;
+                    b = __floats2bfloat162_rn(f[0], f[1]); o.x = *reinterpret_cast<uint32_t*>(&b);
+                    b = __floats2bfloat162_rn(f[2], f[3]); o.y = *reinterpret_cast<uint32_t*>(&b);
+                    b = __floats2bfloat162_rn(f[4], f[5]); o.z = *reinterpret_cast<uint32_t*>(&b);
+                    b = __floats2bfloat162_rn(f[6], f[7]); o.w = *reinterpret_cast<uint32_t*>(&b);
+                    xb8[c] = o;
+                }
+            }
 #pragma unroll
             for (int j = 0; j < NJ; ++j) {
                 const int e = (int)l + 32 * j;
-                float t = 0.0f;
-                if (e < a.d) t = x[e];
-                if (e < a.ld) a.Xt[(size_t)p * a.ld + e] = t;
-                if (xb && e < a.ldb) xb[e] = __float2bfloat16_rn(t);  // the tensor-core copy, zero padded
-                v[j] = t;
+                v[j] = e < a.d ? x[e] : 0.0f;
             }
-            for (int e = (int)l + 32 * NJ; e < a.ld; e += 32)  // (the row is already divided)
-                a.Xt[(size_t)p * a.ld + e] = e < a.d ? x[e] : 0.0f;
         }
         for (int i = (int)l; EMB != 0 && i < a.ld; i += 32) {
             float t = 0.0f;
@@ -358,9 +396,10 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 5)) k_project(ProjectArgs
 #pragma unroll
             for (int j = 0; j < NJ; ++j)
                 v[j] = __int_as_float(__float_as_int(v[j]) ^ (int)((uint32_t)((sgn >> j) & 1u) << 31));
-#pragma unroll
-            for (int s = 1; s < 32; s <<= 1) {
-                if (s >= FD) break;
+            // (a rolled loop over the five cross-lane strides keeps the per-point
+            // loop body small: the kernel's top stall is instruction fetch)
+#pragma unroll 1
+            for (int s = 1; s < 32 && s < FD; s <<= 1) {
                 // lower element a: a + b; upper element b: a - b, i.e. fma(-1, b, a),
                 // exactly the reference's rounding either way
                 const float mul = (l & s) ? -1.0f : 1.0f;

@@ -375,6 +375,55 @@ def test_bf16_l2_screening_is_exact_on_its_candidates(port, n, d, ker, sigma, ep
     assert 0 < ocore.sum() < n
 
 
+def _ragged_case(dist, d, seed):
+    """Data, kernel width sigma and an eps for the ragged-dimension L1 / L2
+    cases: sigma = the median pairwise distance of 200 points, eps = the
+    median distance to the 20th nearest of 200 sampled points."""
+    from sdbscan_gb300 import datasets
+    X = datasets.cfg3_aniso_l2(6000, d, n_comp=8, scale=0.1, seed=seed)[0]
+    S = X[:200].astype(np.float64)
+    diff = S[:, None, :] - X[None, :, :].astype(np.float64)
+    D = np.abs(diff).sum(-1) if dist == "L1" else np.sqrt((diff ** 2).sum(-1))
+    sigma = float(np.median(D[:, :200][np.triu_indices(200, 1)]))
+    eps = float(np.median(np.sort(D, axis=1)[:, 20]))
+    return X, sigma, eps
+
+
+@pytest.mark.parametrize("dist,d,nproj,ker", [("L2", 30, 512, 256), ("L1", 19, 256, 256), ("L2", 17, 1024, 1024)])
+def test_rff_ragged_dims(port, dist, d, nproj, ker):
+    """L1 / L2 with d not a multiple of 4: the transformed rows are padded to
+    a multiple of 4 and the projection kernel stages them through shared
+    memory, the last d % 4 elements included.  Projections agree with the
+    oracle's to 1e-5 of the row norm (CUDA's cosf / sinf), and on the fit's
+    own top-k / top-m the neighbourhood sizes, core flags, labels and
+    n_clusters_ equal the oracle's bit for bit."""
+    from oracle.oracle import fht_dim
+    from sdbscan_gb300 import capi
+    X, sigma, eps = _ragged_case(dist, d, seed=61 + d)
+    n = X.shape[0]
+    eng = capi.Engine(n, d)
+    eng.set_params(n_proj=nproj, topK=5, topM=40, distance=dist, ker_n_features=ker, ker_sigma=sigma,
+                   random_seed=8)
+    eng.fit_sdbscan(X, eps, 10)
+    tK, tM = eng.topk(), eng.topm()
+    core, deg = eng.core()
+    labels, ncl = eng.labels()
+    P = eng.projections()
+    eng.close()
+    Xt, rc = port.transform(X, dist)
+    assert rc == 0
+    fd = fht_dim(nproj, ker)
+    oP = port.project(Xt, dist, ker, 0.4, port._R(dist, ker, d, sigma, 8), port.hd3_bits(3 * fd, 8), fd, nproj)
+    scale = np.linalg.norm(oP, axis=1, keepdims=True)
+    assert np.max(np.abs(P - oP) / scale) < 1e-5
+    ocore, odeg, olabels, oncl = port.core_cluster_lean(Xt, dist, tK, tM, eps, 10)
+    np.testing.assert_array_equal(deg, odeg)
+    np.testing.assert_array_equal(core, ocore)
+    np.testing.assert_array_equal(labels, olabels)
+    assert ncl == oncl
+    assert 0 < ocore.sum() < n
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_eps_sweep_equals_separate_fits(precision):
     """test_sDbscan's pattern (index and distances once, then per eps) gives
