@@ -155,8 +155,9 @@ struct ProjectArgs {
     int ldb;                 // its row stride, <= fhtDim
 };
 int launch_project(const ProjectArgs& a, cudaStream_t st);
-// Chunks in one full wave of k_project (a block per chunk, five blocks per SM).
-inline int project_wave_chunks() { return sm_count() * 5; }
+// Blocks in one full wave of k_project (six blocks per SM; each walks its
+// launch's chunks grid-stride).
+inline int project_wave_chunks() { return sm_count() * 6; }
 // transformData alone into Xt (uses X, ldx, Xt, ld, n, d, dist, scale, err).
 int launch_transform(const ProjectArgs& a, cudaStream_t st);
 

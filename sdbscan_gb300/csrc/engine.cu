@@ -213,10 +213,10 @@ sdb_status sdb_engine::fit(const float* X, bool xOnDevice, float eps, int minPts
     const int nct = (m + TNc - 1) / TNc;
     const int W = (m + 63) / 64;
     const int L = 2 * D;
-    // top-m threshold chunks: eight full waves of projection blocks (4 per
-    // SM; a wave or more per upload segment), and at least 4m chunks so the
-    // chunk maxima bound the m-th value
-    const int chunksWanted = std::max(sm_count() * 4 * 8, 4 * m);
+    // top-m threshold chunks: six chunks per projection block of one full
+    // wave (project_wave_chunks), so the grid-stride blocks end together, and
+    // at least 4m chunks so the chunk maxima bound the m-th value
+    const int chunksWanted = std::max(project_wave_chunks() * 6, 4 * m);
     const int chunk = std::max(8, (n + chunksWanted - 1) / chunksWanted);
     const int G = (n + chunk - 1) / chunk;
     int cap = 256;

@@ -230,7 +230,7 @@ __device__ bool warp_topk(const uint32_t (&key)[NJ], int nproj, int k, int32_t* 
 }
 
 template <int NJ, int EMB>
-__global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 5)) k_project(ProjectArgs a, const float* __restrict__ scale) {
+__global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 6)) k_project(ProjectArgs a, const float* __restrict__ scale) {
     extern __shared__ float smem[];
     const int warps = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
@@ -246,18 +246,20 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 5)) k_project(ProjectArgs
     __nv_bfloat162* ext = reinterpret_cast<__nv_bfloat162*>(base + warps * rowLen) + (size_t)w * a.nproj;
     const int gEnd = a.chunkEnd > 0 ? a.chunkEnd : (a.n + a.chunk - 1) / a.chunk;
     int g = a.chunkBase + blockIdx.x;  // the block's current chunk of points
-    // per-warp double buffer of input rows: the next point's row is fetched
-    // with cp.async while the current one is transformed
+    // per-warp input row buffer: the next point's row is fetched with
+    // cp.async as soon as the current one has been read, so it lands while
+    // the current point's rotations and top-k run (one buffer instead of two
+    // leaves room for six blocks per SM)
     const int xs = (a.d + 3) & ~3;
-    float* xbuf = base + warps * rowLen + warps * a.nproj + (size_t)w * 2 * xs;
+    float* xbuf = base + warps * rowLen + warps * a.nproj + (size_t)w * xs;
     // 16-byte copies need whole 16-byte rows: L1 / L2 pass the padded Xt
     // (ldx = ld, a multiple of 4) with any d, and d / 4 chunks would then
     // leave the row's last d % 4 elements unstaged
     const bool vec16 = (a.ldx & 3) == 0 && (a.d & 3) == 0 && (reinterpret_cast<uintptr_t>(a.X) & 15) == 0;
-    auto fetch = [&](int pp, int b) {
+    auto fetch = [&](int pp) {
         if (pp < min(a.n, (g + 1) * a.chunk)) {
             const float* src = a.X + (size_t)pp * a.ldx;
-            float* dst = xbuf + b * xs;
+            float* dst = xbuf;
             if (vec16) {
                 for (int c = (int)l; c < a.d / 4; c += 32) cp_async16(dst + 4 * c, src + 4 * c);
             } else {
@@ -291,14 +293,12 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 5)) k_project(ProjectArgs
     __syncwarp();
     const int p0 = g * a.chunk;
     const int p1 = min(a.n, p0 + a.chunk);
-    int buf = 0;
-    fetch(p0 + w, 0);
-    for (int p = p0 + w; p < p1; p += warps, buf ^= 1) {
-        fetch(p + warps, buf ^ 1);
+    fetch(p0 + w);
+    for (int p = p0 + w; p < p1; p += warps) {
         const float sc = scale[p];
-        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         __syncwarp();
-        const float* x = xbuf + buf * xs;  // this point's input row, in shared memory
+        const float* x = xbuf;  // this point's input row, in shared memory
         // transformed row -> Xt (zero padded to ld)
         float v[NJ];
         if (EMB == 0) {
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 5)) k_project(ProjectArgs
             // (32 unrolled divisions made the body too large for the
             // instruction cache: 9.3 -> 8.2 ms at 1M x 784)
             if (a.do_transform) {
-                float* xw = xbuf + buf * xs;
+                float* xw = xbuf;
 #pragma unroll 1
                 for (int e = (int)l; e < a.d; e += 32) xw[e] = __fdiv_rn(xw[e], sc);
                 __syncwarp();
@@ -369,6 +369,8 @@ __global__ void __launch_bounds__(128, (NJ >= 64 ? 1 : 5)) k_project(ProjectArgs
             a.Xt[(size_t)p * a.ld + i] = t;
             if (EMB == 2 && i < a.d) rowbuf[i] = t;
         }
+        __syncwarp();        // every lane is done with the staged row
+        fetch(p + warps);    // the next point's row
         if (EMB == 2) {
             // Chi2 / JS embedding (src/Utilities.h:132-208) into the warp's row
             // buffer, lane-strided, then picked up per register below.
@@ -640,13 +642,13 @@ int launch_project_nje(const ProjectArgs& a, const float* scale, cudaStream_t st
     const int warps = 4;
     const int G = (a.chunkEnd > 0 ? a.chunkEnd : (a.n + a.chunk - 1) / a.chunk) - a.chunkBase;
     if (G <= 0) return 0;
-    // one full wave of 5 blocks per SM; the blocks walk the launch's chunks grid-stride
+    // one full wave of 6 blocks per SM; the blocks walk the launch's chunks grid-stride
     const int grid = std::min(G, project_wave_chunks());
     const int nsw = (3 * a.fhtDim + 31) / 32;
     const int rowLen = EMB == 2 ? ((a.d + 3) & ~3) + a.fhtDim : 0;
     const size_t xs = (size_t)((a.d + 3) & ~3);
     size_t sm = sizeof(float) * (warps * 64 + ((nsw + 3) & ~3) + (size_t)warps * rowLen + (size_t)warps * a.nproj +
-                                 (size_t)warps * 2 * xs);
+                                 (size_t)warps * xs);
     if (sm > 227 * 1024) return -1;
     if (sm > 48 * 1024) {
         if (cudaFuncSetAttribute(k_project<NJ, EMB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
