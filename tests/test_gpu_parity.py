@@ -424,6 +424,67 @@ def test_rff_ragged_dims(port, dist, d, nproj, ker):
     assert 0 < ocore.sum() < n
 
 
+def _maxima_case(dist, n, d, seed):
+    """Data and eps for the engine-maxima cases: eps = the median distance to
+    the 15th nearest of 100 sampled points, on the transformed rows."""
+    from sdbscan_gb300 import datasets
+    if dist == "Chi2":
+        X = datasets.cfg2_mnist_like(n, d, n_comp=6, seed=seed)[0]
+        T = X / X.sum(1, keepdims=True)
+        S = T[:100].astype(np.float64)
+        D = np.empty((100, n))
+        for i in range(100):
+            a, b = S[i][None, :], T.astype(np.float64)
+            both = (a > 0) & (b > 0)
+            D[i] = 1.0 - 2.0 * np.where(both, a * b / np.where(both, a + b, 1.0), 0.0).sum(1)
+    else:
+        X = (datasets.cfg2_mnist_like(n, d, n_comp=6, seed=seed)[0] if d > 256
+             else datasets.cfg1_cosine(n, d, seed=seed)[0])
+        T = X / np.linalg.norm(X, axis=1, keepdims=True)
+        D = 1.0 - T[:100].astype(np.float64) @ T.astype(np.float64).T
+    return X, float(np.median(np.sort(D, axis=1)[:, 15]))
+
+
+@pytest.mark.parametrize("dist,n,d,nproj,ker,k,m", [
+    ("Cosine", 3000, 1500, 256, None, 5, 20),   # 2048-point rotations from d: the register kernel's widest form
+    ("Cosine", 4000, 64, 2048, None, 31, 100),  # n_proj 2048 and topK 31 (the engine's maxima), two mask words
+    ("Chi2", 2000, 1024, 256, 2048, 5, 20),     # 2048-point rotations from the Chi2 embedding (square roots only)
+])
+def test_engine_maxima_match_oracle(port, dist, n, d, nproj, ker, k, m):
+    """The widest register projection kernel (2048-element rotation vectors,
+    64 per lane), the largest n_proj and topK, and top-m lists over two mask
+    words: projections bit-exact against the oracle, top-k / top-m sets equal
+    to the oracle's under the engine's tie rule, and neighbourhood sizes, core
+    flags, labels and n_clusters_ bit-exact."""
+    from oracle.oracle import fht_dim
+    from sdbscan_gb300 import capi
+    X, eps = _maxima_case(dist, n, d, seed=nproj + d)
+    kw = dict(ker_n_features=ker) if ker else {}
+    eng = capi.Engine(n, d)
+    eng.set_params(n_proj=nproj, topK=k, topM=m, distance=dist, random_seed=13, **kw)
+    eng.fit_sdbscan(X, eps, 10)
+    P, tK, tM = eng.projections(), eng.topk(), eng.topm()
+    core, deg = eng.core()
+    labels, ncl = eng.labels()
+    eng.close()
+    Xt, rc = port.transform(X, dist)
+    assert rc == 0
+    kk = ker or d
+    fd = fht_dim(nproj, kk)
+    assert fd == 2048
+    oP = port.project(Xt, dist, kk, 0.4, None, port.hd3_bits(3 * fd, 13), fd, nproj)
+    np.testing.assert_array_equal(P, oP)
+    oK, oM = port.topk_canon(oP, k), port.topm_canon(oP, m)
+    np.testing.assert_array_equal(_sorted_rows(tK), _sorted_rows(oK))
+    np.testing.assert_array_equal(_sorted_rows(tM), _sorted_rows(oM))
+    ocore, odeg, olabels, oncl = port.core_cluster_lean(Xt, dist, oK, oM, eps, 10)
+    np.testing.assert_array_equal(deg, odeg)
+    np.testing.assert_array_equal(core, ocore)
+    np.testing.assert_array_equal(labels, olabels)
+    assert ncl == oncl
+    assert 0 < ocore.sum() < n
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_eps_sweep_equals_separate_fits(precision):
     """test_sDbscan's pattern (index and distances once, then per eps) gives
