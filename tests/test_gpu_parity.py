@@ -320,6 +320,8 @@ def test_fit_soptics_matches_oracle(port, n, d, k, m, eps, minPts):
     ("vmf", 3000, 64, 5, 20, 0.15, 10),
     ("vmf", 30000, 128, 5, 50, 0.15, 20),
     ("mnist", 20000, 784, 10, 50, 0.25, 50),
+    ("vmf", 6000, 30, 5, 20, 0.02, 10),     # d % 4 != 0: rows staged element-wise, BF16 rows end mid-chunk
+    ("mnist", 8000, 100, 8, 40, 0.25, 20),  # d % 8 == 4: the BF16 row's last 8-value store is partly padding
 ])
 def test_bf16_screening_equals_plain(gen, n, d, k, m, eps, minPts):
     """BF16 tensor-core screening with FP32 re-decision near eps gives the
@@ -477,6 +479,47 @@ def test_engine_maxima_match_oracle(port, dist, n, d, nproj, ker, k, m):
     oK, oM = port.topk_canon(oP, k), port.topm_canon(oP, m)
     np.testing.assert_array_equal(_sorted_rows(tK), _sorted_rows(oK))
     np.testing.assert_array_equal(_sorted_rows(tM), _sorted_rows(oM))
+    ocore, odeg, olabels, oncl = port.core_cluster_lean(Xt, dist, oK, oM, eps, 10)
+    np.testing.assert_array_equal(deg, odeg)
+    np.testing.assert_array_equal(core, ocore)
+    np.testing.assert_array_equal(labels, olabels)
+    assert ncl == oncl
+    assert 0 < ocore.sum() < n
+
+
+@pytest.mark.parametrize("dist,d", [("Chi2", 30), ("Chi2", 61)])
+def test_chi2_ragged_dims_bit_exact(port, dist, d):
+    """Chi2 with d not a multiple of 4 (rows staged element by element, the
+    embedding's row buffer padded to a multiple of 4) and ker_n_features = the
+    next multiple of 32 (square-root terms only): projections bit-exact, top-k
+    / top-m sets equal to the oracle's under the engine's tie rule, sizes,
+    core flags, labels and n_clusters_ bit-exact."""
+    from oracle.oracle import fht_dim
+    from sdbscan_gb300 import capi, datasets
+    n, nproj, k, m, ker = 5000, 256, 5, 20, (d + 31) // 32 * 32
+    X = datasets.cfg2_mnist_like(n, d, n_comp=6, seed=90 + d)[0]
+    Xt, rc = port.transform(X, dist)
+    assert rc == 0
+    fd = fht_dim(nproj, ker)
+    oP = port.project(Xt, dist, ker, 0.4, None, port.hd3_bits(3 * fd, 21), fd, nproj)
+    oK, oM = port.topk_canon(oP, k), port.topm_canon(oP, m)
+    # eps: the median distance to the 15th nearest of 100 sampled points
+    S, T = Xt[:100].astype(np.float64), Xt.astype(np.float64)
+    D = np.empty((100, n))
+    for i in range(100):
+        a, b = S[i][None, :], T
+        both = (a > 0) & (b > 0)
+        D[i] = 1.0 - 2.0 * np.where(both, a * b / np.where(both, a + b, 1.0), 0.0).sum(1)
+    eps = float(np.median(np.sort(D, axis=1)[:, 15]))
+    eng = capi.Engine(n, d)
+    eng.set_params(n_proj=nproj, topK=k, topM=m, distance=dist, ker_n_features=ker, random_seed=21)
+    eng.fit_sdbscan(X, eps, 10)
+    np.testing.assert_array_equal(eng.projections(), oP)
+    np.testing.assert_array_equal(_sorted_rows(eng.topk()), _sorted_rows(oK))
+    np.testing.assert_array_equal(_sorted_rows(eng.topm()), _sorted_rows(oM))
+    core, deg = eng.core()
+    labels, ncl = eng.labels()
+    eng.close()
     ocore, odeg, olabels, oncl = port.core_cluster_lean(Xt, dist, oK, oM, eps, 10)
     np.testing.assert_array_equal(deg, odeg)
     np.testing.assert_array_equal(core, ocore)
