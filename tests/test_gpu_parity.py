@@ -296,7 +296,8 @@ def test_fit_soptics_matches_reference(port, path):
         np.testing.assert_array_equal(reach, o_reach)
 
 
-@pytest.mark.parametrize("n,d,k,m,eps,minPts", [(8000, 64, 5, 30, 0.2, 10), (6000, 196, 10, 50, 0.25, 30)])
+@pytest.mark.parametrize("n,d,k,m,eps,minPts", [(8000, 64, 5, 30, 0.2, 10), (6000, 196, 10, 50, 0.25, 30),
+                                                (5000, 30, 5, 20, 0.02, 10)])  # d % 4 != 0
 def test_fit_soptics_matches_oracle(port, n, d, k, m, eps, minPts):
     from sdbscan_gb300 import capi, datasets
     if d == 196:
@@ -487,16 +488,18 @@ def test_engine_maxima_match_oracle(port, dist, n, d, nproj, ker, k, m):
     assert 0 < ocore.sum() < n
 
 
-@pytest.mark.parametrize("dist,d", [("Chi2", 30), ("Chi2", 61)])
-def test_chi2_ragged_dims_bit_exact(port, dist, d):
-    """Chi2 with d not a multiple of 4 (rows staged element by element, the
-    embedding's row buffer padded to a multiple of 4) and ker_n_features = the
-    next multiple of 32 (square-root terms only): projections bit-exact, top-k
-    / top-m sets equal to the oracle's under the engine's tie rule, sizes,
-    core flags, labels and n_clusters_ bit-exact."""
+@pytest.mark.parametrize("dist,d", [("Chi2", 30), ("Chi2", 61), ("Cosine", 30), ("Cosine", 45)])
+def test_ragged_dims_bit_exact(port, dist, d):
+    """Cosine and Chi2 with d not a multiple of 4: rows staged element by
+    element, Xt written from the staged row with its padding zeroed, and for
+    Chi2 the embedding's row buffer padded to a multiple of 4, with
+    ker_n_features = the next multiple of 32 (square-root terms only).
+    Projections bit-exact, top-k / top-m sets equal to the oracle's under the
+    engine's tie rule, sizes, core flags, labels and n_clusters_ bit-exact."""
     from oracle.oracle import fht_dim
     from sdbscan_gb300 import capi, datasets
-    n, nproj, k, m, ker = 5000, 256, 5, 20, (d + 31) // 32 * 32
+    n, nproj, k, m = 5000, 256, 5, 20
+    ker = (d + 31) // 32 * 32 if dist == "Chi2" else d
     X = datasets.cfg2_mnist_like(n, d, n_comp=6, seed=90 + d)[0]
     Xt, rc = port.transform(X, dist)
     assert rc == 0
@@ -505,14 +508,18 @@ def test_chi2_ragged_dims_bit_exact(port, dist, d):
     oK, oM = port.topk_canon(oP, k), port.topm_canon(oP, m)
     # eps: the median distance to the 15th nearest of 100 sampled points
     S, T = Xt[:100].astype(np.float64), Xt.astype(np.float64)
-    D = np.empty((100, n))
-    for i in range(100):
-        a, b = S[i][None, :], T
-        both = (a > 0) & (b > 0)
-        D[i] = 1.0 - 2.0 * np.where(both, a * b / np.where(both, a + b, 1.0), 0.0).sum(1)
+    if dist == "Chi2":
+        D = np.empty((100, n))
+        for i in range(100):
+            a, b = S[i][None, :], T
+            both = (a > 0) & (b > 0)
+            D[i] = 1.0 - 2.0 * np.where(both, a * b / np.where(both, a + b, 1.0), 0.0).sum(1)
+    else:
+        D = 1.0 - S @ T.T
     eps = float(np.median(np.sort(D, axis=1)[:, 15]))
     eng = capi.Engine(n, d)
-    eng.set_params(n_proj=nproj, topK=k, topM=m, distance=dist, ker_n_features=ker, random_seed=21)
+    kw = dict(ker_n_features=ker) if dist == "Chi2" else {}
+    eng.set_params(n_proj=nproj, topK=k, topM=m, distance=dist, random_seed=21, **kw)
     eng.fit_sdbscan(X, eps, 10)
     np.testing.assert_array_equal(eng.projections(), oP)
     np.testing.assert_array_equal(_sorted_rows(eng.topk()), _sorted_rows(oK))
