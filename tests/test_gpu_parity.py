@@ -323,6 +323,8 @@ def test_fit_soptics_matches_oracle(port, n, d, k, m, eps, minPts):
     ("mnist", 20000, 784, 10, 50, 0.25, 50),
     ("vmf", 6000, 30, 5, 20, 0.02, 10),     # d % 4 != 0: rows staged element-wise, BF16 rows end mid-chunk
     ("mnist", 8000, 100, 8, 40, 0.25, 20),  # d % 8 == 4: the BF16 row's last 8-value store is partly padding
+    ("mnist", 8000, 196, 6, 100, 0.25, 20),  # topM 100: two 64-column candidate tiles per list
+    ("vmf", 5000, 64, 31, 70, 0.15, 10),     # topK 31 (62 slots per point) with two candidate tiles
 ])
 def test_bf16_screening_equals_plain(gen, n, d, k, m, eps, minPts):
     """BF16 tensor-core screening with FP32 re-decision near eps gives the
